@@ -1,0 +1,214 @@
+"""Generate the golden vectors that pin the oracle and the synthetic-state builder.
+
+Runs the Veros reference NumPy backend (``/root/reference``) in this process,
+so it only works where that checkout exists; the ``.npz`` files it writes are
+committed and the tests read only those. Usage::
+
+    python tests/golden/make_golden.py [/path/to/veros/checkout]
+
+``loguru`` is not installed here, so a no-op stand-in module is registered
+before Veros is imported (Veros only logs through it).
+
+Cases (all float64, reference layout):
+
+* ``iso_random_*``: the reference's own random-state fixture
+  (veros/pyom_compat.py:487-526, seeded like test/conftest.py:31-35) at a small
+  size with the settings of test/pyom_consistency/isoneutral_test.py:9-19;
+  every variable, including the outputs' untouched cells, starts random.
+  Runs pre, diffusion of temp and salt (energy branch on) and skew diffusion.
+* ``iso_synth_eq1`` / ``iso_synth_eq3``: ``veros_gb300.synthetic.make_state``
+  states run through the reference pre + diffusion(temp) + diffusion(salt).
+* ``tridiag_random``: the reference's tridiagonal test form
+  (test/pyom_consistency/tridiag_test.py:40-67) at a small size.
+* ``grid_topo``: reference ``numerics.calc_grid`` / ``calc_topo`` outputs for the
+  spacings and ``kbot`` the synthetic builder uses.
+"""
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def _import_reference(path):
+    class _NoLog:
+        def patch(self, *a, **k):
+            return self
+
+        def opt(self, *a, **k):
+            return self
+
+        def __getattr__(self, name):
+            return lambda *a, **k: None
+
+    mod = types.ModuleType("loguru")
+    mod.logger = _NoLog()
+    sys.modules.setdefault("loguru", mod)
+    sys.path.insert(0, path)
+    os.environ["VEROS_BACKEND"] = "numpy"
+    import veros  # noqa: F401
+
+
+PRE_FIELDS = ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "K_11", "K_22", "K_33")
+INPUT_FIELDS = (
+    "dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt", "kbot",
+    "maskT", "maskU", "maskV", "maskW", "temp", "salt", "K_iso", "K_gm",
+    "int_drhodT", "int_drhodS", "dtemp_iso", "dsalt_iso", "P_diss_iso", "P_diss_skew",
+) + PRE_FIELDS
+SETTING_KEYS = ("iso_slopec", "iso_dslope", "K_iso_steep", "dt_tracer", "grav", "rho_0",
+                "eq_of_state_type", "enable_conserve_energy")
+
+
+def _snapshot(vs, names):
+    return {n: np.array(getattr(vs, n)).copy() for n in names}
+
+
+def _settings_blob(settings):
+    return {f"setting_{k}": np.array(getattr(settings, k)) for k in SETTING_KEYS}
+
+
+def _run_iso_chain(state, with_skew):
+    from veros.core import isoneutral
+
+    vs = state.variables
+    out = {}
+    vs.update(isoneutral.isoneutral_diffusion_pre(state))
+    out.update({f"pre_{k}": np.array(getattr(vs, k)).copy() for k in PRE_FIELDS})
+    isoneutral.isoneutral_diffusion(state, vs.temp, True)
+    for k in ("temp", "dtemp_iso", "P_diss_iso"):
+        out[f"diffT_{k}"] = np.array(getattr(vs, k)).copy()
+    isoneutral.isoneutral_diffusion(state, vs.salt, False)
+    for k in ("salt", "dsalt_iso", "P_diss_iso"):
+        out[f"diffS_{k}"] = np.array(getattr(vs, k)).copy()
+    if with_skew:
+        isoneutral.isoneutral_skew_diffusion(state, vs.temp, True)
+        for k in ("temp", "dtemp_iso", "P_diss_skew"):
+            out[f"skewT_{k}"] = np.array(getattr(vs, k)).copy()
+    return out
+
+
+def make_random_case(nx, ny, nz, conserve_energy):
+    from veros.pyom_compat import get_random_state
+
+    np.random.seed(17)
+    settings = dict(nx=nx, ny=ny, nz=nz, dt_tracer=3600, dt_mom=3600, enable_neutral_diffusion=True,
+                    enable_skew_diffusion=True, enable_TEM_friction=True, K_iso_steep=1,
+                    enable_conserve_energy=conserve_energy)
+    state = get_random_state(extra_settings=settings)
+    vs = state.variables
+    blob = {f"in_{k}": v for k, v in _snapshot(vs, INPUT_FIELDS).items()}
+    blob.update(_settings_blob(state.settings))
+    blob.update(tau=np.array(vs.tau), taup1=np.array(vs.taup1), taum1=np.array(vs.taum1))
+    blob.update(_run_iso_chain(state, with_skew=True))
+    return blob
+
+
+def _reference_state_from_host(host):
+    from veros.state import get_default_state
+
+    state = get_default_state()
+    s = host.settings
+    with state.settings.unlock():
+        state.settings.update(
+            nx=host.nx, ny=host.ny, nz=host.nz, enable_neutral_diffusion=True, coord_degree=True,
+            **{k: s[k] for k in SETTING_KEYS},
+        )
+    state.initialize_variables()
+    state.variables.__locked__ = False
+    vs = state.variables
+    for name in INPUT_FIELDS:
+        setattr(vs, name, host.arrays[name])
+    return state
+
+
+def make_synth_case(seed, eq_type, conserve_energy, sigma):
+    sys.path.insert(0, REPO)
+    from veros_gb300.synthetic import make_state
+
+    host = make_state(16, 12, 10, seed=seed, y_origin=-60.0, dz_top=10.0, dz_bottom=400.0,
+                      land_fraction=0.2, eq_of_state_type=eq_type, k_iso_lognormal_sigma=sigma,
+                      settings=dict(enable_conserve_energy=conserve_energy))
+    state = _reference_state_from_host(host)
+    vs = state.variables
+    blob = {f"in_{k}": v for k, v in _snapshot(vs, INPUT_FIELDS).items()}
+    blob.update(_settings_blob(state.settings))
+    blob.update(tau=np.array(vs.tau), taup1=np.array(vs.taup1), taum1=np.array(vs.taum1))
+    blob.update(_run_iso_chain(state, with_skew=False))
+    return blob
+
+
+def make_tridiag_case():
+    from veros.core.operators import solve_tridiagonal_numpy
+    from veros.core.utilities import create_water_masks, solve_implicit
+
+    np.random.seed(17)
+    nx, ny, nz = 12, 10, 16
+    a, b, c, d = (np.random.randn(nx, ny, nz) for _ in range(4))
+    kbot = np.random.randint(0, nz, size=(nx, ny))
+    _, water_mask, edge_mask = create_water_masks(kbot, nz)
+    out_random = solve_tridiagonal_numpy(a, b, c, d, water_mask, edge_mask)
+    # diagonally dominant systems of the implicit-mixing form, with b_edge/d_edge substitution
+    delta = np.abs(np.random.randn(nx, ny, nz)) * 3.0
+    ad = -delta
+    cd = -np.roll(delta, -1, axis=-1)
+    bd = 1.0 + delta + np.roll(delta, -1, axis=-1)
+    b_edge = 1.0 + np.abs(np.random.randn(nx, ny, nz))
+    d_edge = np.random.randn(nx, ny, nz)
+    out_dd = solve_implicit(ad, bd, cd, d, water_mask, edge_mask, b_edge=b_edge, d_edge=d_edge)
+    return dict(a=a, b=b, c=c, d=d, kbot=kbot, water_mask=water_mask, edge_mask=edge_mask, out_random=out_random,
+                ad=ad, bd=bd, cd=cd, b_edge=b_edge, d_edge=d_edge, out_dd=out_dd)
+
+
+def make_grid_case():
+    sys.path.insert(0, REPO)
+    from veros.core import numerics
+    from veros.state import get_default_state
+    from veros_gb300.synthetic import geometric_dz
+
+    nx, ny, nz = 14, 11, 9
+    rng = np.random.default_rng(5)
+    dxt = np.full(nx + 4, 1.0) * (1 + 0.01 * rng.standard_normal(nx + 4))
+    dyt = np.full(ny + 4, 1.0) * (1 + 0.01 * rng.standard_normal(ny + 4))
+    dzt = geometric_dz(nz, 10.0, 400.0)
+    kbot = np.zeros((nx + 4, ny + 4), dtype=np.int32)
+    kbot[1:-1, 1:-1] = rng.integers(0, nz + 1, size=(nx + 2, ny + 2))
+
+    state = get_default_state()
+    with state.settings.unlock():
+        state.settings.update(nx=nx, ny=ny, nz=nz, coord_degree=True, x_origin=0.0, y_origin=-60.0)
+    state.initialize_variables()
+    state.variables.__locked__ = False
+    vs = state.variables
+    vs.dxt, vs.dyt, vs.dzt, vs.kbot = dxt, dyt, dzt, kbot
+    numerics.calc_grid(state)
+    numerics.calc_topo(state)
+    names = ("dxt", "dxu", "xt", "xu", "dyt", "dyu", "yt", "yu", "dzt", "dzw", "zt", "zw", "cost", "cosu",
+             "kbot", "maskT", "maskU", "maskV", "maskW")
+    blob = {f"out_{n}": np.array(getattr(vs, n)).copy() for n in names}
+    blob.update(in_dxt=dxt, in_dyt=dyt, in_dzt=dzt, in_kbot=kbot, nx=np.array(nx), ny=np.array(ny), nz=np.array(nz))
+    return blob
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    _import_reference(ref)
+    cases = {
+        "iso_random_energy": make_random_case(12, 10, 8, True),
+        "iso_random_noenergy": make_random_case(10, 9, 7, False),
+        "iso_synth_eq1": make_synth_case(0, 1, False, None),
+        "iso_synth_eq3": make_synth_case(1, 3, True, 0.3),
+        "tridiag": make_tridiag_case(),
+        "grid_topo": make_grid_case(),
+    }
+    for name, blob in cases.items():
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **blob)
+        print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+if __name__ == "__main__":
+    main()
