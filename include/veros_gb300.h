@@ -1,0 +1,171 @@
+/*
+ * veros_gb300 — C ABI of the GB300 (sm_103a) isoneutral mixing path.
+ *
+ * Plain pointers and sizes; no framework types. Every entry point returns an
+ * int status (VG_OK on success) and never exits the process; the message of
+ * the last failure on the calling thread is available from vg_last_error().
+ * All work is enqueued on the caller's CUDA stream (passed as void*, a
+ * cudaStream_t; NULL = legacy default stream) and no call synchronises the
+ * host, except where stated.
+ *
+ * Device layout of one domain ("canonical layout"): a 3-D field f(i, j, k)
+ * with i in [0, X), j in [0, Y), k in [0, Z) lives at
+ *     base[i + j * pitch + k * plane]
+ * (x fastest). X = nx + 4 and Y = ny + 4 include the two halo cells on each
+ * side; k = 0 is the bottom level. Fields with a time axis are passed as the
+ * pointer of one level. The (2, 2) tensors Ai_* hold component (p, r)
+ * (p = ip or jp, r = kr) at base + p * ai_stride_p + r * ai_stride_r.
+ * kbot is an int32 (X, Y) plane with the same pitch. The four boolean masks
+ * are packed into one byte per cell (bit 0 T, bit 1 U, bit 2 V, bit 3 W).
+ */
+#ifndef VEROS_GB300_H
+#define VEROS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  VG_OK = 0,
+  VG_ERR_SHAPE = 1,       /* extents out of range or inconsistent */
+  VG_ERR_STRIDE = 2,      /* pitch/plane/component strides not usable */
+  VG_ERR_ARG = 3,         /* NULL pointer or bad flag */
+  VG_ERR_LAUNCH = 4,      /* CUDA launch or runtime error */
+  VG_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  VG_ERR_UNSUPPORTED = 6, /* setting outside what the kernels implement */
+  VG_ERR_SCRATCH = 7      /* scratch buffer too small */
+};
+
+#define VG_MASK_T 1u
+#define VG_MASK_U 2u
+#define VG_MASK_V 4u
+#define VG_MASK_W 8u
+
+typedef struct VgDomain {
+  int X, Y, Z;          /* extents including halos */
+  long long pitch;      /* elements between consecutive j rows (>= X) */
+  long long plane;      /* elements between consecutive k levels (>= pitch * Y) */
+} VgDomain;
+
+typedef struct VgGrid {
+  const double *dxt, *dxu;               /* length X */
+  const double *dyt, *dyu, *cost, *cosu; /* length Y */
+  const double *dzt, *dzw, *zt;          /* length Z */
+} VgGrid;
+
+typedef struct VgIsoSettings {
+  double iso_slopec, iso_dslope, K_iso_steep, dt_tracer, grav, rho_0;
+  int eq_of_state_type;        /* 1..4 */
+  int enable_conserve_energy;  /* 0/1 */
+} VgIsoSettings;
+
+typedef struct VgTensorFields {
+  double *K_11, *K_22, *K_33;
+  double *Ai_ez, *Ai_nz, *Ai_bx, *Ai_by;
+  long long ai_stride_p, ai_stride_r;
+} VgTensorFields;
+
+typedef struct VgTracerArgs {
+  const double *tr_tau;         /* tracer at level tau (read) */
+  double *tr_taup1;             /* tracer at level taup1 (read, updated) */
+  double *dtracer_iso;          /* dtemp_iso or dsalt_iso (updated) */
+  const double *int_drhodX_tau; /* int_drhodT or int_drhodS at tau; energy branch only */
+  double *P_diss;               /* P_diss_iso (iso) or P_diss_skew (skew); energy branch only */
+} VgTracerArgs;
+
+/* Message of the last failure on this thread ("" if none). */
+const char *vg_last_error(void);
+/* Library version string. */
+const char *vg_version(void);
+
+/* Pack four bool (0/1 byte) masks in canonical layout into the mask byte plane.
+ * No reference counterpart: Veros keeps maskT/U/V/W as separate bool arrays
+ * (veros/variables.py:255-292); packing is this library's layout choice. */
+int vg_pack_masks(const VgDomain *dom, const uint8_t *maskT, const uint8_t *maskU,
+                  const uint8_t *maskV, const uint8_t *maskW, uint8_t *mask_bits, void *stream);
+
+/* Replaces veros.core.isoneutral.isoneutral_diffusion_pre
+ * (veros/core/isoneutral/isoneutral.py:18-229): slopes, taper and the
+ * diffusion tensor. Writes K_11[1:-2,2:-2,:], K_22[2:-2,1:-2,:],
+ * K_33[2:-2,2:-2,:-1] and K_33[...,-1] = 0, Ai_ez/Ai_nz/Ai_bx/Ai_by on the
+ * reference's sub-ranges; every other cell of the outputs is left untouched. */
+int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                          const double *temp_tau, const double *salt_tau, const double *K_iso,
+                          const uint8_t *mask_bits, const VgTensorFields *out, void *stream);
+
+/* Scratch bytes vg_isoneutral_diffusion_f64 needs for one domain. */
+size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom);
+
+/* Replaces veros.core.isoneutral.isoneutral_diffusion (skew = 0,
+ * veros/core/isoneutral/diffusion.py:286-295) and isoneutral_skew_diffusion
+ * (skew = 1, :298-307) through isoneutral_diffusion_kernel (:210-283):
+ * explicit flux divergence, implicit vertical K_33 solve (iso only),
+ * dtracer_iso update and, when enable_conserve_energy, the P_diss update.
+ * K_field is K_iso (iso) or K_gm (skew). */
+int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                const VgTensorFields *ten, const double *K_field,
+                                const uint8_t *mask_bits, const int32_t *kbot,
+                                const VgTracerArgs *tr, int skew,
+                                void *scratch, size_t scratch_bytes, void *stream);
+
+/* Fields of one rollout step (vg_isoneutral_step_f64). */
+typedef struct VgStepFields {
+  const double *temp_tau;
+  double *temp_taup1;
+  const double *salt_tau;
+  double *salt_taup1;
+  const double *K_iso;
+  const uint8_t *mask_bits;
+  const int32_t *kbot;
+  VgTensorFields ten;
+  double *dtemp_iso, *dsalt_iso;
+  const double *int_drhodT_tau, *int_drhodS_tau; /* energy branch only */
+  double *P_diss_iso;                            /* may be NULL without the energy branch */
+} VgStepFields;
+
+/* One isoneutral step as the reference's caller runs it
+ * (veros/core/thermodynamics.py:226-241 with zero advection, then :425-432):
+ * tr[taup1] = tr[tau] * maskT for temp and salt; dtemp_iso = dsalt_iso = 0
+ * and P_diss_iso = 0 (if given; needed with the energy branch); pre; diffusion of temp; diffusion
+ * of salt. The caller rotates the time levels (veros/veros.py:321-322).
+ * Scratch as for vg_isoneutral_diffusion_f64. */
+int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                           const VgStepFields *f, void *scratch, size_t scratch_bytes, void *stream);
+
+/* First stage of vg_isoneutral_step_f64 alone (new time level and zeroed
+ * tendencies), for callers that time or interleave the stages. */
+int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, void *stream);
+
+/* Replaces veros.core.utilities.solve_implicit (veros/core/utilities.py:51-59)
+ * and veros.core.operators.solve_tridiagonal (veros/core/operators.py:60-77,
+ * :102-156). nsys columns of nz levels; element (s, k) of every array is at
+ * s_x * (s % nsx) + s_y * (s / nsx) + s_z * k with nsys = nsx * nsy.
+ * water/edge are 0/1 bytes as produced by create_water_masks
+ * (veros/core/utilities.py:38-48): per column, water is k >= ks and edge is
+ * k == ks. b_edge/d_edge may be NULL. Outside water the output is 0.
+ * Columns whose masks do not have that form are counted into *bad_columns
+ * (device int, may be NULL) and solved over their water cells only.
+ * Elimination uses partial pivoting, as LAPACK dgtsv does. */
+int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, long long s_y, long long s_z,
+                          const double *a, const double *b, const double *c, const double *d,
+                          const uint8_t *water, const uint8_t *edge,
+                          const double *b_edge, const double *d_edge, double *out,
+                          int *bad_columns, void *stream);
+
+/* Drop-in for the XLA GPU custom-call targets tdma_cuda_double / tdma_cuda_float
+ * (veros/core/special/cuda_tdma_kernels.cu:103-111, registered in
+ * veros/core/special/tdma_.py:35-37): buffers = {a, b, c, d, out, workspace},
+ * opaque = {int num_systems; int system_depth}, operands system-fastest
+ * ((k, s) at k * num_systems + s). On error the message is kept for
+ * vg_last_error() instead of exiting the process. The workspace is not used. */
+void vg_tdma_cuda_double(void *stream, void **buffers, const char *opaque, size_t opaque_len);
+void vg_tdma_cuda_float(void *stream, void **buffers, const char *opaque, size_t opaque_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VEROS_GB300_H */

@@ -1,0 +1,80 @@
+// Shared helpers of the veros_gb300 CUDA library: status handling, layout
+// indexing and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/veros_gb300.h"
+
+namespace vg {
+
+// Sets the thread's last-error message and returns `code`.
+int fail(int code, const char *fmt, ...);
+void clear_error();
+
+// Converts a CUDA error after a launch into a status.
+inline int check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "%s: %s", what, cudaGetErrorString(e));
+  return VG_OK;
+}
+
+int validate_domain(const VgDomain *dom);
+
+struct Layout {
+  int X, Y, Z;
+  long long pitch, plane;
+  __host__ __device__ __forceinline__ long long at(int i, int j, int k) const {
+    return (long long)i + (long long)j * pitch + (long long)k * plane;
+  }
+  __host__ __device__ __forceinline__ long long at2(int i, int j) const {
+    return (long long)i + (long long)j * pitch;
+  }
+};
+
+inline Layout layout_of(const VgDomain *d) { return Layout{d->X, d->Y, d->Z, d->pitch, d->plane}; }
+
+struct Grid {
+  const double *dxt, *dxu, *dyt, *dyu, *cost, *cosu, *dzt, *dzw, *zt;
+};
+
+inline Grid grid_of(const VgGrid *g) {
+  return Grid{g->dxt, g->dxu, g->dyt, g->dyu, g->cost, g->cosu, g->dzt, g->dzw, g->zt};
+}
+
+inline bool grid_complete(const VgGrid *g) {
+  return g && g->dxt && g->dxu && g->dyt && g->dyu && g->cost && g->cosu && g->dzt && g->dzw && g->zt;
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Equation-of-state derivatives for eq types 1-4
+// (veros/core/density/linear_eq.py:36-43, nonlinear_eq1.py:39-47,
+//  nonlinear_eq2.py:57-66, nonlinear_eq3.py:39-47).
+struct Eos {
+  int type;
+  static constexpr double rho0 = 1024.0;
+  static constexpr double theta0 = 283.0 - 273.15;
+  static constexpr double betaT = 1.67e-4;
+  static constexpr double betaS = 0.78e-3;
+  static constexpr double betaTs3 = 1e-5;
+  static constexpr double betaTs24 = 1e-5 / 2.0;
+  static constexpr double gammas = 1.1e-8;
+  static constexpr double grav = 9.81;
+
+  __device__ __forceinline__ double drdT(double T, double zt) const {
+    if (type == 1) return -betaT * rho0;
+    if (type == 3) {
+      double zz = -fabs(zt) - 0.0;
+      double thetas = T - theta0;
+      return -(betaTs3 * thetas + betaT * (1.0 - gammas * grav * zz * rho0)) * rho0;
+    }
+    return -(betaT + 2.0 * betaTs24 * (T - theta0)) * rho0;  // types 2 and 4
+  }
+  __device__ __forceinline__ double drdS() const { return type == 4 ? 0.0 * rho0 : betaS * rho0; }
+};
+
+}  // namespace vg

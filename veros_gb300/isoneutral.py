@@ -1,0 +1,138 @@
+"""Drop-ins for ``veros.core.isoneutral`` on the GB300 CUDA library.
+
+Same call signatures as the reference:
+
+* ``isoneutral_diffusion_pre(state) -> KernelOutput(Ai_ez, Ai_nz, Ai_bx, Ai_by, K_11, K_22, K_33)``
+  (veros/core/isoneutral/isoneutral.py:18-229)
+* ``isoneutral_diffusion(state, tr, istemp) -> None``
+  (veros/core/isoneutral/diffusion.py:286-295)
+* ``isoneutral_skew_diffusion(state, tr, istemp) -> None``
+  (veros/core/isoneutral/diffusion.py:298-307)
+
+``state`` is either a :class:`veros_gb300.state.DeviceState` (fields stay on
+the GPU, all work is enqueued on torch's current stream, nothing synchronises)
+or a NumPy-backend ``VerosState``, whose fields are uploaded, processed and
+written back (the reference's ``vs.update`` contract: pre returns the new
+arrays, the diffusion routines mutate ``state.variables``).
+"""
+
+import torch
+
+from . import _capi
+from .state import DeviceState, KernelOutput, FIELDS_MASK
+
+PRE_OUT = ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "K_11", "K_22", "K_33")
+
+
+def _stream(dev):
+    return torch.cuda.current_stream(dev.device).cuda_stream
+
+
+def _level(t, n):
+    """Pointer of time level ``n`` of a (X, Y, Z, 3) tensor."""
+    return t[..., n].data_ptr()
+
+
+def run_pre(dev):
+    """Enqueue the slope/tensor kernel on a DeviceState (in place)."""
+    v = dev.variables
+    dev.check_layout(("temp", "salt", "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by"))
+    lib = _capi.load()
+    st = lib.vg_isoneutral_pre_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), _level(v.temp, v.tau),
+                                   _level(v.salt, v.tau), v.K_iso.data_ptr(), dev.mask_bits().data_ptr(),
+                                   dev.tensor_fields(), _stream(dev))
+    _capi.check(st, "isoneutral_diffusion_pre")
+
+
+def diffusion_scratch(dev):
+    nbytes = _capi.load().vg_isoneutral_diffusion_scratch_bytes(dev.domain())
+    return torch.empty(nbytes // 8, dtype=torch.float64, device=dev.device)
+
+
+def run_diffusion(dev, istemp, skew=False, scratch=None):
+    """Enqueue diffusion of temp (istemp) or salt on a DeviceState (in place)."""
+    v = dev.variables
+    tr = v.temp if istemp else v.salt
+    dtr = v.dtemp_iso if istemp else v.dsalt_iso
+    energy = bool(dev.settings.enable_conserve_energy)
+    kfield = v.K_gm if skew else v.K_iso
+    names = ["temp" if istemp else "salt", "dtemp_iso" if istemp else "dsalt_iso", "K_11", "K_22", "K_33",
+             "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "K_gm" if skew else "K_iso"]
+    if energy:
+        names += ["int_drhodT" if istemp else "int_drhodS", "P_diss_skew" if skew else "P_diss_iso"]
+    dev.check_layout(names)
+    if energy:
+        idr = (v.int_drhodT if istemp else v.int_drhodS)
+        P = v.P_diss_skew if skew else v.P_diss_iso
+        tra = _capi.VgTracerArgs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), _level(idr, v.tau),
+                                 P.data_ptr())
+    else:
+        tra = _capi.VgTracerArgs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), None, None)
+    if scratch is None:
+        scratch = diffusion_scratch(dev)
+    kb = v.kbot
+    if kb.stride(0) != 1 or kb.stride(1) != dev.pitch:
+        raise ValueError("kbot is not in the canonical layout")
+    lib = _capi.load()
+    st = lib.vg_isoneutral_diffusion_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), dev.tensor_fields(),
+                                         kfield.data_ptr(), dev.mask_bits().data_ptr(), kb.data_ptr(), tra,
+                                         1 if skew else 0, scratch.data_ptr(), scratch.numel() * 8, _stream(dev))
+    _capi.check(st, "isoneutral_skew_diffusion" if skew else "isoneutral_diffusion")
+
+
+# ---------------------------------------------------------------------------
+# reference-signature entry points
+
+
+def _is_device_state(state):
+    return isinstance(state, DeviceState)
+
+
+def isoneutral_diffusion_pre(state):
+    if _is_device_state(state):
+        run_pre(state)
+        v = state.variables
+        return KernelOutput(**{n: getattr(v, n) for n in PRE_OUT})
+    names = ("temp", "salt", "K_iso", "dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt",
+             *FIELDS_MASK, *PRE_OUT)
+    dev = DeviceState.from_host(state, fields=names)
+    run_pre(dev)
+    return KernelOutput(**{n: dev.download(n) for n in PRE_OUT})
+
+
+def _diffusion_entry(state, tr, istemp, skew):
+    name = "temp" if istemp else "salt"
+    dname = "dtemp_iso" if istemp else "dsalt_iso"
+    pname = "P_diss_skew" if skew else "P_diss_iso"
+    if _is_device_state(state):
+        v = state.variables
+        target = getattr(v, name)
+        if tr is not None and tr is not target:
+            target.copy_(tr)  # the reference passes tr by value and writes back to temp/salt
+        run_diffusion(state, istemp, skew=skew)
+        return None
+    energy = bool(state.settings.enable_conserve_energy)
+    names = [name, dname, "K_iso", "K_gm", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "kbot",
+             "dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt", *FIELDS_MASK]
+    if energy:
+        names += ["int_drhodT" if istemp else "int_drhodS", pname]
+    dev = DeviceState.from_host(state, fields=names)
+    if tr is not None:
+        dev.upload(name, tr)
+    run_diffusion(dev, istemp, skew=skew)
+    vs = state.variables
+    out = {name: dev.download(name), dname: dev.download(dname)}
+    if energy:
+        out[pname] = dev.download(pname)
+    vs.update(out)
+    return None
+
+
+def isoneutral_diffusion(state, tr, istemp):
+    """Isopycnal diffusion of ``tr`` (temp if ``istemp`` else salt); mutates the state."""
+    return _diffusion_entry(state, tr, istemp, skew=False)
+
+
+def isoneutral_skew_diffusion(state, tr, istemp):
+    """Skew (GM) diffusion of ``tr``; mutates the state."""
+    return _diffusion_entry(state, tr, istemp, skew=True)

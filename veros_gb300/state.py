@@ -1,0 +1,261 @@
+"""Device-resident state in the canonical GB300 layout.
+
+``DeviceState`` duck-types the parts of ``veros.state.VerosState`` that the
+isoneutral path touches: ``state.variables.<field>``, ``state.variables.tau``
+and friends, ``state.variables.update(...)`` and ``state.settings.<name>``.
+Fields are torch CUDA tensors with the reference's logical shapes
+(``(X, Y, Z)``, tracers ``(X, Y, Z, 3)``, ``Ai_*`` ``(X, Y, Z, 2, 2)``) but
+x-fastest storage: element (i, j, k) sits at ``i + j*pitch + k*plane`` with
+the row pitch rounded up to 16 elements (16-byte aligned rows for every
+element size, as the tensor-memory-access engine requires). Time levels and
+tensor components are whole x-y-z blocks.
+"""
+
+from collections import namedtuple
+
+import numpy as np
+import torch
+
+from . import _capi
+
+PITCH_ALIGN = 16
+
+FIELDS_3D = ("K_iso", "K_gm", "K_11", "K_22", "K_33", "dtemp_iso", "dsalt_iso", "P_diss_iso", "P_diss_skew")
+FIELDS_TIME = ("temp", "salt", "int_drhodT", "int_drhodS")
+FIELDS_TENSOR = ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by")
+FIELDS_MASK = ("maskT", "maskU", "maskV", "maskW")
+FIELDS_X = ("dxt", "dxu")
+FIELDS_Y = ("dyt", "dyu", "cost", "cosu")
+FIELDS_Z = ("dzt", "dzw", "zt")
+
+SETTING_NAMES = ("iso_slopec", "iso_dslope", "K_iso_steep", "dt_tracer", "grav", "rho_0",
+                 "eq_of_state_type", "enable_conserve_energy", "enable_skew_diffusion",
+                 "enable_neutral_diffusion")
+
+
+def KernelOutput(**kwargs):
+    """Same factory as veros/state.py:16-20: a namedtuple named KernelOutput."""
+    try:
+        from veros.state import KernelOutput as ref_factory
+    except Exception:  # veros not importable: identical local factory
+        return namedtuple("KernelOutput", list(kwargs.keys()))(*kwargs.values())
+    return ref_factory(**kwargs)
+
+
+def pitch_for(X):
+    return -(-X // PITCH_ALIGN) * PITCH_ALIGN
+
+
+def canonical_empty(X, Y, Z, extra=(), dtype=torch.float64, device="cuda"):
+    """Uninitialised tensor of logical shape (X, Y, Z, *extra) in canonical layout."""
+    P = pitch_for(X)
+    store = torch.empty((*extra, Z, Y, P), dtype=dtype, device=device)
+    ne = len(extra)
+    perm = (ne + 2, ne + 1, ne) + tuple(range(ne))
+    return store.permute(*perm)[:X]
+
+
+def canonical_zeros(X, Y, Z, extra=(), dtype=torch.float64, device="cuda"):
+    t = canonical_empty(X, Y, Z, extra, dtype, device)
+    t.zero_()
+    return t
+
+
+def canonical_empty_2d(X, Y, dtype=torch.int32, device="cuda"):
+    P = pitch_for(X)
+    return torch.empty((Y, P), dtype=dtype, device=device).permute(1, 0)[:X]
+
+
+def is_canonical(t, X, Y, Z):
+    """True if ``t`` has x stride 1, y stride = pitch and z stride = pitch*Y."""
+    if t.shape[:3] != (X, Y, Z) or t.stride(0) != 1:
+        return False
+    P = t.stride(1)
+    return P >= X and (Z == 1 or t.stride(2) == P * Y)
+
+
+class Settings:
+    """Attribute namespace of model settings."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+    def get(self, name, default=None):
+        return self.__dict__.get(name, default)
+
+    def to_struct(self):
+        return _capi.VgIsoSettings(
+            float(self.iso_slopec), float(self.iso_dslope), float(self.K_iso_steep), float(self.dt_tracer),
+            float(self.grav), float(self.rho_0), int(self.eq_of_state_type), int(bool(self.enable_conserve_energy)))
+
+
+class DeviceVariables:
+    """Attribute container of device tensors plus the time-level indices."""
+
+    def __init__(self):
+        object.__setattr__(self, "_fields", {})
+        self.tau, self.taup1, self.taum1 = 1, 2, 0
+
+    def __getattr__(self, name):
+        f = object.__getattribute__(self, "_fields")
+        if name in f:
+            return f[name]
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in ("tau", "taup1", "taum1"):
+            object.__setattr__(self, name, int(value))
+            return
+        f = object.__getattribute__(self, "_fields")
+        if name in f and isinstance(value, torch.Tensor) and value is not f[name]:
+            cur = f[name]
+            if value.shape != cur.shape:
+                raise ValueError(f"{name}: shape {tuple(value.shape)} does not match {tuple(cur.shape)}")
+            cur.copy_(value)  # keep the canonical storage
+            return
+        f[name] = value
+
+    def fields(self):
+        return list(object.__getattribute__(self, "_fields").keys())
+
+    def update(self, other=None, **new_fields):
+        """Same contract as VerosVariables.update (veros/state.py:70-90)."""
+        if other is not None:
+            if new_fields:
+                raise ValueError("Either other or new_fields can be given")
+            if hasattr(other, "_fields"):
+                new_fields = dict(zip(other._fields, other))
+            elif isinstance(other, dict):
+                new_fields = other
+            else:
+                raise TypeError(f"Cannot update from {type(other)} type")
+        for k, v in new_fields.items():
+            setattr(self, k, v)
+
+
+class DeviceState:
+    """One ocean domain resident on a CUDA device in the canonical layout."""
+
+    def __init__(self, nx, ny, nz, settings, device="cuda"):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.X, self.Y, self.Z = nx + 4, ny + 4, nz
+        self.device = torch.device(device)
+        self.settings = settings if isinstance(settings, Settings) else Settings(**settings)
+        self.variables = DeviceVariables()
+        self.dimensions = dict(xt=nx, xu=nx, yt=ny, yu=ny, zt=nz, zw=nz, timesteps=3, isle=1, tensor1=2, tensor2=2)
+        self.pitch = pitch_for(self.X)
+        self.plane = self.pitch * self.Y
+        self._mask_bits = None
+        self._mask_version = None
+
+    # ---- allocation -------------------------------------------------------
+    def alloc_fields(self):
+        X, Y, Z, dev = self.X, self.Y, self.Z, self.device
+        v = self.variables
+        for n in FIELDS_3D:
+            setattr(v, n, canonical_zeros(X, Y, Z, device=dev))
+        for n in FIELDS_TIME:
+            setattr(v, n, canonical_zeros(X, Y, Z, (3,), device=dev))
+        for n in FIELDS_TENSOR:
+            setattr(v, n, canonical_zeros(X, Y, Z, (2, 2), device=dev))
+        for n in FIELDS_MASK:
+            setattr(v, n, canonical_zeros(X, Y, Z, dtype=torch.bool, device=dev))
+        kb = canonical_empty_2d(X, Y, device=dev)
+        kb.zero_()
+        v.kbot = kb
+        for n in FIELDS_X:
+            setattr(v, n, torch.zeros(X, dtype=torch.float64, device=dev))
+        for n in FIELDS_Y:
+            setattr(v, n, torch.zeros(Y, dtype=torch.float64, device=dev))
+        for n in FIELDS_Z:
+            setattr(v, n, torch.zeros(Z, dtype=torch.float64, device=dev))
+
+    @classmethod
+    def from_host(cls, host, device="cuda", fields=None):
+        """Upload a ``synthetic.HostState`` or a NumPy ``VerosState``."""
+        if hasattr(host, "variables"):  # a VerosState
+            vs = host.variables
+            nx, ny, nz = host.settings.nx, host.settings.ny, host.settings.nz
+            settings = {n: getattr(host.settings, n) for n in SETTING_NAMES if hasattr(host.settings, n)}
+            get = lambda n: getattr(vs, n, None)  # noqa: E731
+            taus = (vs.tau, vs.taup1, vs.taum1)
+        else:
+            nx, ny, nz = host.nx, host.ny, host.nz
+            settings = {n: host.settings[n] for n in SETTING_NAMES if n in host.settings}
+            get = lambda n: host.arrays.get(n)  # noqa: E731
+            taus = (host.tau, host.taup1, host.taum1)
+        st = cls(nx, ny, nz, settings, device=device)
+        st.alloc_fields()
+        v = st.variables
+        v.tau, v.taup1, v.taum1 = (int(t) for t in taus)
+        for n in v.fields():
+            if fields is not None and n not in fields:
+                continue
+            arr = get(n)
+            if arr is None:
+                continue
+            st.upload(n, np.asarray(arr))
+        return st
+
+    def upload(self, name, arr):
+        dst = getattr(self.variables, name)
+        src = torch.from_numpy(np.ascontiguousarray(arr))
+        if src.dtype != dst.dtype:
+            src = src.to(dst.dtype)
+        dst.copy_(src, non_blocking=False)
+        if name in FIELDS_MASK:
+            self._mask_version = None
+
+    def download(self, name):
+        t = getattr(self.variables, name)
+        if isinstance(t, torch.Tensor):
+            return t.detach().cpu().contiguous().numpy()
+        return t
+
+    # ---- derived device views --------------------------------------------
+    def domain(self):
+        return _capi.VgDomain(self.X, self.Y, self.Z, self.pitch, self.plane)
+
+    def grid(self):
+        v = self.variables
+        return _capi.VgGrid(*(getattr(v, n).data_ptr() for n in ("dxt", "dxu", "dyt", "dyu", "cost", "cosu",
+                                                                   "dzt", "dzw", "zt")))
+
+    def mask_bits(self, stream=None):
+        """Packed T/U/V/W mask bytes; rebuilt whenever a mask tensor changed."""
+        v = self.variables
+        version = tuple((getattr(v, n).data_ptr(), getattr(v, n)._version) for n in FIELDS_MASK)
+        if self._mask_bits is None or self._mask_version != version:
+            if self._mask_bits is None:
+                self._mask_bits = canonical_empty(self.X, self.Y, self.Z, dtype=torch.uint8, device=self.device)
+            lib = _capi.load()
+            dom = self.domain()
+            s = stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+            _capi.check(lib.vg_pack_masks(dom, *(getattr(v, n).data_ptr() for n in FIELDS_MASK),
+                                          self._mask_bits.data_ptr(), s), "vg_pack_masks")
+            self._mask_version = version
+        return self._mask_bits
+
+    def tensor_fields(self):
+        v = self.variables
+        ai = v.Ai_ez
+        for n in FIELDS_TENSOR:
+            t = getattr(v, n)
+            if t.stride()[3:] != ai.stride()[3:]:
+                raise ValueError(f"{n}: component strides {t.stride()[3:]} differ from Ai_ez {ai.stride()[3:]}")
+        return _capi.VgTensorFields(v.K_11.data_ptr(), v.K_22.data_ptr(), v.K_33.data_ptr(), v.Ai_ez.data_ptr(),
+                                    v.Ai_nz.data_ptr(), v.Ai_bx.data_ptr(), v.Ai_by.data_ptr(),
+                                    ai.stride(3), ai.stride(4))
+
+    def check_layout(self, names):
+        v = self.variables
+        for n in names:
+            t = getattr(v, n)
+            if not t.is_cuda or t.device != self.device:
+                raise ValueError(f"{n} is not on {self.device}")
+            if not is_canonical(t, self.X, self.Y, self.Z) or t.stride(1) != self.pitch:
+                raise ValueError(f"{n}: strides {t.stride()} are not the canonical layout (pitch {self.pitch})")
+
+    def to_host_dict(self, names=None):
+        names = names or self.variables.fields()
+        return {n: self.download(n) for n in names}

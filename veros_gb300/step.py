@@ -1,0 +1,113 @@
+"""Rollouts of the isoneutral step on a :class:`DeviceState`.
+
+One step is the caller-side sequence of veros/core/thermodynamics.py:226-241
+(zero advection) and :425-432, followed by the time-level rotation of
+veros/veros.py:321-322; see ``vg_isoneutral_step_f64`` in
+``include/veros_gb300.h``. The whole step is one C call, so a rollout can be
+captured in a CUDA graph: ``capture(n)`` records ``n`` steps (the rotation of
+time levels is a pointer permutation with period 3, so graphs are recorded
+for each of the three phases and replayed in turn).
+"""
+
+import torch
+
+from . import _capi
+from .isoneutral import diffusion_scratch
+
+
+class IsoneutralStepper:
+    def __init__(self, dev):
+        self.dev = dev
+        self.lib = _capi.load()
+        self.scratch = diffusion_scratch(dev)
+        self._graphs = {}
+
+    def _fields(self):
+        dev, v = self.dev, self.dev.variables
+        lvl = lambda t, n: t[..., n].data_ptr()  # noqa: E731
+        energy = bool(dev.settings.enable_conserve_energy)
+        dev.check_layout(("temp", "salt", "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by",
+                          "dtemp_iso", "dsalt_iso", "P_diss_iso", "int_drhodT", "int_drhodS"))
+        return _capi.VgStepFields(
+            lvl(v.temp, v.tau), lvl(v.temp, v.taup1), lvl(v.salt, v.tau), lvl(v.salt, v.taup1), v.K_iso.data_ptr(),
+            dev.mask_bits().data_ptr(), v.kbot.data_ptr(), dev.tensor_fields(), v.dtemp_iso.data_ptr(),
+            v.dsalt_iso.data_ptr(), lvl(v.int_drhodT, v.tau) if energy else None,
+            lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr())
+
+    def _launch(self, stream):
+        dev = self.dev
+        st = self.lib.vg_isoneutral_step_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), self._fields(),
+                                             self.scratch.data_ptr(), self.scratch.numel() * 8, stream)
+        _capi.check(st, "vg_isoneutral_step_f64")
+
+    def _rotate(self):
+        v = self.dev.variables
+        v.taum1, v.tau, v.taup1 = v.tau, v.taup1, v.taum1
+
+    def step(self, n=1):
+        """Run ``n`` steps eagerly on torch's current stream (one C call each)."""
+        stream = torch.cuda.current_stream(self.dev.device).cuda_stream
+        for _ in range(n):
+            self._launch(stream)
+            self._rotate()
+
+    def step_stages(self, events=None):
+        """One step as four C calls (prepare, pre, diffusion of temp, of salt).
+
+        ``events``: optional list of 5 ``torch.cuda.Event`` recorded on the
+        current stream before, between and after the stages.
+        """
+        dev, lib = self.dev, self.lib
+        stream_obj = torch.cuda.current_stream(dev.device)
+        stream = stream_obj.cuda_stream
+        f = self._fields()
+        dom, grid, sett = dev.domain(), dev.grid(), dev.settings.to_struct()
+        nbytes = self.scratch.numel() * 8
+        rec = (lambda n: events[n].record(stream_obj)) if events else (lambda n: None)
+        rec(0)
+        _capi.check(lib.vg_isoneutral_step_prepare_f64(dom, f, stream), "step prepare")
+        rec(1)
+        _capi.check(lib.vg_isoneutral_pre_f64(dom, grid, sett, f.temp_tau, f.salt_tau, f.K_iso, f.mask_bits,
+                                              f.ten, stream), "pre")
+        rec(2)
+        for n, (tau, taup1, dtr, idr) in enumerate(((f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau),
+                                                    (f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau))):
+            tra = _capi.VgTracerArgs(tau, taup1, dtr, idr, f.P_diss_iso)
+            _capi.check(lib.vg_isoneutral_diffusion_f64(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot, tra, 0,
+                                                        self.scratch.data_ptr(), nbytes, stream), "diffusion")
+            rec(3 + n)
+        self._rotate()
+
+    def step_host(self, temp_tau, salt_tau, out_temp, out_salt, out_dtemp, out_dsalt, staging=None):
+        """One step from and to host buffers in the reference layout.
+
+        ``temp_tau``/``salt_tau``: (X, Y, Z) float64 CPU tensors (pinned for
+        asynchronous copies) holding the current level; the new level and the
+        tendencies ``dtemp_iso``/``dsalt_iso`` land in the ``out_*`` CPU tensors.
+        Copies and kernels are enqueued on the current stream; the host waits
+        only for the final device-to-host copies.
+        """
+        v = self.dev.variables
+        shape = (self.dev.X, self.dev.Y, self.dev.Z)
+        if staging is None:
+            staging = torch.empty((6, *shape), dtype=torch.float64, device=self.dev.device)
+        staging[0].copy_(temp_tau, non_blocking=True)
+        staging[1].copy_(salt_tau, non_blocking=True)
+        v.temp[..., v.tau].copy_(staging[0])
+        v.salt[..., v.tau].copy_(staging[1])
+        self.step(1)
+        new = v.tau  # the level just written, after the rotation
+        staging[2].copy_(v.temp[..., new])
+        staging[3].copy_(v.salt[..., new])
+        staging[4].copy_(v.dtemp_iso)
+        staging[5].copy_(v.dsalt_iso)
+        out_temp.copy_(staging[2], non_blocking=True)
+        out_salt.copy_(staging[3], non_blocking=True)
+        out_dtemp.copy_(staging[4], non_blocking=True)
+        out_dsalt.copy_(staging[5], non_blocking=True)
+        torch.cuda.current_stream(self.dev.device).synchronize()
+
+    def launches_per_step(self):
+        """Kernels of this library one step enqueues (prepare + pre + 2 x diffusion)."""
+        per_diffusion = 3 if self.dev.settings.enable_conserve_energy else 2
+        return 1 + 1 + 2 * per_diffusion
