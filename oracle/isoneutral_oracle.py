@@ -213,10 +213,87 @@ def create_water_masks(ks, nz):
     return land_mask, water_mask, edge_mask
 
 
-def solve_tridiagonal(a, b, c, d, water_mask, edge_mask):
-    """veros/core/operators.py:60-77: one ``dgtsv`` over all wet cells, couplings cut."""
-    from scipy.linalg import lapack
+def _kbot_form(water_mask, edge_mask):
+    """True if every column is water from its first wet level to the top with the edge there."""
+    nz = water_mask.shape[-1]
+    wm = water_mask.reshape(-1, nz)
+    em = edge_mask.reshape(-1, nz)
+    has = wm.any(axis=1)
+    ks = np.where(has, wm.argmax(axis=1), nz)
+    kk = np.arange(nz)[None, :]
+    return np.array_equal(wm, kk >= ks[:, None]) and np.array_equal(em, (kk == ks[:, None]) & has[:, None])
 
+
+def dgtsv_columns(dl, d, du, b, ks):
+    """LAPACK ``dgtsv`` (Gaussian elimination with partial pivoting, NRHS = 1)
+    restated column-parallel in NumPy.
+
+    LAPACK 3.x ``dgtsv`` is the third-party routine the reference calls
+    (veros/core/operators.py:75, through scipy.linalg.lapack; scipy 1.18.1 with
+    OpenBLAS 0.3.x). Its published algorithm, for rows i = 0..n-2: if
+    ``|d[i]| >= |dl[i]|`` eliminate without interchange (``fact = dl/d``,
+    ``d[i+1] -= fact*du[i]``, ``b[i+1] -= fact*b[i]``, second super-diagonal 0);
+    otherwise interchange rows i and i+1 (``fact = d/dl``; the second
+    super-diagonal takes ``du[i+1]`` except on the last step). Back
+    substitution ``x[i] = (b[i] - du[i] x[i+1] - du2[i] x[i+2]) / d[i]``.
+
+    Arrays are (ncols, nz); column ``s`` is the system of rows ``ks[s]..nz-1``
+    (``dl[:, k]`` is the entry left of the diagonal in row k). Every operation
+    is a single IEEE-rounded NumPy ufunc, so results do not depend on the
+    platform's floating-point contraction.
+    """
+    ncols, nz = d.shape
+    D = d.copy()
+    DU = du.copy()
+    DU2 = np.zeros_like(d)
+    B = b.copy()
+    kk = np.arange(nz)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for k in range(nz - 1):
+            act = k >= ks
+            if not act.any():
+                continue
+            l = dl[:, k + 1]
+            dk, dk1, duk, bk, bk1 = D[:, k], D[:, k + 1], DU[:, k], B[:, k], B[:, k + 1]
+            du1 = DU[:, k + 1]
+            keep = np.abs(dk) >= np.abs(l)
+            f_keep = l / dk
+            f_swap = dk / l
+            n_dk = np.where(keep, dk, l)
+            n_dk1 = np.where(keep, dk1 - f_keep * duk, duk - f_swap * dk1)
+            n_duk = np.where(keep, duk, dk1)
+            n_bk = np.where(keep, bk, bk1)
+            n_bk1 = np.where(keep, bk1 - f_keep * bk, bk - f_swap * bk1)
+            if k < nz - 2:
+                n_du2 = np.where(keep, 0.0, du1)
+                n_du1 = np.where(keep, du1, -f_swap * du1)
+            else:
+                n_du2 = np.zeros(ncols)
+                n_du1 = du1
+            D[:, k] = np.where(act, n_dk, dk)
+            D[:, k + 1] = np.where(act, n_dk1, dk1)
+            DU[:, k] = np.where(act, n_duk, duk)
+            DU[:, k + 1] = np.where(act, n_du1, du1)
+            DU2[:, k] = np.where(act, n_du2, 0.0)
+            B[:, k] = np.where(act, n_bk, bk)
+            B[:, k + 1] = np.where(act, n_bk1, bk1)
+        X = np.zeros_like(d)
+        X[:, nz - 1] = B[:, nz - 1] / D[:, nz - 1]
+        if nz > 1:
+            X[:, nz - 2] = (B[:, nz - 2] - DU[:, nz - 2] * X[:, nz - 1]) / D[:, nz - 2]
+        for k in range(nz - 3, -1, -1):
+            X[:, k] = (B[:, k] - DU[:, k] * X[:, k + 1] - DU2[:, k] * X[:, k + 2]) / D[:, k]
+    return np.where(kk[None, :] >= ks[:, None], X, 0.0)
+
+
+def solve_tridiagonal(a, b, c, d, water_mask, edge_mask):
+    """veros/core/operators.py:60-77: one ``dgtsv`` over all wet cells, couplings cut.
+
+    With masks of the ``create_water_masks`` form the cut couplings make the
+    concatenated system block-diagonal, one block per column, so the
+    column-parallel restatement ``dgtsv_columns`` gives the same result;
+    masks of any other form go to LAPACK exactly as the reference does.
+    """
     out = np.zeros(a.shape, dtype=a.dtype)
     if not np.any(water_mask):
         return out
@@ -224,6 +301,16 @@ def solve_tridiagonal(a, b, c, d, water_mask, edge_mask):
     c = c.copy()
     a[edge_mask] = 0
     c[..., -1] = 0
+    if _kbot_form(water_mask, edge_mask):
+        nz = a.shape[-1]
+        shape = a.shape
+        wm = water_mask.reshape(-1, nz)
+        has = wm.any(axis=1)
+        ks = np.where(has, wm.argmax(axis=1), nz)
+        sol = dgtsv_columns(a.reshape(-1, nz), b.reshape(-1, nz), c.reshape(-1, nz), d.reshape(-1, nz), ks)
+        return sol.reshape(shape)
+    from scipy.linalg import lapack
+
     sol = lapack.dgtsv(a[water_mask][1:], b[water_mask], c[water_mask][:-1], d[water_mask])[3]
     out[water_mask] = sol
     return out

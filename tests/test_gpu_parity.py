@@ -9,7 +9,7 @@ multiplies by a mask.
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import assert_field_close, load_golden, p_diss_floor
 
 pytestmark = pytest.mark.gpu
 
@@ -83,20 +83,24 @@ def test_diffusion_chain_vs_reference_golden(case):
     run_pre(dev)
     run_diffusion(dev, istemp=True)
     torch.cuda.synchronize()
+    dt = float(g["setting_dt_tracer"])
+    settings = {k[8:]: v.item() for k, v in g.items() if k.startswith("setting_")}
+    arrays = {k[3:]: v for k, v in g.items() if k.startswith("in_")}
+    arrays.update(K_33=g["pre_K_33"], temp=g["diffT_temp"], salt=g["diffS_salt"])
+    pfloor = p_diss_floor(arrays, settings, int(g["tau"]))
     for name in ("temp", "dtemp_iso", "P_diss_iso"):
-        got, ref = dev.download(name), g[f"diffT_{name}"]
-        assert _rel(got, ref) <= TOL, f"T {name}: {_rel(got, ref):.3e}"
+        assert_field_close(name, dev.download(name), g[f"diffT_{name}"], tracer=g["diffT_temp"], dt=dt,
+                           floor=pfloor if name == "P_diss_iso" else 0.0)
     run_diffusion(dev, istemp=False)
     torch.cuda.synchronize()
     for name in ("salt", "dsalt_iso", "P_diss_iso"):
-        got, ref = dev.download(name), g[f"diffS_{name}"]
-        assert _rel(got, ref) <= TOL, f"S {name}: {_rel(got, ref):.3e}"
+        assert_field_close(name, dev.download(name), g[f"diffS_{name}"], tracer=g["diffS_salt"], dt=dt,
+                           floor=pfloor if name == "P_diss_iso" else 0.0)
     if "skewT_temp" in g:
         run_diffusion(dev, istemp=True, skew=True)
         torch.cuda.synchronize()
         for name in ("temp", "dtemp_iso", "P_diss_skew"):
-            got, ref = dev.download(name), g[f"skewT_{name}"]
-            assert _rel(got, ref) <= TOL, f"skew {name}: {_rel(got, ref):.3e}"
+            assert_field_close(name, dev.download(name), g[f"skewT_{name}"], tracer=g["skewT_temp"], dt=dt)
 
 
 def test_tridiag_vs_reference_golden():
@@ -107,9 +111,12 @@ def test_tridiag_vs_reference_golden():
     out = solve_tridiagonal(g["a"], g["b"], g["c"], g["d"], g["water_mask"], g["edge_mask"])
     np.testing.assert_allclose(out, g["out_random"], rtol=1e-7)
     assert np.all(out[~g["water_mask"]] == 0.0)
+    # dgtsv's operation order without contraction: identical bits, interchanges included
+    assert np.array_equal(out, g["out_random"])
     out = solve_implicit(g["ad"], g["bd"], g["cd"], g["d"], g["water_mask"], g["edge_mask"],
                          b_edge=g["b_edge"], d_edge=g["d_edge"])
     assert _rel(out, g["out_dd"]) <= TOL
+    assert np.array_equal(out, g["out_dd"])
 
 
 def test_tridiag_device_tensors_and_bad_masks():
@@ -177,45 +184,89 @@ def _oracle_steps(host, n):
     return vs
 
 
+def _check_state(dev, vs, names, settings, tau_in):
+    """Compare every named field; tendencies and P_diss_iso get their differencing floors."""
+    arrays = vs.__dict__
+    for name in names:
+        tracer = None
+        floor = 0.0
+        if name == "dtemp_iso":
+            tracer = vs.temp
+        elif name == "dsalt_iso":
+            tracer = vs.salt
+        elif name == "P_diss_iso":
+            floor = p_diss_floor(arrays, settings, tau_in)
+        assert_field_close(name, dev.download(name), getattr(vs, name), tracer=tracer, dt=settings["dt_tracer"],
+                           floor=floor)
+
+
 STEP_FIELDS = ("temp", "salt", "dtemp_iso", "dsalt_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by")
+
+
+def _teacher_forced_rollout(host, nsteps, stages=False):
+    """Every step of a GPU rollout against one oracle step from the GPU's own previous state.
+
+    A free-running comparison would mix the per-step parity with the
+    rollout's own amplification of last-bit differences (slopes divide by
+    near-zero vertical density gradients); this checks each step at the FP64
+    bar and returns the GPU state.
+    """
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    dev = DeviceState.from_host(host)
+    st = IsoneutralStepper(dev)
+    fields = STEP_FIELDS + (("P_diss_iso",) if host.settings["enable_conserve_energy"] else ())
+    for n in range(nsteps):
+        v = dev.variables
+        arrays = dict(host.arrays)
+        arrays.update(dev.to_host_dict([f for f in host.arrays if f in v.fields()]))
+        vs = orc.OracleState({k: np.array(a, copy=True) for k, a in arrays.items()}, tau=v.tau, taup1=v.taup1,
+                             taum1=v.taum1)
+        tau_in = vs.tau
+        orc.isoneutral_step(vs, host.settings)
+        if stages and n % 2 == 0:
+            st.step_stages()
+        else:
+            st.step(1)
+        torch.cuda.synchronize()
+        assert dev.variables.tau == vs.tau
+        _check_state(dev, vs, fields, host.settings, tau_in)
+    return dev
 
 
 @pytest.mark.parametrize("energy", [False, True])
 def test_small_linear_rollout_vs_oracle(energy):
-    """64 x 48 x 20, linear EOS: 5 steps of the GPU stepper against 5 oracle steps."""
+    """64 x 48 x 20, linear EOS: 5 steps, each against the oracle."""
+    from veros_gb300 import synthetic
+
+    host = synthetic.small_linear_state(seed=0)
+    host.settings["enable_conserve_energy"] = energy
+    _teacher_forced_rollout(host, 5)
+
+
+def test_rollout_drift_is_bounded():
+    """Free-running: 5 GPU steps against 5 oracle steps from the same start stay within 1e-9."""
     from veros_gb300 import synthetic
     from veros_gb300.state import DeviceState
     from veros_gb300.step import IsoneutralStepper
 
-    host = synthetic.small_linear_state(seed=0)
-    host.settings["enable_conserve_energy"] = energy
+    host = synthetic.small_linear_state(seed=1)
     dev = DeviceState.from_host(host)
     IsoneutralStepper(dev).step(5)
     torch.cuda.synchronize()
     vs = _oracle_steps(host, 5)
-    assert dev.variables.tau == vs.tau
-    fields = STEP_FIELDS + (("P_diss_iso",) if energy else ())
-    for name in fields:
-        err = _rel(dev.download(name), getattr(vs, name))
-        assert err <= TOL, f"{name}: {err:.3e}"
+    for name in ("temp", "salt", "K_11", "K_33", "Ai_bx"):
+        assert _rel(dev.download(name), getattr(vs, name)) <= 1e-9, name
 
 
 def test_global_1deg_step_vs_oracle():
-    """The benchmark workload (360 x 180 x 60, nonlinear EOS): 2 steps, stages driven one by one."""
+    """The benchmark workload (360 x 180 x 60, nonlinear EOS): 2 steps, staged and fused C calls."""
     from veros_gb300 import synthetic
-    from veros_gb300.state import DeviceState
-    from veros_gb300.step import IsoneutralStepper
 
     host = synthetic.global_1deg_state(seed=0)
-    dev = DeviceState.from_host(host)
-    st = IsoneutralStepper(dev)
-    st.step_stages()
-    st.step(1)
-    torch.cuda.synchronize()
-    vs = _oracle_steps(host, 2)
-    for name in STEP_FIELDS:
-        err = _rel(dev.download(name), getattr(vs, name))
-        assert err <= TOL, f"{name}: {err:.3e}"
+    dev = _teacher_forced_rollout(host, 2, stages=True)
     # masks and kbot indexing: land cells of the tracers stay exactly zero
     land = ~host.maskT
     assert np.all(dev.download("temp")[land] == 0.0)
@@ -239,8 +290,7 @@ def test_drop_in_signatures_on_device_state():
     vs.__dict__.update(orc.isoneutral_diffusion_pre(vs, host.settings))
     vs.__dict__.update(orc.isoneutral_diffusion(vs, host.settings, True))
     vs.__dict__.update(orc.isoneutral_diffusion(vs, host.settings, False))
-    for name in ("temp", "salt", "dtemp_iso", "dsalt_iso", "P_diss_iso", "K_33"):
-        assert _rel(dev.download(name), getattr(vs, name)) <= TOL, name
+    _check_state(dev, vs, ("temp", "salt", "dtemp_iso", "dsalt_iso", "P_diss_iso", "K_33"), host.settings, vs.tau)
 
 
 def test_host_buffer_step_matches_device_step():

@@ -7,13 +7,15 @@
 //                   reference leaves them unset.
 //  2. column_kernel one thread per interior column, walking k upward: flux
 //                   divergence (diffusion.py:116-139), explicit update, the
-//                   implicit K_33 solve as a Thomas sweep whose c'/d' live in
-//                   shared memory (diffusion.py:142-169), and the dtracer_iso
-//                   accumulation (diffusion.py:196-205).
+//                   implicit K_33 solve in the operation order of LAPACK dgtsv
+//                   (the solver behind the reference's solve_implicit), with
+//                   the eliminated rows in shared memory (diffusion.py:142-169),
+//                   and the dtracer_iso accumulation (diffusion.py:196-205).
 //  3. energy_kernel (enable_conserve_energy only) one thread per cell:
 //                   dissipation on the W grid and the vertical-mixing term
 //                   added to P_diss (diffusion.py:234-281).
 #include "common.cuh"
+#include "dgtsv.cuh"
 
 namespace vg {
 
@@ -133,9 +135,35 @@ __global__ void __launch_bounds__(128) flux_kernel(DiffArgs a) {
   a.ft[o] = ft;
 }
 
+// Row source of one column's implicit system (diffusion.py:154-164), read
+// back from global memory for the interchange path.
+struct ColSrc {
+  const DiffArgs &a;
+  long long base;
+  int ks, Z;
+  __device__ double delta(int k) const {
+    return k < Z - 1 ? rmul(rdiv(a.dt, a.g.dzw[k]), a.K33[base + (long long)k * a.L.plane]) : 0.0;
+  }
+  __device__ double a_(int k) const { return rdiv(-delta(k - 1), a.g.dzt[k]); }
+  __device__ double b(int k) const {
+    return k == ks ? radd(1.0, rdiv(delta(k), a.g.dzt[k])) : radd(1.0, rdiv(radd(delta(k), delta(k - 1)), a.g.dzt[k]));
+  }
+  __device__ double c(int k) const { return rdiv(-delta(k), a.g.dzt[k]); }
+  __device__ double d(int k) const { return a.trp[base + (long long)k * a.L.plane]; }
+};
+struct ColSrcView {
+  const ColSrc &s;
+  __device__ double a(int k) const { return s.a_(k); }
+  __device__ double b(int k) const { return s.b(k); }
+  __device__ double c(int k) const { return s.c(k); }
+  __device__ double d(int k) const { return s.d(k); }
+};
+
 // Per interior column: explicit divergence, explicit update and (iso) the
-// implicit vertical solve. Shared memory holds c' and d' of the Thomas sweep
-// for each thread's column: 2 * Z doubles, laid out [k][thread].
+// implicit vertical solve in dgtsv's operation order. Shared memory holds the
+// eliminated diagonal and right-hand side of each thread's column, 2 * Z
+// doubles laid out [k][thread]; tr1 and the partial tendency are parked in
+// the output arrays between the two sweeps.
 __global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int ncols) {
   extern __shared__ double smem[];
   const int t = threadIdx.x;
@@ -145,18 +173,18 @@ __global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int
   const int Z = L.Z;
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
-  double *cp = smem;
-  double *dp = smem + (size_t)Z * blockDim.x;
   const int nb = blockDim.x;
+  double *Ds = smem;
+  double *Bs = smem + (size_t)Z * nb;
 
   const double cost = a.g.cost[j];
   const double fx = cost * a.g.dxt[i];
   const double fy = cost * a.g.dyt[j];
   const int ks = a.kbot[L.at2(i, j)] - 1;  // create_water_masks (utilities.py:38-48)
-  const bool land_col = ks < 0;
-  const bool solve = a.iso && !land_col;
+  const bool solve = a.iso && ks >= 0;
 
-  double ft_prev = 0.0, cp_prev = 0.0, dp_prev = 0.0, delta_prev = 0.0;
+  double ft_prev = 0.0, delta_prev = 0.0, Dp = 0.0, Bp = 0.0, cp = 0.0;
+  bool interchange = false;
   for (int k = 0; k < Z; ++k) {
     const long long o = L.at(i, j, k);
     const double mT = (__ldg(a.m + o) & VG_MASK_T) ? 1.0 : 0.0;
@@ -167,34 +195,61 @@ __global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int
     else
       e = e + mT * (ftk - ft_prev) / a.g.dzt[k];
     ft_prev = ftk;
-    const double d1 = a.dtr_iso[o] + e;
-    const double tr1 = a.trp[o] + a.dt * e;
+    const double d1 = radd(a.dtr_iso[o], e);
+    const double tr1 = radd(a.trp[o], rmul(a.dt, e));
     a.dtr_iso[o] = d1;
     a.trp[o] = tr1;
     if (solve) {
-      const double delta = k < Z - 1 ? a.dt / a.g.dzw[k] * ld(a.K33, o) : 0.0;
+      const double dzt = a.g.dzt[k];
+      const double delta = k < Z - 1 ? rmul(rdiv(a.dt, a.g.dzw[k]), ld(a.K33, o)) : 0.0;
       if (k >= ks) {
-        const double dzt = a.g.dzt[k];
-        const double ak = k == ks ? 0.0 : -delta_prev / dzt;
-        const double bk = k == ks ? 1.0 + delta / dzt : 1.0 + (delta + delta_prev) / dzt;
-        const double ck = k < Z - 1 ? -delta / dzt : 0.0;
-        const double den = bk - ak * cp_prev;
-        cp_prev = ck / den;
-        dp_prev = (tr1 - ak * dp_prev) / den;
-        cp[(size_t)k * nb + t] = cp_prev;
-        dp[(size_t)k * nb + t] = dp_prev;
+        const double ck = rdiv(-delta, dzt);
+        double Dk, Bk;
+        if (k == ks) {
+          Dk = radd(1.0, rdiv(delta, dzt));
+          Bk = tr1;
+        } else {
+          const double dl = rdiv(-delta_prev, dzt);
+          const double bk = radd(1.0, rdiv(radd(delta, delta_prev), dzt));
+          if (fabs(Dp) < fabs(dl)) interchange = true;
+          const double fact = rdiv(dl, Dp);
+          Dk = rsub(bk, rmul(fact, cp));
+          Bk = rsub(tr1, rmul(fact, Bp));
+        }
+        Ds[(size_t)k * nb + t] = Dk;
+        Bs[(size_t)k * nb + t] = Bk;
+        Dp = Dk;
+        Bp = Bk;
+        cp = ck;
       }
       delta_prev = delta;
     }
   }
   if (!solve) return;
-  double x = 0.0;
+  const long long base = L.at2(i, j);
+  if (interchange) {
+    // rows that dgtsv would interchange: replay the elimination with pivoting
+    ColSrc src{a, base, ks, Z};
+    dgtsv_slow_solve(ColSrcView{src}, ks, Z, Ds + t, nb);
+  } else {
+    double x = 0.0;
+    for (int k = Z - 1; k >= ks; --k) {
+      const double Dk = Ds[(size_t)k * nb + t], Bk = Bs[(size_t)k * nb + t];
+      if (k == Z - 1) {
+        x = rdiv(Bk, Dk);
+      } else {
+        const double delta = rmul(rdiv(a.dt, a.g.dzw[k]), ld(a.K33, base + (long long)k * L.plane));
+        x = rdiv(rsub(Bk, rmul(rdiv(-delta, a.g.dzt[k]), x)), Dk);
+      }
+      Ds[(size_t)k * nb + t] = x;
+    }
+  }
   for (int k = Z - 1; k >= ks; --k) {
-    const long long o = L.at(i, j, k);
-    x = dp[(size_t)k * nb + t] - (k < Z - 1 ? cp[(size_t)k * nb + t] * x : 0.0);
+    const long long o = base + (long long)k * L.plane;
+    const double x = Ds[(size_t)k * nb + t];
     const double tr1 = a.trp[o];
     a.trp[o] = x;
-    a.dtr_iso[o] = a.dtr_iso[o] + (x - tr1) / a.dt;
+    a.dtr_iso[o] = radd(a.dtr_iso[o], rdiv(rsub(x, tr1), a.dt));
   }
 }
 

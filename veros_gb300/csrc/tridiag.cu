@@ -3,8 +3,8 @@
 // * vg_solve_implicit_f64: the drop-in for solve_implicit / solve_tridiagonal
 //   (veros/core/utilities.py:51-59, veros/core/operators.py:60-77). One thread
 //   per column solves that column's water cells k = ks..nz-1 by Gaussian
-//   elimination with partial pivoting, the method of LAPACK dgtsv which the
-//   reference calls; the factors stay in shared memory.
+//   elimination with partial pivoting in the operation order of LAPACK dgtsv,
+//   which the reference calls (dgtsv.cuh); the factors stay in shared memory.
 // * vg_tdma_cuda_{double,float}: same buffers/descriptor contract as the XLA
 //   custom-call targets of veros/core/special/cuda_tdma_kernels.cu:81-111
 //   (full-depth Thomas sweep, identity rows already folded in by the caller,
@@ -14,6 +14,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "dgtsv.cuh"
 
 namespace vg {
 
@@ -30,8 +31,22 @@ struct TriArgs {
   int *bad;
 };
 
-// Per row r of a column the shared memory holds the eliminated diagonal,
-// first and second super-diagonals and right-hand side, laid out [r][field][thread].
+// Row source of one generic column (b_edge/d_edge substituted at ks,
+// utilities.py:53-57; a at the edge row is never read, operators.py:72).
+struct GenSrc {
+  const TriArgs &p;
+  long long base;
+  int ks;
+  __device__ long long at(int k) const { return base + p.sz * k; }
+  __device__ double a(int k) const { return p.a[at(k)]; }
+  __device__ double b(int k) const { return (k == ks && p.b_edge) ? p.b_edge[at(k)] : p.b[at(k)]; }
+  __device__ double c(int k) const { return p.c[at(k)]; }
+  __device__ double d(int k) const { return (k == ks && p.d_edge) ? p.d_edge[at(k)] : p.d[at(k)]; }
+};
+
+// One thread per column. Shared memory holds the eliminated diagonal and
+// right-hand side of the column, laid out [k][field][thread]; the solution
+// reuses the diagonal slots.
 __global__ void pivoting_solve_kernel(TriArgs p) {
   extern __shared__ double sm[];
   const int t = threadIdx.x;
@@ -48,67 +63,45 @@ __global__ void pivoting_solve_kernel(TriArgs p) {
     const long long o = base + p.sz * k;
     const bool w = p.water[o] != 0, e = p.edge[o] != 0;
     if (ks < 0 && w) ks = k;
-    const bool w_exp = ks >= 0;
-    const bool e_exp = ks == k;
-    if (w != w_exp || e != e_exp) bad = true;
+    if (w != (ks >= 0) || e != (ks == k)) bad = true;
   }
   if (bad && p.bad) atomicAdd(p.bad, 1);
 
-  for (int k = 0; k < nz; ++k) p.out[base + p.sz * k] = 0.0;
+  for (int k = 0; k < (ks < 0 ? nz : ks); ++k) p.out[base + p.sz * k] = 0.0;
   if (ks < 0) return;
-  const int n = nz - ks;
+  GenSrc src{p, base, ks};
+  double *Ds = sm + t;
+  double *Bs = sm + (size_t)nz * nb + t;
 
-  auto D = [&](int r) -> double & { return sm[((size_t)r * 4 + 0) * nb + t]; };
-  auto DU = [&](int r) -> double & { return sm[((size_t)r * 4 + 1) * nb + t]; };
-  auto DU2 = [&](int r) -> double & { return sm[((size_t)r * 4 + 2) * nb + t]; };
-  auto B = [&](int r) -> double & { return sm[((size_t)r * 4 + 3) * nb + t]; };
-
-  // row r = 0 is the edge row: b_edge/d_edge substitution (utilities.py:53-57)
-  {
-    const long long o = base + p.sz * ks;
-    double b0 = p.b_edge ? p.b_edge[o] : p.b[o];
-    double d0 = p.d_edge ? p.d_edge[o] : p.d[o];
-    D(0) = b0;
-    B(0) = d0;
-    DU(0) = n > 1 ? p.c[o] : 0.0;  // c[..., -1] = 0 cuts the top (operators.py:73)
-  }
-  for (int r = 0; r < n - 1; ++r) {
-    const long long o1 = base + p.sz * (ks + r + 1);
-    double dl = p.a[o1];
-    double d_next = p.b[o1];
-    double du_next = (r + 1 < n - 1) ? p.c[o1] : 0.0;
-    double b_next = p.d[o1];
-    const double dr = D(r);
-    if (fabs(dr) >= fabs(dl)) {
-      const double fact = dl / dr;
-      d_next = d_next - fact * DU(r);
-      b_next = b_next - fact * B(r);
-      DU2(r) = 0.0;
-    } else {
-      const double fact = dr / dl;
-      D(r) = dl;
-      const double tmp = d_next;
-      d_next = DU(r) - fact * tmp;
-      DU2(r) = du_next;
-      du_next = -fact * du_next;
-      DU(r) = tmp;
-      const double br = B(r);
-      B(r) = b_next;
-      b_next = br - fact * b_next;
+  // elimination without interchange while dgtsv would take that branch
+  bool interchange = false;
+  double Dp = src.b(ks), Bp = src.d(ks), cp = ks < nz - 1 ? src.c(ks) : 0.0;
+  Ds[(size_t)ks * nb] = Dp;
+  Bs[(size_t)ks * nb] = Bp;
+  for (int k = ks + 1; k < nz && !interchange; ++k) {
+    const double dl = src.a(k);
+    if (fabs(Dp) < fabs(dl)) {
+      interchange = true;
+      break;
     }
-    D(r + 1) = d_next;
-    DU(r + 1) = du_next;
-    B(r + 1) = b_next;
+    const double fact = rdiv(dl, Dp);
+    Dp = rsub(src.b(k), rmul(fact, cp));
+    Bp = rsub(src.d(k), rmul(fact, Bp));
+    cp = k < nz - 1 ? src.c(k) : 0.0;
+    Ds[(size_t)k * nb] = Dp;
+    Bs[(size_t)k * nb] = Bp;
   }
-  // back substitution
-  double x1 = B(n - 1) / D(n - 1), x2 = 0.0;
-  p.out[base + p.sz * (ks + n - 1)] = x1;
-  for (int r = n - 2; r >= 0; --r) {
-    const double x = (B(r) - DU(r) * x1 - DU2(r) * x2) / D(r);
-    p.out[base + p.sz * (ks + r)] = x;
-    x2 = x1;
-    x1 = x;
+  if (interchange) {
+    dgtsv_slow_solve(src, ks, nz, Ds, nb);
+  } else {
+    double x = 0.0;
+    for (int k = nz - 1; k >= ks; --k) {
+      const double Dk = Ds[(size_t)k * nb], Bk = Bs[(size_t)k * nb];
+      x = (k == nz - 1) ? rdiv(Bk, Dk) : rdiv(rsub(Bk, rmul(src.c(k), x)), Dk);
+      Ds[(size_t)k * nb] = x;
+    }
   }
+  for (int k = ks; k < nz; ++k) p.out[base + p.sz * k] = Ds[(size_t)k * nb];
 }
 
 template <typename F>
@@ -203,8 +196,8 @@ extern "C" int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, lo
   if (nsys > 0x7fffffffLL) return fail(VG_ERR_SHAPE, "too many columns");
   TriArgs p{nsx, (int)nsys, nz, s_x, s_y, s_z, a, b, c, d, b_edge, d_edge, water, edge, out, bad_columns};
   int nb = 128;
-  while (nb > 32 && (size_t)nb * nz * 4 * sizeof(double) > 100 * 1024) nb /= 2;
-  const size_t smem = (size_t)nb * nz * 4 * sizeof(double);
+  while (nb > 32 && (size_t)nb * nz * 2 * sizeof(double) > 100 * 1024) nb /= 2;
+  const size_t smem = (size_t)nb * nz * 2 * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(pivoting_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pivoting_solve_kernel smem: %s", cudaGetErrorString(e));

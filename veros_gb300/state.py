@@ -139,7 +139,10 @@ class DeviceState:
     def __init__(self, nx, ny, nz, settings, device="cuda"):
         self.nx, self.ny, self.nz = nx, ny, nz
         self.X, self.Y, self.Z = nx + 4, ny + 4, nz
-        self.device = torch.device(device)
+        device = torch.device(device)
+        if device.type == "cuda" and device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
         self.settings = settings if isinstance(settings, Settings) else Settings(**settings)
         self.variables = DeviceVariables()
         self.dimensions = dict(xt=nx, xu=nx, yt=ny, yu=ny, zt=nz, zw=nz, timesteps=3, isle=1, tensor1=2, tensor2=2)
