@@ -109,6 +109,18 @@ def _peaks():
     return 6800.0, "fallback"
 
 
+def _profiled_traffic(name):
+    """dram read+write bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    return None
+
+
 def cpu_baseline_sample(nz_band=None, steps=1):
     """Time the oracle step on one host core on a y-band sample of the workload."""
     from oracle import isoneutral_oracle as orc
@@ -241,11 +253,7 @@ def run_gb300(args):
     pre_ms = float(stage_ms[:, 1].mean())
     pre_achieved = PRE_BYTES_PER_CELL * cells / (pre_ms / 1e3) / 1e9
     step_achieved = STEP_BYTES_PER_CELL * cells * args.steps / (ms / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "pre_traffic_bytes.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("bytes_per_launch")
+    traffic = _profiled_traffic("pre_cell_kernel_global1deg.md")
     base = cpu_baseline_sample(steps=1)
     line = {
         "metric": "isoneutral step cells/s (FP64)", "value": value, "unit": "cells/s", "n_gpus": world,
