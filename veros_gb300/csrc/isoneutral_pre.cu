@@ -1,179 +1,313 @@
 // Isoneutral slopes and diffusion tensor (FP64), the work of
 // veros/core/isoneutral/isoneutral.py:18-229.
 //
-// One thread per cell (i, j, k). Every thread derives the face gradients and
-// density derivatives it needs from temp/salt directly; neighbouring threads
-// read the same cache lines, which L1/L2 serve. Outputs are written only on
-// the reference's sub-ranges so that all other cells keep their contents.
+// On GB300 the FP64 pipe (about 1 TFLOP/s) bounds this kernel, not HBM, so
+// the design minimises FP64 instructions per cell:
+//
+// * 2.5-D tiling. A CTA owns a TX x TY tile of columns and walks k upward.
+//   For every T point of the tile plus a one-cell ring it computes, once per
+//   level, the quantities several faces share: drho/dT and drho/dS
+//   (isoneutral.py:40-41), the east/north face gradients of T and S
+//   (:64-95), and the reciprocals of the two clamped vertical density
+//   gradients min(0, drho/dz) - epsln that every slope divides by (:121, :158,
+//   :188, :207): one for the face below the point (kr = 0) and one above
+//   (kr = 1). Two planes (k and k+1) live in shared memory.
+// * Grid divisions become multiplications by reciprocals computed once per
+//   CTA; slope divisions become multiplications by the shared reciprocals.
+// * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
+//   Taylor polynomial on [-4, 2) (taper_table.inc, truncation error < 5e-17),
+//   the library tanh elsewhere, and an FP32 exp below x = -10 where the taper
+//   is below 2e-9 and the reference itself carries ~1e-16 absolute error.
+// * Faces whose mask is zero skip the slope work and store the zeros the
+//   reference's mask multiplication produces.
+//
+// Outputs are written only on the reference's sub-ranges (K_11[1:-2,2:-2],
+// K_22[2:-2,1:-2], K_33[2:-2,2:-2,:-1], K_33[...,-1] = 0, Ai_* likewise); all
+// other cells keep their contents.
 #include "common.cuh"
 
 namespace vg {
 
+#include "taper_table.inc"
+
 namespace {
 
 constexpr double kEpsln = 1e-20;  // isoneutral.py:28
+constexpr int TX = 32, TY = 8, NT = TX * TY;
+constexpr int PX = TX + 2, PY = TY + 2, NP = PX * PY;  // point region: tile + 1-cell ring
+constexpr int kPtSlots = (NP + NT - 1) / NT;
+enum { Q_RT, Q_RS, Q_TX, Q_SX, Q_TY, Q_SY, Q_R0, Q_R1, NQ };
 
 struct PreArgs {
   Layout L;
   Grid g;
-  Eos eos;
-  double slopec, dslope, ksteep;
+  int eos_type;
+  double slopec, inv_dslope, ksteep;
   const double *__restrict__ T;
   const double *__restrict__ S;
   const double *__restrict__ K;
   const uint8_t *__restrict__ m;
   double *K11, *K22, *K33, *Aez, *Anz, *Abx, *Aby;
   long long sp, sr;
+  int kchunk;
 };
 
-struct Fields {
-  const PreArgs &a;
-  __device__ __forceinline__ double T(int i, int j, int k) const { return __ldg(a.T + a.L.at(i, j, k)); }
-  __device__ __forceinline__ double S(int i, int j, int k) const { return __ldg(a.S + a.L.at(i, j, k)); }
-  __device__ __forceinline__ unsigned M(int i, int j, int k) const { return __ldg(a.m + a.L.at(i, j, k)); }
-  // drho/dT and drho/dS at T points, masked (isoneutral.py:40-41)
-  __device__ __forceinline__ double drdT(int i, int j, int k) const {
-    return (M(i, j, k) & VG_MASK_T) ? a.eos.drdT(T(i, j, k), a.g.zt[k]) : 0.0;
-  }
-  __device__ __forceinline__ double drdS(int i, int j, int k) const {
-    return (M(i, j, k) & VG_MASK_T) ? a.eos.drdS() : 0.0;
-  }
-  // gradients at the top face (isoneutral.py:46-59); zero on the top level
-  __device__ __forceinline__ double dTdz(int i, int j, int k) const {
-    if (k >= a.L.Z - 1 || !(M(i, j, k) & VG_MASK_W)) return 0.0;
-    return (T(i, j, k + 1) - T(i, j, k)) / a.g.dzw[k];
-  }
-  __device__ __forceinline__ double dSdz(int i, int j, int k) const {
-    if (k >= a.L.Z - 1 || !(M(i, j, k) & VG_MASK_W)) return 0.0;
-    return (S(i, j, k + 1) - S(i, j, k)) / a.g.dzw[k];
-  }
-  // gradients at the east face (isoneutral.py:64-77); zero on the last column
-  __device__ __forceinline__ double dTdx(int i, int j, int k) const {
-    if (i >= a.L.X - 1 || !(M(i, j, k) & VG_MASK_U)) return 0.0;
-    return (T(i + 1, j, k) - T(i, j, k)) / (a.g.dxu[i] * a.g.cost[j]);
-  }
-  __device__ __forceinline__ double dSdx(int i, int j, int k) const {
-    if (i >= a.L.X - 1 || !(M(i, j, k) & VG_MASK_U)) return 0.0;
-    return (S(i + 1, j, k) - S(i, j, k)) / (a.g.dxu[i] * a.g.cost[j]);
-  }
-  // gradients at the north face (isoneutral.py:82-95); zero on the last row
-  __device__ __forceinline__ double dTdy(int i, int j, int k) const {
-    if (j >= a.L.Y - 1 || !(M(i, j, k) & VG_MASK_V)) return 0.0;
-    return (T(i, j + 1, k) - T(i, j, k)) / a.g.dyu[j];
-  }
-  __device__ __forceinline__ double dSdy(int i, int j, int k) const {
-    if (j >= a.L.Y - 1 || !(M(i, j, k) & VG_MASK_V)) return 0.0;
-    return (S(i, j + 1, k) - S(i, j, k)) / a.g.dyu[j];
-  }
+struct Smem {
+  double q[2][NQ][NP];
+  double inv_dxu[PX], inv_dyu[PY], inv_cost[PY], facty[PY];
+  double qinv_dxt[PX], qinv_dyt_cost[PY], dxu[PX];
+  // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant
 };
 
-// dm_taper (isoneutral.py:10-15)
-__device__ __forceinline__ double taper_of(double sx, double slopec, double dslope) {
-  return 0.5 * (1.0 + tanh((-fabs(sx) + slopec) / dslope));
+__device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
+  const double x = (slopec - fabs(s)) * inv_dslope;
+  if (x >= kTaperX0 && x < kTaperX1) {
+    int idx = (int)((x - kTaperX0) * kTaperPerUnit);
+    idx = idx < kTaperN - 1 ? idx : kTaperN - 1;
+    const double b = x - (kTaperX0 + ((double)idx + 0.5) * (1.0 / kTaperPerUnit));
+    const double *c = kTaperCoef[idx];
+    double r = __ldg(c + 6);
+    r = fma(r, b, __ldg(c + 5));
+    r = fma(r, b, __ldg(c + 4));
+    r = fma(r, b, __ldg(c + 3));
+    r = fma(r, b, __ldg(c + 2));
+    r = fma(r, b, __ldg(c + 1));
+    return fma(r, b, __ldg(c + 0));
+  }
+  if (x < -10.0) return (double)expf(2.0f * (float)x);
+  return 0.5 * (1.0 + tanh(x));
 }
 
-__device__ __forceinline__ double slope_of(double num, double den) { return -num / (fmin(0.0, den) - kEpsln); }
-
-__global__ void __launch_bounds__(128) pre_cell_kernel(PreArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  const int k = blockIdx.z;
+__global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
+  double *zdzw = reinterpret_cast<double *>(smem_raw + sizeof(Smem));
   const Layout &L = a.L;
-  if (i >= L.X) return;
-  Fields f{a};
-  const long long o = L.at(i, j, k);
+  const int Z = L.Z;
+  double *zinv_dzw = zdzw + Z;
+  double *zq_dzt = zinv_dzw + Z;
+  double *zeos = zq_dzt + Z;
 
-  // K_33 on the top level is zero everywhere (isoneutral.py:225)
-  if (k == L.Z - 1) a.K33[o] = 0.0;
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int i0 = 1 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
+  const int kb = blockIdx.z * a.kchunk;
+  const int ke = min(Z, kb + a.kchunk);
 
-  // east face: Ai_ez and K_11 (isoneutral.py:100-132)
-  if (i >= 1 && i < L.X - 2 && j >= 2 && j < L.Y - 2) {
-    const bool mU = f.M(i, j, k) & VG_MASK_U;
-    double diffloc;
-    if (k >= 1)
-      diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + L.at(i, j, k - 1)) + __ldg(a.K + L.at(i + 1, j, k)) +
-                        __ldg(a.K + L.at(i + 1, j, k - 1)));
-    else
-      diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + L.at(i + 1, j, 0)));
-    const double dTx = f.dTdx(i, j, k), dSx = f.dSdx(i, j, k);
-    double sumz = 0.0;
-#pragma unroll
-    for (int kr = 0; kr < 2; ++kr) {
-      const int ki = kr == 1 ? 0 : 1;
-      if (k < ki) continue;
-#pragma unroll
-      for (int ip = 0; ip < 2; ++ip) {
-        const double rT = f.drdT(i + ip, j, k), rS = f.drdS(i + ip, j, k);
-        const double drodxe = rT * dTx + rS * dSx;
-        const double drodze = rT * f.dTdz(i + ip, j, k - 1 + kr) + rS * f.dSdz(i + ip, j, k - 1 + kr);
-        const double sxe = slope_of(drodxe, drodze);
-        const double taper = taper_of(sxe, a.slopec, a.dslope);
-        sumz += a.g.dzw[k - 1 + kr] * (mU ? 1.0 : 0.0) * fmax(a.ksteep, diffloc * taper);
-        a.Aez[o + ip * a.sp + kr * a.sr] = taper * sxe * (mU ? 1.0 : 0.0);
-      }
-    }
-    a.K11[o] = sumz / (4.0 * a.g.dzt[k]);
+  // ---- per-CTA grid tables ------------------------------------------------
+  for (int p = tid; p < PX; p += NT) {
+    const int i = min(max(i0 - 1 + p, 0), L.X - 1);
+    sm.inv_dxu[p] = 1.0 / a.g.dxu[i];
+    sm.qinv_dxt[p] = 1.0 / (4.0 * a.g.dxt[i]);
+    sm.dxu[p] = a.g.dxu[i];
+  }
+  for (int p = tid; p < PY; p += NT) {
+    const int j = min(max(j0 - 1 + p, 0), L.Y - 1);
+    sm.inv_dyu[p] = 1.0 / a.g.dyu[j];
+    sm.inv_cost[p] = 1.0 / a.g.cost[j];
+    sm.facty[p] = a.g.cosu[j] * a.g.dyu[j];  // isoneutral.py:202
+    sm.qinv_dyt_cost[p] = 1.0 / (4.0 * a.g.dyt[j] * a.g.cost[j]);
+  }
+  for (int k = tid; k < Z; k += NT) {
+    zdzw[k] = a.g.dzw[k];
+    zinv_dzw[k] = 1.0 / a.g.dzw[k];
+    zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
+    // eq type 3: drho/dT = -(betaTs*(T - theta0) + betaT*(1 - gammas*grav*zz*rho0))*rho0
+    const double zz = -fabs(a.g.zt[k]) - 0.0;
+    zeos[k] = Eos::betaT * (1.0 - Eos::gammas * Eos::grav * zz * Eos::rho0);
   }
 
-  // north face: Ai_nz and K_22 (isoneutral.py:137-168)
-  if (i >= 2 && i < L.X - 2 && j >= 1 && j < L.Y - 2) {
-    const bool mV = f.M(i, j, k) & VG_MASK_V;
-    double diffloc;
-    if (k >= 1)
-      diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + L.at(i, j, k - 1)) + __ldg(a.K + L.at(i, j + 1, k)) +
-                        __ldg(a.K + L.at(i, j + 1, k - 1)));
-    else
-      diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + L.at(i, j + 1, 0)));
-    const double dTy = f.dTdy(i, j, k), dSy = f.dSdy(i, j, k);
-    double sumz = 0.0;
-#pragma unroll
-    for (int kr = 0; kr < 2; ++kr) {
-      const int ki = kr == 1 ? 0 : 1;
-      if (k < ki) continue;
-#pragma unroll
-      for (int jp = 0; jp < 2; ++jp) {
-        const double rT = f.drdT(i, j + jp, k), rS = f.drdS(i, j + jp, k);
-        const double drodyn = rT * dTy + rS * dSy;
-        const double drodzn = rT * f.dTdz(i, j + jp, k - 1 + kr) + rS * f.dSdz(i, j + jp, k - 1 + kr);
-        const double syn = slope_of(drodyn, drodzn);
-        const double taper = taper_of(syn, a.slopec, a.dslope);
-        sumz += a.g.dzw[k - 1 + kr] * (mV ? 1.0 : 0.0) * fmax(a.ksteep, diffloc * taper);
-        a.Anz[o + jp * a.sp + kr * a.sr] = taper * syn * (mV ? 1.0 : 0.0);
-      }
+  // K_33 on the top level is zero on the whole plane (isoneutral.py:225)
+  if (ke == Z) {
+    for (int p = tid; p < (PX + 1) * (PY + 1); p += NT) {
+      const int i = i0 - 1 + p % (PX + 1), j = j0 - 1 + p / (PX + 1);
+      if (i < L.X && j < L.Y) a.K33[L.at(i, j, Z - 1)] = 0.0;
     }
-    a.K22[o] = sumz / (4.0 * a.g.dzt[k]);
   }
+  __syncthreads();
 
-  // top face: Ai_bx, Ai_by and K_33 (isoneutral.py:173-224)
-  if (i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2 && k < L.Z - 1) {
-    const bool mW = f.M(i, j, k) & VG_MASK_W;
-    const double wm = mW ? 1.0 : 0.0;
-    const double Kc = __ldg(a.K + o);
-    const double dTz = f.dTdz(i, j, k), dSz = f.dSdz(i, j, k);
-    double sumx = 0.0, sumy = 0.0;
+  // ---- per-point plane quantities ------------------------------------------
+  double carryT[kPtSlots], carryS[kPtSlots];  // dT/dz, dS/dz of the previous level per point slot
 #pragma unroll
-    for (int kr = 0; kr < 2; ++kr) {
-      const double rT = f.drdT(i, j, k + kr), rS = f.drdS(i, j, k + kr);
-      const double drodzb = rT * dTz + rS * dSz;
+  for (int s = 0; s < kPtSlots; ++s) carryT[s] = carryS[s] = 0.0;
+
+  auto compute_plane = [&](int lev, int buf, bool store) {
 #pragma unroll
-      for (int ip = 0; ip < 2; ++ip) {
-        const double drodxb = rT * f.dTdx(i - 1 + ip, j, k + kr) + rS * f.dSdx(i - 1 + ip, j, k + kr);
-        const double sxb = slope_of(drodxb, drodzb);
-        const double taper = taper_of(sxb, a.slopec, a.dslope);
-        sumx = sumx + a.g.dxu[i - 1 + ip] * Kc * taper * (sxb * sxb) * wm;
-        a.Abx[o + ip * a.sp + kr * a.sr] = taper * sxb * wm;
+    for (int s = 0; s < kPtSlots; ++s) {
+      const int p = tid + s * NT;
+      if (p >= NP) break;
+      const int pi = p % PX, pj = p / PX;
+      const int i = i0 - 1 + pi, j = j0 - 1 + pj;
+      double rT = 0, rS = 0, dTx = 0, dSx = 0, dTy = 0, dSy = 0, dTz = 0, dSz = 0;
+      if (i < L.X && j < L.Y) {
+        const long long o = L.at(i, j, lev);
+        const unsigned mk = __ldg(a.m + o);
+        const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
+        if (mk & VG_MASK_T) {
+          if (a.eos_type == 1)
+            rT = -Eos::betaT * Eos::rho0;
+          else if (a.eos_type == 3)
+            rT = -(Eos::betaTs3 * (Tc - Eos::theta0) + zeos[lev]) * Eos::rho0;
+          else
+            rT = -(Eos::betaT + 2.0 * Eos::betaTs24 * (Tc - Eos::theta0)) * Eos::rho0;
+          rS = a.eos_type == 4 ? 0.0 : Eos::betaS * Eos::rho0;
+        }
+        if ((mk & VG_MASK_U) && i < L.X - 1) {
+          const double f = sm.inv_dxu[pi] * sm.inv_cost[pj];
+          dTx = (__ldg(a.T + o + 1) - Tc) * f;
+          dSx = (__ldg(a.S + o + 1) - Sc) * f;
+        }
+        if ((mk & VG_MASK_V) && j < L.Y - 1) {
+          dTy = (__ldg(a.T + o + L.pitch) - Tc) * sm.inv_dyu[pj];
+          dSy = (__ldg(a.S + o + L.pitch) - Sc) * sm.inv_dyu[pj];
+        }
+        if ((mk & VG_MASK_W) && lev < Z - 1) {
+          dTz = (__ldg(a.T + o + L.plane) - Tc) * zinv_dzw[lev];
+          dSz = (__ldg(a.S + o + L.plane) - Sc) * zinv_dzw[lev];
+        }
       }
-#pragma unroll
-      for (int jp = 0; jp < 2; ++jp) {
-        const double facty = a.g.cosu[j - 1 + jp] * a.g.dyu[j - 1 + jp];
-        const double drodyb = rT * f.dTdy(i, j - 1 + jp, k + kr) + rS * f.dSdy(i, j - 1 + jp, k + kr);
-        const double syb = slope_of(drodyb, drodzb);
-        const double taper = taper_of(syb, a.slopec, a.dslope);
-        sumy = sumy + facty * Kc * taper * (syb * syb) * wm;
-        a.Aby[o + jp * a.sp + kr * a.sr] = taper * syb * wm;
+      if (store) {
+        const double G0 = rT * carryT[s] + rS * carryS[s];  // face below (kr = 0)
+        const double G1 = rT * dTz + rS * dSz;              // face above (kr = 1)
+        double(*q)[NP] = sm.q[buf];
+        q[Q_RT][p] = rT;
+        q[Q_RS][p] = rS;
+        q[Q_TX][p] = dTx;
+        q[Q_SX][p] = dSx;
+        q[Q_TY][p] = dTy;
+        q[Q_SY][p] = dSy;
+        q[Q_R0][p] = 1.0 / (fmin(0.0, G0) - kEpsln);
+        q[Q_R1][p] = 1.0 / (fmin(0.0, G1) - kEpsln);
       }
+      carryT[s] = dTz;
+      carryS[s] = dSz;
     }
-    a.K33[o] = sumx / (4.0 * a.g.dxt[i]) + sumy / (4.0 * a.g.dyt[j] * a.g.cost[j]);
+  };
+
+  if (kb > 0) compute_plane(kb - 1, 0, false);  // only the carries
+  compute_plane(kb, kb & 1, true);
+
+  const int i = i0 + tx, j = j0 + ty;
+  const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
+  const bool east = i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  const bool north = i >= 2 && i < L.X - 2 && j < L.Y - 2;
+  const bool top = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
+
+  for (int k = kb; k < ke; ++k) {
+    if (k + 1 < Z) compute_plane(k + 1, (k + 1) & 1, true);
+    __syncthreads();
+    const double(*q)[NP] = sm.q[k & 1];
+    const double(*qn)[NP] = sm.q[(k + 1) & 1];
+    const long long o = L.at(i, j, k);
+    unsigned mk = 0;
+    if (east || north) mk = __ldg(a.m + o);
+
+    // east face: Ai_ez, K_11 (isoneutral.py:100-132)
+    if (east) {
+      double sumz = 0.0;
+      if (mk & VG_MASK_U) {
+        double diffloc;
+        if (k >= 1)
+          diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + 1) +
+                            __ldg(a.K + o + 1 - L.plane));
+        else
+          diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + o + 1));
+        const double dTx = q[Q_TX][pc], dSx = q[Q_SX][pc];
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+#pragma unroll
+          for (int ip = 0; ip < 2; ++ip) {
+            const int pp = pc + ip;
+            const double s = -(q[Q_RT][pp] * dTx + q[Q_RS][pp] * dSx) * q[kr ? Q_R1 : Q_R0][pp];
+            const double tp = taper_of(s, a.slopec, a.inv_dslope);
+            sumz += zdzw[k - 1 + kr] * fmax(a.ksteep, diffloc * tp);
+            a.Aez[o + ip * a.sp + kr * a.sr] = tp * s;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+          a.Aez[o + kr * a.sr] = 0.0;
+          a.Aez[o + a.sp + kr * a.sr] = 0.0;
+        }
+      }
+      a.K11[o] = sumz * zq_dzt[k];
+    }
+
+    // north face: Ai_nz, K_22 (isoneutral.py:137-168)
+    if (north) {
+      double sumz = 0.0;
+      if (mk & VG_MASK_V) {
+        double diffloc;
+        if (k >= 1)
+          diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + L.pitch) +
+                            __ldg(a.K + o + L.pitch - L.plane));
+        else
+          diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
+        const double dTy = q[Q_TY][pc], dSy = q[Q_SY][pc];
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+#pragma unroll
+          for (int jp = 0; jp < 2; ++jp) {
+            const int pp = pc + jp * PX;
+            const double s = -(q[Q_RT][pp] * dTy + q[Q_RS][pp] * dSy) * q[kr ? Q_R1 : Q_R0][pp];
+            const double tp = taper_of(s, a.slopec, a.inv_dslope);
+            sumz += zdzw[k - 1 + kr] * fmax(a.ksteep, diffloc * tp);
+            a.Anz[o + jp * a.sp + kr * a.sr] = tp * s;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+          a.Anz[o + kr * a.sr] = 0.0;
+          a.Anz[o + a.sp + kr * a.sr] = 0.0;
+        }
+      }
+      a.K22[o] = sumz * zq_dzt[k];
+    }
+
+    // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224)
+    if (top && k < Z - 1) {
+      double sumx = 0.0, sumy = 0.0;
+      if (mk & VG_MASK_W) {
+        const double Kc = __ldg(a.K + o);
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          const double(*qq)[NP] = kr ? qn : q;
+          const double rT = qq[Q_RT][pc], rS = qq[Q_RS][pc];
+          const double Rz = kr ? qn[Q_R0][pc] : q[Q_R1][pc];
+#pragma unroll
+          for (int ip = 0; ip < 2; ++ip) {
+            const int pp = pc - 1 + ip;
+            const double s = -(rT * qq[Q_TX][pp] + rS * qq[Q_SX][pp]) * Rz;
+            const double tp = taper_of(s, a.slopec, a.inv_dslope);
+            sumx += sm.dxu[tx + ip] * Kc * tp * (s * s);
+            a.Abx[o + ip * a.sp + kr * a.sr] = tp * s;
+          }
+#pragma unroll
+          for (int jp = 0; jp < 2; ++jp) {
+            const int pp = pc - PX + jp * PX;
+            const double s = -(rT * qq[Q_TY][pp] + rS * qq[Q_SY][pp]) * Rz;
+            const double tp = taper_of(s, a.slopec, a.inv_dslope);
+            sumy += sm.facty[ty + jp] * Kc * tp * (s * s);
+            a.Aby[o + jp * a.sp + kr * a.sr] = tp * s;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const long long oc = o + (c >> 1) * a.sp + (c & 1) * a.sr;
+          a.Abx[oc] = 0.0;
+          a.Aby[oc] = 0.0;
+        }
+      }
+      a.K33[o] = sumx * sm.qinv_dxt[tx + 1] + sumy * sm.qinv_dyt_cost[ty + 1];
+    }
+    __syncthreads();
   }
 }
 
@@ -195,12 +329,13 @@ extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, co
   if (set->eq_of_state_type < 1 || set->eq_of_state_type > 4)
     return fail(VG_ERR_UNSUPPORTED, "eq_of_state_type %d not implemented (1-4 are)", set->eq_of_state_type);
   if (!(set->iso_dslope != 0.0)) return fail(VG_ERR_ARG, "iso_dslope must be non-zero");
+  if (dom->Z > 512) return fail(VG_ERR_SHAPE, "Z=%d above the 512 levels the per-CTA tables hold", dom->Z);
   PreArgs a;
   a.L = layout_of(dom);
   a.g = grid_of(grid);
-  a.eos = Eos{set->eq_of_state_type};
+  a.eos_type = set->eq_of_state_type;
   a.slopec = set->iso_slopec;
-  a.dslope = set->iso_dslope;
+  a.inv_dslope = 1.0 / set->iso_dslope;
   a.ksteep = set->K_iso_steep;
   a.T = temp_tau;
   a.S = salt_tau;
@@ -215,8 +350,15 @@ extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, co
   a.Aby = out->Ai_by;
   a.sp = out->ai_stride_p;
   a.sr = out->ai_stride_r;
-  dim3 block(128);
-  dim3 g((a.L.X + 127) / 128, a.L.Y, a.L.Z);
-  pre_cell_kernel<<<g, block, 0, as_stream(stream)>>>(a);
-  return check_launch("pre_cell_kernel");
+  // k-chunking: enough CTAs for two per SM on the 152 SMs of a GB300
+  const int nbx = (a.L.X - 3 + TX - 1) / TX, nby = (a.L.Y - 3 + TY - 1) / TY;
+  int nchunks = 1;
+  while ((long long)nbx * nby * nchunks < 2 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
+  a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
+  const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
+  const size_t smem = sizeof(Smem) + 4 * (size_t)a.L.Z * sizeof(double);
+  cudaError_t e = cudaFuncSetAttribute(pre_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_tile_kernel smem %zu: %s", smem, cudaGetErrorString(e));
+  pre_tile_kernel<<<dim3(nbx, nby, nbz), NT, smem, as_stream(stream)>>>(a);
+  return check_launch("pre_tile_kernel");
 }
