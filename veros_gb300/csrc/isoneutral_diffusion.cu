@@ -1,25 +1,31 @@
 // Isoneutral tracer diffusion (FP64), the work of
 // veros/core/isoneutral/diffusion.py:9-295 and veros/core/diffusion.py:9-62.
 //
-// Three launches per tracer:
-//  1. flux_kernel   one thread per cell: east, north and top fluxes
-//                   (diffusion.py:9-113) into a scratch triple; zero where the
-//                   reference leaves them unset.
-//  2. column_kernel one thread per interior column, walking k upward: flux
-//                   divergence (diffusion.py:116-139), explicit update, the
-//                   implicit K_33 solve in the operation order of LAPACK dgtsv
-//                   (the solver behind the reference's solve_implicit), with
-//                   the eliminated rows in shared memory (diffusion.py:142-169),
-//                   and the dtracer_iso accumulation (diffusion.py:196-205).
-//  3. energy_kernel (enable_conserve_energy only) one thread per cell:
-//                   dissipation on the W grid and the vertical-mixing term
-//                   added to P_diss (diffusion.py:234-281).
+// Two launches per tracer (three with the energy branch):
+//  1. flux_div_kernel  2.5-D tiled: a CTA owns 32 x 8 interior columns and
+//                      walks k upward. Per level it forms the east, north and
+//                      top fluxes (diffusion.py:9-113) of its faces plus the
+//                      west/south halo faces, exchanges them through shared
+//                      memory, and applies the divergence (:116-139), the
+//                      explicit update of tr[taup1] and the dtracer_iso
+//                      accumulation (:196-197). Grid divisions are
+//                      multiplications by per-thread reciprocals.
+//  2. implicit_kernel  (iso only) one thread per interior column: the
+//                      implicit K_33 solve (:142-169) in the operation order
+//                      of LAPACK dgtsv, the solver behind the reference's
+//                      solve_implicit (dgtsv.cuh), with the eliminated rows in
+//                      shared memory, and the second dtracer_iso term (:204).
+//  3. energy_kernel    (enable_conserve_energy) dissipation on the W grid and
+//                      the vertical-mixing term added to P_diss (:234-281),
+//                      from the fluxes step 1 saved in the scratch buffer.
 #include "common.cuh"
 #include "dgtsv.cuh"
 
 namespace vg {
 
 namespace {
+
+constexpr int TX = 32, TY = 8, NT = TX * TY;
 
 struct DiffArgs {
   Layout L;
@@ -42,107 +48,171 @@ struct DiffArgs {
   double *dtr_iso;
   const double *__restrict__ idr;  // int_drhodX at tau
   double *P;
-  double *fe, *fn, *ft;  // scratch fluxes
-  int iso;
+  double *fe, *fn, *ft;  // scratch fluxes (energy branch)
+  int iso, save_fluxes, kchunk;
 };
 
 __device__ __forceinline__ double ld(const double *p, long long o) { return __ldg(p + o); }
 
-__global__ void __launch_bounds__(128) flux_kernel(DiffArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  const int k = blockIdx.z;
+// east-face flux at cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
+__device__ __forceinline__ double flux_east(const DiffArgs &a, int i, int j, int k, double inv_cost_dxu,
+                                            double q_dzt) {
   const Layout &L = a.L;
-  if (i >= L.X) return;
   const long long o = L.at(i, j, k);
   const int Z = L.Z;
-  const int km = k > 0 ? k - 1 : 0;      // edge padding in z (utilities.py:24-35)
-  const int kp = k < Z - 1 ? k + 1 : Z - 1;
+  const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
+  const long long dp = k < Z - 1 ? L.plane : 0;
+  double diffloc;
+  if (k >= 1)
+    diffloc = 0.25 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o - L.plane) + a.s1 * ld(a.K, o + 1) +
+                      a.s1 * ld(a.K, o + 1 - L.plane));
+  else
+    diffloc = 0.5 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o + 1));
+  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + 1);
+  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + 1 - dm);
+  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + 1 + dp);
+  double sumz = 0.0;
+  sumz += diffloc * ld(a.Aez, o) * (t0 - t0m);
+  sumz += diffloc * ld(a.Aez, o + a.sp) * (t1 - t1m);
+  sumz += diffloc * ld(a.Aez, o + a.sr) * (t0p - t0);
+  sumz += diffloc * ld(a.Aez, o + a.sp + a.sr) * (t1p - t1);
+  return sumz * q_dzt + (t1 - t0) * inv_cost_dxu * ld(a.K11, o);
+}
 
-  // east face (diffusion.py:25-47)
-  double fe = 0.0;
-  if (i >= 1 && i < L.X - 2 && j >= 2 && j < L.Y - 2) {
-    const double K1c = a.s1 * ld(a.K, o), K1e = a.s1 * ld(a.K, L.at(i + 1, j, k));
-    double diffloc;
-    if (k >= 1)
-      diffloc = 0.25 * (K1c + a.s1 * ld(a.K, L.at(i, j, k - 1)) + K1e + a.s1 * ld(a.K, L.at(i + 1, j, k - 1)));
-    else
-      diffloc = 0.5 * (K1c + K1e);
-    double sumz = 0.0;
-#pragma unroll
-    for (int kr = 0; kr < 2; ++kr) {
-#pragma unroll
-      for (int ip = 0; ip < 2; ++ip) {
-        const double hi = ld(a.tr, L.at(i + ip, j, kr ? kp : k));
-        const double lo = ld(a.tr, L.at(i + ip, j, kr ? k : km));
-        sumz = sumz + diffloc * ld(a.Aez, o + ip * a.sp + kr * a.sr) * (hi - lo);
-      }
-    }
-    const double tc = ld(a.tr, o), te = ld(a.tr, L.at(i + 1, j, k));
-    fe = sumz / (4.0 * a.g.dzt[k]) + (te - tc) / (a.g.cost[j] * a.g.dxu[i]) * ld(a.K11, o);
-  }
-  a.fe[o] = fe;
+// north-face flux at cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
+__device__ __forceinline__ double flux_north(const DiffArgs &a, int i, int j, int k, double cosu, double inv_dyu,
+                                             double q_dzt) {
+  const Layout &L = a.L;
+  const long long o = L.at(i, j, k);
+  const long long P = L.pitch;
+  const int Z = L.Z;
+  const long long dm = k > 0 ? L.plane : 0;
+  const long long dp = k < Z - 1 ? L.plane : 0;
+  double diffloc;
+  if (k >= 1)
+    diffloc = 0.25 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o - L.plane) + a.s1 * ld(a.K, o + P) +
+                      a.s1 * ld(a.K, o + P - L.plane));
+  else
+    diffloc = 0.5 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o + P));
+  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + P);
+  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + P - dm);
+  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + P + dp);
+  double sumz = 0.0;
+  sumz += diffloc * ld(a.Anz, o) * (t0 - t0m);
+  sumz += diffloc * ld(a.Anz, o + a.sp) * (t1 - t1m);
+  sumz += diffloc * ld(a.Anz, o + a.sr) * (t0p - t0);
+  sumz += diffloc * ld(a.Anz, o + a.sp + a.sr) * (t1p - t1);
+  return cosu * (sumz * q_dzt + (t1 - t0) * inv_dyu * ld(a.K22, o));
+}
 
-  // north face (diffusion.py:52-77)
-  double fn = 0.0;
-  if (i >= 2 && i < L.X - 2 && j >= 1 && j < L.Y - 2) {
-    const double K1c = a.s1 * ld(a.K, o), K1n = a.s1 * ld(a.K, L.at(i, j + 1, k));
-    double diffloc;
-    if (k >= 1)
-      diffloc = 0.25 * (K1c + a.s1 * ld(a.K, L.at(i, j, k - 1)) + K1n + a.s1 * ld(a.K, L.at(i, j + 1, k - 1)));
-    else
-      diffloc = 0.5 * (K1c + K1n);
-    double sumz = 0.0;
-#pragma unroll
-    for (int kr = 0; kr < 2; ++kr) {
-#pragma unroll
-      for (int jp = 0; jp < 2; ++jp) {
-        const double hi = ld(a.tr, L.at(i, j + jp, kr ? kp : k));
-        const double lo = ld(a.tr, L.at(i, j + jp, kr ? k : km));
-        sumz = sumz + diffloc * ld(a.Anz, o + jp * a.sp + kr * a.sr) * (hi - lo);
-      }
-    }
-    const double tc = ld(a.tr, o), tn = ld(a.tr, L.at(i, j + 1, k));
-    fn = a.g.cosu[j] * (sumz / (4.0 * a.g.dzt[k]) + (tn - tc) / a.g.dyu[j] * ld(a.K22, o));
-  }
-  a.fn[o] = fn;
+// top-face flux at interior cell (i, j, k < Z-1) (diffusion.py:85-111)
+__device__ __forceinline__ double flux_top(const DiffArgs &a, long long o, double inv_cost, double cosu_s,
+                                           double cosu_c, double q_dxt, double q_dyt_cost) {
+  const Layout &L = a.L;
+  const long long P = L.pitch, Q = L.plane;
+  const double diffloc = a.s2 * ld(a.K, o);
+  const double tc = ld(a.tr, o), tcu = ld(a.tr, o + Q);
+  double sumx = 0.0;
+  sumx += diffloc * ld(a.Abx, o) * inv_cost * (tc - ld(a.tr, o - 1));
+  sumx += diffloc * ld(a.Abx, o + a.sr) * inv_cost * (tcu - ld(a.tr, o - 1 + Q));
+  sumx += diffloc * ld(a.Abx, o + a.sp) * inv_cost * (ld(a.tr, o + 1) - tc);
+  sumx += diffloc * ld(a.Abx, o + a.sp + a.sr) * inv_cost * (ld(a.tr, o + 1 + Q) - tcu);
+  double sumy = 0.0;
+  sumy += diffloc * ld(a.Aby, o) * cosu_s * (tc - ld(a.tr, o - P));
+  sumy += diffloc * ld(a.Aby, o + a.sr) * cosu_s * (tcu - ld(a.tr, o - P + Q));
+  sumy += diffloc * ld(a.Aby, o + a.sp) * cosu_c * (ld(a.tr, o + P) - tc);
+  sumy += diffloc * ld(a.Aby, o + a.sp + a.sr) * cosu_c * (ld(a.tr, o + P + Q) - tcu);
+  return sumx * q_dxt + sumy * q_dyt_cost;
+}
 
-  // top face (diffusion.py:85-111)
-  double ft = 0.0;
-  if (i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2 && k < Z - 1) {
-    const double diffloc = a.s2 * ld(a.K, o);
-    const double cost = a.g.cost[j];
-    double sumx = 0.0;
-#pragma unroll
-    for (int ip = 0; ip < 2; ++ip) {
-#pragma unroll
-      for (int kr = 0; kr < 2; ++kr) {
-        const double d = ld(a.tr, L.at(i + ip, j, k + kr)) - ld(a.tr, L.at(i - 1 + ip, j, k + kr));
-        sumx = sumx + diffloc * ld(a.Abx, o + ip * a.sp + kr * a.sr) / cost * d;
-      }
-    }
-    double sumy = 0.0;
-#pragma unroll
-    for (int jp = 0; jp < 2; ++jp) {
-#pragma unroll
-      for (int kr = 0; kr < 2; ++kr) {
-        const double d = ld(a.tr, L.at(i, j + jp, k + kr)) - ld(a.tr, L.at(i, j - 1 + jp, k + kr));
-        sumy = sumy + diffloc * ld(a.Aby, o + jp * a.sp + kr * a.sr) * a.g.cosu[j - 1 + jp] * d;
-      }
-    }
-    ft = sumx / (4.0 * a.g.dxt[i]) + sumy / (4.0 * a.g.dyt[j] * cost);
+__global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
+  __shared__ double fe_s[2][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
+  __shared__ double fn_s[2][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
+  extern __shared__ double zq_dzt[];      // 1/(4 dzt[k]), then 1/dzt[k]
+  const Layout &L = a.L;
+  const int Z = L.Z;
+  double *zinv_dzt = zq_dzt + Z;
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX, warp = tid / 32, lane = tid % 32;
+  const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
+  const int kb = blockIdx.z * a.kchunk, ke = min(Z, kb + a.kchunk);
+  for (int k = tid; k < Z; k += NT) {
+    zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
+    zinv_dzt[k] = 1.0 / a.g.dzt[k];
   }
-  a.ft[o] = ft;
+  __syncthreads();
+
+  const int i = i0 + tx, j = j0 + ty;
+  const bool own = i < L.X - 2 && j < L.Y - 2;
+  const int ic = min(i, L.X - 3), jc = min(j, L.Y - 3);
+  const double cost = a.g.cost[jc];
+  const double inv_cost = 1.0 / cost;
+  const double inv_cost_dxu = 1.0 / (cost * a.g.dxu[ic]);
+  const double cosu_c = a.g.cosu[jc], cosu_s = a.g.cosu[jc - 1];
+  const double inv_dyu = 1.0 / a.g.dyu[jc];
+  const double inv_fx = 1.0 / (cost * a.g.dxt[ic]);  // divergence factors (diffusion.py:127, :129)
+  const double inv_fy = 1.0 / (cost * a.g.dyt[jc]);
+  const double q_dxt = 1.0 / (4.0 * a.g.dxt[ic]);
+  const double q_dyt_cost = 1.0 / (4.0 * a.g.dyt[jc] * cost);
+  // halo faces: warp 0 the south row of north faces, warp 1 the west column of east faces
+  const int hi_n = i0 + lane;  // north face (hi_n, j0-1)
+  const bool halo_n = warp == 0 && hi_n < L.X - 2 && j0 - 1 < L.Y - 2;
+  const int hj_e = j0 + lane;  // east face (i0-1, hj_e)
+  const bool halo_e = warp == 1 && lane < TY && hj_e < L.Y - 2 && i0 - 1 < L.X - 2;
+  double h_cosu = 0, h_inv_dyu = 0, h_inv_cost_dxu = 0;
+  if (halo_n) {
+    h_cosu = a.g.cosu[j0 - 1];
+    h_inv_dyu = 1.0 / a.g.dyu[j0 - 1];
+  }
+  if (halo_e) h_inv_cost_dxu = 1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]);
+
+  double ft_prev = 0.0;
+  if (own && kb > 0) ft_prev = flux_top(a, L.at(i, j, kb - 1), inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
+
+  for (int k = kb; k < ke; ++k) {
+    // double-buffered exchange: the barrier of level k+1 orders level k's
+    // reads before level k+2's writes to the same buffer
+    const int b = k & 1;
+    const long long o = L.at(i, j, k);
+    double fe = 0, fn = 0, ft = 0;
+    if (own) {
+      fe = flux_east(a, i, j, k, inv_cost_dxu, zq_dzt[k]);
+      fn = flux_north(a, i, j, k, cosu_c, inv_dyu, zq_dzt[k]);
+      if (k < Z - 1) ft = flux_top(a, o, inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
+      fe_s[b][ty][tx + 1] = fe;
+      fn_s[b][ty + 1][tx] = fn;
+    }
+    if (halo_n) fn_s[b][0][lane] = flux_north(a, hi_n, j0 - 1, k, h_cosu, h_inv_dyu, zq_dzt[k]);
+    if (halo_e) fe_s[b][lane][0] = flux_east(a, i0 - 1, hj_e, k, h_inv_cost_dxu, zq_dzt[k]);
+    __syncthreads();
+    if (own) {
+      const double mT = (__ldg(a.m + o) & VG_MASK_T) ? 1.0 : 0.0;
+      double e = mT * ((fe - fe_s[b][ty][tx]) * inv_fx + (fn - fn_s[b][ty][tx]) * inv_fy);
+      e = e + mT * (ft - ft_prev) * zinv_dzt[k];  // k = 0: ft_prev = 0 (diffusion.py:132-137)
+      ft_prev = ft;
+      a.dtr_iso[o] = radd(a.dtr_iso[o], e);
+      a.trp[o] = radd(a.trp[o], rmul(a.dt, e));
+      if (a.save_fluxes) {
+        a.fe[o] = fe;
+        a.fn[o] = fn;
+        a.ft[o] = ft;
+      }
+    }
+    if (a.save_fluxes) {
+      if (halo_n) a.fn[L.at(hi_n, j0 - 1, k)] = fn_s[b][0][lane];
+      if (halo_e) a.fe[L.at(i0 - 1, hj_e, k)] = fe_s[b][lane][0];
+    }
+  }
 }
 
 // Row source of one column's implicit system (diffusion.py:154-164), read
 // back from global memory for the interchange path.
 struct ColSrc {
   const DiffArgs &a;
+  const double *dtdzw;
   long long base;
   int ks, Z;
   __device__ double delta(int k) const {
-    return k < Z - 1 ? rmul(rdiv(a.dt, a.g.dzw[k]), a.K33[base + (long long)k * a.L.plane]) : 0.0;
+    return k < Z - 1 ? rmul(dtdzw[k], a.K33[base + (long long)k * a.L.plane]) : 0.0;
   }
   __device__ double a_(int k) const { return rdiv(-delta(k - 1), a.g.dzt[k]); }
   __device__ double b(int k) const {
@@ -159,77 +229,55 @@ struct ColSrcView {
   __device__ double d(int k) const { return s.d(k); }
 };
 
-// Per interior column: explicit divergence, explicit update and (iso) the
-// implicit vertical solve in dgtsv's operation order. Shared memory holds the
-// eliminated diagonal and right-hand side of each thread's column, 2 * Z
-// doubles laid out [k][thread]; tr1 and the partial tendency are parked in
-// the output arrays between the two sweeps.
-__global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int ncols) {
+// One thread per interior column: the implicit solve on tr1 = tr[taup1] after
+// the explicit update. Shared memory: dt/dzw per level, then the eliminated
+// diagonal and right-hand side [k][thread] of each column.
+__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, int ncols_x, int ncols) {
   extern __shared__ double smem[];
-  const int t = threadIdx.x;
-  const int col = blockIdx.x * blockDim.x + t;
-  if (col >= ncols) return;
   const Layout &L = a.L;
   const int Z = L.Z;
+  const int t = threadIdx.x, nb = blockDim.x;
+  double *dtdzw = smem;
+  double *Ds = smem + Z;
+  double *Bs = Ds + (size_t)Z * nb;
+  for (int k = t; k < Z; k += nb) dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
+  __syncthreads();
+  const int col = blockIdx.x * nb + t;
+  if (col >= ncols) return;
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
-  const int nb = blockDim.x;
-  double *Ds = smem;
-  double *Bs = smem + (size_t)Z * nb;
-
-  const double cost = a.g.cost[j];
-  const double fx = cost * a.g.dxt[i];
-  const double fy = cost * a.g.dyt[j];
   const int ks = a.kbot[L.at2(i, j)] - 1;  // create_water_masks (utilities.py:38-48)
-  const bool solve = a.iso && ks >= 0;
-
-  double ft_prev = 0.0, delta_prev = 0.0, Dp = 0.0, Bp = 0.0, cp = 0.0;
-  bool interchange = false;
-  for (int k = 0; k < Z; ++k) {
-    const long long o = L.at(i, j, k);
-    const double mT = (__ldg(a.m + o) & VG_MASK_T) ? 1.0 : 0.0;
-    const double ftk = a.ft[o];
-    double e = mT * ((a.fe[o] - a.fe[o - 1]) / fx + (a.fn[o] - a.fn[o - L.pitch]) / fy);
-    if (k == 0)
-      e = e + mT * ftk / a.g.dzt[0];
-    else
-      e = e + mT * (ftk - ft_prev) / a.g.dzt[k];
-    ft_prev = ftk;
-    const double d1 = radd(a.dtr_iso[o], e);
-    const double tr1 = radd(a.trp[o], rmul(a.dt, e));
-    a.dtr_iso[o] = d1;
-    a.trp[o] = tr1;
-    if (solve) {
-      const double dzt = a.g.dzt[k];
-      const double delta = k < Z - 1 ? rmul(rdiv(a.dt, a.g.dzw[k]), ld(a.K33, o)) : 0.0;
-      if (k >= ks) {
-        const double ck = rdiv(-delta, dzt);
-        double Dk, Bk;
-        if (k == ks) {
-          Dk = radd(1.0, rdiv(delta, dzt));
-          Bk = tr1;
-        } else {
-          const double dl = rdiv(-delta_prev, dzt);
-          const double bk = radd(1.0, rdiv(radd(delta, delta_prev), dzt));
-          if (fabs(Dp) < fabs(dl)) interchange = true;
-          const double fact = rdiv(dl, Dp);
-          Dk = rsub(bk, rmul(fact, cp));
-          Bk = rsub(tr1, rmul(fact, Bp));
-        }
-        Ds[(size_t)k * nb + t] = Dk;
-        Bs[(size_t)k * nb + t] = Bk;
-        Dp = Dk;
-        Bp = Bk;
-        cp = ck;
-      }
-      delta_prev = delta;
-    }
-  }
-  if (!solve) return;
+  if (ks < 0 || ks >= Z) return;
   const long long base = L.at2(i, j);
+
+  double delta_prev = 0.0, Dp = 0.0, Bp = 0.0, cp = 0.0;
+  bool interchange = false;
+  for (int k = ks; k < Z; ++k) {
+    const long long o = base + (long long)k * L.plane;
+    const double dzt = a.g.dzt[k];
+    const double delta = k < Z - 1 ? rmul(dtdzw[k], ld(a.K33, o)) : 0.0;
+    const double tr1 = a.trp[o];
+    double Dk, Bk;
+    if (k == ks) {
+      Dk = radd(1.0, rdiv(delta, dzt));
+      Bk = tr1;
+    } else {
+      const double dl = rdiv(-delta_prev, dzt);
+      const double bk = radd(1.0, rdiv(radd(delta, delta_prev), dzt));
+      if (fabs(Dp) < fabs(dl)) interchange = true;
+      const double fact = rdiv(dl, Dp);
+      Dk = rsub(bk, rmul(fact, cp));
+      Bk = rsub(tr1, rmul(fact, Bp));
+    }
+    Ds[(size_t)k * nb + t] = Dk;
+    Bs[(size_t)k * nb + t] = Bk;
+    Dp = Dk;
+    Bp = Bk;
+    cp = rdiv(-delta, dzt);
+    delta_prev = delta;
+  }
   if (interchange) {
-    // rows that dgtsv would interchange: replay the elimination with pivoting
-    ColSrc src{a, base, ks, Z};
+    ColSrc src{a, dtdzw, base, ks, Z};
     dgtsv_slow_solve(ColSrcView{src}, ks, Z, Ds + t, nb);
   } else {
     double x = 0.0;
@@ -238,7 +286,7 @@ __global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int
       if (k == Z - 1) {
         x = rdiv(Bk, Dk);
       } else {
-        const double delta = rmul(rdiv(a.dt, a.g.dzw[k]), ld(a.K33, base + (long long)k * L.plane));
+        const double delta = rmul(dtdzw[k], ld(a.K33, base + (long long)k * L.plane));
         x = rdiv(rsub(Bk, rmul(rdiv(-delta, a.g.dzt[k]), x)), Dk);
       }
       Ds[(size_t)k * nb + t] = x;
@@ -253,14 +301,23 @@ __global__ void __launch_bounds__(64) column_kernel(DiffArgs a, int ncols_x, int
   }
 }
 
+// Scratch flux readers: zero outside the ranges the reference defines.
+__device__ __forceinline__ double fe_at(const DiffArgs &a, int i, int j, int k) {
+  return (i >= 1 && i < a.L.X - 2 && j >= 2 && j < a.L.Y - 2) ? a.fe[a.L.at(i, j, k)] : 0.0;
+}
+__device__ __forceinline__ double fn_at(const DiffArgs &a, int i, int j, int k) {
+  return (i >= 2 && i < a.L.X - 2 && j >= 1 && j < a.L.Y - 2) ? a.fn[a.L.at(i, j, k)] : 0.0;
+}
+
 // Dissipation at T points (veros/core/diffusion.py:9-36); zero on the outer ring.
 __device__ __forceinline__ double diss_at(const DiffArgs &a, int i, int j, int k) {
   const Layout &L = a.L;
   const long long o = L.at(i, j, k);
   const double c = 0.5 * a.grav / a.rho0;
   const double I0 = ld(a.idr, o);
-  const double ex = (ld(a.idr, o + 1) - I0) * a.fe[o] + (I0 - ld(a.idr, o - 1)) * a.fe[o - 1];
-  const double ny = (ld(a.idr, o + L.pitch) - I0) * a.fn[o] + (I0 - ld(a.idr, o - L.pitch)) * a.fn[o - L.pitch];
+  const double ex = (ld(a.idr, o + 1) - I0) * fe_at(a, i, j, k) + (I0 - ld(a.idr, o - 1)) * fe_at(a, i - 1, j, k);
+  const double ny =
+      (ld(a.idr, o + L.pitch) - I0) * fn_at(a, i, j, k) + (I0 - ld(a.idr, o - L.pitch)) * fn_at(a, i, j - 1, k);
   const double cost = a.g.cost[j];
   return c * ex / (a.g.dxt[i] * cost) + c * ny / (a.g.dyt[j] * cost);
 }
@@ -331,6 +388,7 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
   if (set->enable_conserve_energy && (!tr->int_drhodX_tau || !tr->P_diss))
     return fail(VG_ERR_ARG, "enable_conserve_energy needs int_drhodX_tau and P_diss");
   if (!(set->dt_tracer != 0.0)) return fail(VG_ERR_ARG, "dt_tracer must be non-zero");
+  if (dom->Z > 512) return fail(VG_ERR_SHAPE, "Z=%d above the 512 levels supported", dom->Z);
   const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
   if (!scratch || scratch_bytes < need)
     return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
@@ -360,6 +418,7 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
   a.dtr_iso = tr->dtracer_iso;
   a.idr = tr->int_drhodX_tau;
   a.P = tr->P_diss;
+  a.save_fluxes = set->enable_conserve_energy ? 1 : 0;
   const size_t fsz = (size_t)a.L.plane * a.L.Z;
   a.fe = static_cast<double *>(scratch);
   a.fn = a.fe + fsz;
@@ -368,21 +427,25 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
   cudaStream_t s = as_stream(stream);
 
   {
-    dim3 block(128);
-    dim3 g((a.L.X + 127) / 128, a.L.Y, a.L.Z);
-    flux_kernel<<<g, block, 0, s>>>(a);
-    if ((st = check_launch("flux_kernel"))) return st;
+    const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
+    int nchunks = 1;
+    while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
+    a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
+    const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
+    const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
+    flux_div_kernel<<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
+    if ((st = check_launch("flux_div_kernel"))) return st;
   }
-  {
+  if (a.iso) {
     const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
     const int nb = 64;
-    const size_t smem = 2 * (size_t)a.L.Z * nb * sizeof(double);
+    const size_t smem = ((size_t)a.L.Z + 2 * (size_t)a.L.Z * nb) * sizeof(double);
     if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "column_kernel smem %zu: %s", smem, cudaGetErrorString(e));
+      cudaError_t e = cudaFuncSetAttribute(implicit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
     }
-    column_kernel<<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, ncols_x, ncols);
-    if ((st = check_launch("column_kernel"))) return st;
+    implicit_kernel<<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, ncols_x, ncols);
+    if ((st = check_launch("implicit_kernel"))) return st;
   }
   if (set->enable_conserve_energy) {
     dim3 block(128);
