@@ -111,6 +111,22 @@ int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const V
                                 const VgTracerArgs *tr, int skew,
                                 void *scratch, size_t scratch_bytes, void *stream);
 
+/* Scratch-free variant of vg_isoneutral_diffusion_f64 for callers that cannot
+ * allocate device memory (an XLA custom-call or FFI handler working only with
+ * the buffers it is handed, or a host model that fixes its device memory at
+ * start-up). No counterpart in the reference. The scratch is a 32 MiB
+ * file-scope device array held by every GPU that loads the library; domains
+ * needing more (3 * plane * Z * 8 bytes) get VG_ERR_SCRATCH. The first call
+ * on a device looks up the array's address (make it before any stream
+ * capture); all calls share the array, so calls overlapping on the GPU race.
+ * Allocates nothing. */
+int vg_isoneutral_diffusion_noalloc_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                        const VgTensorFields *ten, const double *K_field,
+                                        const uint8_t *mask_bits, const int32_t *kbot,
+                                        const VgTracerArgs *tr, int skew, void *stream);
+/* Bytes of the static scratch array vg_isoneutral_diffusion_noalloc_f64 uses. */
+size_t vg_isoneutral_diffusion_noalloc_capacity(void);
+
 /* Fields of one rollout step (vg_isoneutral_step_f64). */
 typedef struct VgStepFields {
   const double *temp_tau;

@@ -455,3 +455,77 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
   }
   return VG_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Scratch-free variant of vg_isoneutral_diffusion_f64.
+//
+// The diffusion needs a scratch triple of flux fields when the energy branch
+// is on. Some callers cannot call cudaMalloc to provide it: an XLA custom-call
+// or FFI handler (JAX reserves most of the GPU's memory for its own pool and
+// the handler may only touch the buffers it is handed), or a host model that
+// fixes all of its device memory at start-up and forbids allocation inside
+// the time loop. For them this entry point keeps the scratch in a file-scope
+// device array instead.
+//
+// * Limit: the array holds kNoAllocScratchBytes (32 MiB), enough for domains
+//   with 3 * plane * Z * 8 bytes <= 32 MiB (for example 80 x 60 x 60 interior
+//   cells); larger domains are rejected with VG_ERR_SCRATCH before anything is
+//   enqueued. Every GPU that loads this library holds the array until the
+//   process exits.
+// * Set-up: the first call on a device (with that device current) looks up
+//   the array's device address with cudaGetSymbolAddress and caches it per
+//   device; make that first call before any stream capture. Host code must
+//   never pass the array's name itself to a kernel: in host code it is only a
+//   stand-in, not a device address.
+// * Sharing: every call uses the same array, which keeps the last call's
+//   contents. Nothing in it has to start at zero (each call writes every
+//   scratch cell it later reads), but calls that overlap on the GPU (on
+//   different streams, or concurrently from several host threads) race on it.
+// * No allocation: this function calls no cudaMalloc, cudaFree or allocating
+//   library routine.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace vg {
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+}  // namespace vg
+
+extern "C" size_t vg_isoneutral_diffusion_noalloc_capacity(void) { return vg::kNoAllocScratchBytes; }
+
+extern "C" int vg_isoneutral_diffusion_noalloc_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                                   const VgTensorFields *ten, const double *K_field,
+                                                   const uint8_t *mask_bits, const int32_t *kbot,
+                                                   const VgTracerArgs *tr, int skew, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
+  if (need > kNoAllocScratchBytes)
+    return fail(VG_ERR_SCRATCH,
+                "vg_isoneutral_diffusion_noalloc_f64: this domain needs %zu bytes of scratch but the static "
+                "buffer holds %zu (32 MiB); use vg_isoneutral_diffusion_f64 with caller-provided scratch",
+                need, kNoAllocScratchBytes);
+  int device = -1;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= kMaxDevices) return fail(VG_ERR_ARG, "device index %d out of range", device);
+  void *ptr = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return fail(VG_ERR_LAUNCH, "cudaGetSymbolAddress(scratch) on device %d: %s", device, cudaGetErrorString(e));
+      g_noalloc_ptr[device] = ptr;
+    }
+    ptr = g_noalloc_ptr[device];
+  }
+  return vg_isoneutral_diffusion_f64(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, ptr,
+                                     kNoAllocScratchBytes, stream);
+}
