@@ -202,7 +202,7 @@ def run_gb300(args):
         stepper.step_stages()
     torch.cuda.synchronize()
 
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
         dist.barrier()
@@ -216,7 +216,7 @@ def run_gb300(args):
     if dist:
         dist.barrier()
     ms = start.elapsed_time(stop)
-    stage_ms = np.array([[e[n].elapsed_time(e[n + 1]) for n in range(4)] for e in ev])
+    stage_ms = np.array([[e[n].elapsed_time(e[n + 1]) for n in range(3)] for e in ev])
     if dist:
         t = torch.tensor([ms], device=device, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -264,7 +264,7 @@ def run_gb300(args):
                    "l2": "inputs larger than L2: one step touches ~0.9 GB of fields (Ai_* alone 0.5 GB)",
                    "parallelism": f"replicas x{world}"},
         "stage_ms": {"prepare": float(stage_ms[:, 0].mean()), "pre": pre_ms,
-                     "diffusion_temp": float(stage_ms[:, 2].mean()), "diffusion_salt": float(stage_ms[:, 3].mean())},
+                     "diffusion_temp_and_salt": float(stage_ms[:, 2].mean())},
         "roofline": {"bound": "hbm", "kernel": "pre_tile_kernel", "achieved": pre_achieved, "peak": peak,
                      "unit": "GB/s", "frac": pre_achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "algorithmic_bytes_per_cell": PRE_BYTES_PER_CELL,

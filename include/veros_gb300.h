@@ -111,6 +111,18 @@ int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const V
                                 const VgTracerArgs *tr, int skew,
                                 void *scratch, size_t scratch_bytes, void *stream);
 
+/* Diffusion of temp and then salt with one shared factorisation of the
+ * implicit K_33 system (both tracers solve the same matrix): the same results
+ * as vg_isoneutral_diffusion_f64 for temp followed by salt
+ * (veros/core/thermodynamics.py:431-432), with fewer FP64 operations. Scratch:
+ * vg_isoneutral_diffusion_pair_scratch_bytes. */
+size_t vg_isoneutral_diffusion_pair_scratch_bytes(const VgDomain *dom);
+int vg_isoneutral_diffusion_pair_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                     const VgTensorFields *ten, const double *K_iso,
+                                     const uint8_t *mask_bits, const int32_t *kbot,
+                                     const VgTracerArgs *temp, const VgTracerArgs *salt,
+                                     void *scratch, size_t scratch_bytes, void *stream);
+
 /* Scratch-free variant of vg_isoneutral_diffusion_f64 for callers that cannot
  * allocate device memory (an XLA custom-call or FFI handler working only with
  * the buffers it is handed, or a host model that fixes its device memory at
@@ -147,7 +159,7 @@ typedef struct VgStepFields {
  * tr[taup1] = tr[tau] * maskT for temp and salt; dtemp_iso = dsalt_iso = 0
  * and P_diss_iso = 0 (if given; needed with the energy branch); pre; diffusion of temp; diffusion
  * of salt. The caller rotates the time levels (veros/veros.py:321-322).
- * Scratch as for vg_isoneutral_diffusion_f64. */
+ * Scratch as for vg_isoneutral_diffusion_pair_f64. */
 int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                            const VgStepFields *f, void *scratch, size_t scratch_bytes, void *stream);
 

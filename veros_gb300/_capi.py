@@ -78,6 +78,12 @@ SIGNATURES = {
                                                            ctypes.POINTER(VgTracerArgs), ctypes.c_int,
                                                            ctypes.c_void_p]),
     "vg_isoneutral_diffusion_noalloc_capacity": (ctypes.c_size_t, []),
+    "vg_isoneutral_diffusion_pair_scratch_bytes": (ctypes.c_size_t, [ctypes.POINTER(VgDomain)]),
+    "vg_isoneutral_diffusion_pair_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                        ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgTensorFields),
+                                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.POINTER(VgTracerArgs), ctypes.POINTER(VgTracerArgs),
+                                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_isoneutral_step_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                               ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgStepFields),
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -11,15 +11,15 @@
 //                      accumulation (:196-197). Grid divisions are
 //                      multiplications by per-thread reciprocals.
 //  2. implicit_kernel  (iso only) one thread per interior column: the
-//                      implicit K_33 solve (:142-169) in the operation order
-//                      of LAPACK dgtsv, the solver behind the reference's
-//                      solve_implicit (dgtsv.cuh), with the eliminated rows in
-//                      shared memory, and the second dtracer_iso term (:204).
+//                      implicit K_33 solve (:142-169) as a Thomas sweep whose
+//                      c'/d' live in shared memory, shared by temp and salt
+//                      when both are diffused together, and the second
+//                      dtracer_iso term (:204).
 //  3. energy_kernel    (enable_conserve_energy) dissipation on the W grid and
 //                      the vertical-mixing term added to P_diss (:234-281),
 //                      from the fluxes step 1 saved in the scratch buffer.
 #include "common.cuh"
-#include "dgtsv.cuh"
+#include "dgtsv.cuh"  // rounded arithmetic helpers
 
 namespace vg {
 
@@ -204,42 +204,40 @@ __global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
   }
 }
 
-// Row source of one column's implicit system (diffusion.py:154-164), read
-// back from global memory for the interchange path.
-struct ColSrc {
+// Row source of one column's implicit system (diffusion.py:154-164): the
+// matrix entries from K_33 and the grid, in the reference's operation order.
+struct ColMatrix {
   const DiffArgs &a;
-  const double *dtdzw;
+  const double *dtdzw;  // dt / dzw[k], per level
   long long base;
   int ks, Z;
   __device__ double delta(int k) const {
-    return k < Z - 1 ? rmul(dtdzw[k], a.K33[base + (long long)k * a.L.plane]) : 0.0;
+    return k < Z - 1 ? rmul(dtdzw[k], ld(a.K33, base + (long long)k * a.L.plane)) : 0.0;
   }
-  __device__ double a_(int k) const { return rdiv(-delta(k - 1), a.g.dzt[k]); }
-  __device__ double b(int k) const {
+  __device__ double lower(int k) const { return rdiv(-delta(k - 1), a.g.dzt[k]); }  // a_tri[k], k > ks
+  __device__ double diag(int k) const {                                              // b_tri / b_tri_edge
     return k == ks ? radd(1.0, rdiv(delta(k), a.g.dzt[k])) : radd(1.0, rdiv(radd(delta(k), delta(k - 1)), a.g.dzt[k]));
   }
-  __device__ double c(int k) const { return rdiv(-delta(k), a.g.dzt[k]); }
-  __device__ double d(int k) const { return a.trp[base + (long long)k * a.L.plane]; }
-};
-struct ColSrcView {
-  const ColSrc &s;
-  __device__ double a(int k) const { return s.a_(k); }
-  __device__ double b(int k) const { return s.b(k); }
-  __device__ double c(int k) const { return s.c(k); }
-  __device__ double d(int k) const { return s.d(k); }
+  __device__ double upper(int k) const { return rdiv(-delta(k), a.g.dzt[k]); }  // c_tri[k], k < Z-1
 };
 
-// One thread per interior column: the implicit solve on tr1 = tr[taup1] after
-// the explicit update. Shared memory: dt/dzw per level, then the eliminated
-// diagonal and right-hand side [k][thread] of each column.
-__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, int ncols_x, int ncols) {
+// Implicit solve of NRHS tracers sharing one matrix, one thread per column.
+// The system (diffusion.py:154-164) is an M-matrix that is diagonally
+// dominant by columns (|b_k| >= |a_{k+1}| + |c_{k-1}|), for which elimination
+// without interchanges is backward stable; the Thomas sweep in reciprocal form
+// keeps one division per level on the column's serial chain and none in the
+// back substitution. The matrix entries use the reference's divisions; the
+// factorisation is shared by the tracers. Shared memory holds c'_k and d'_k of
+// each tracer, [k][thread].
+template <int NRHS>
+__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, int ncols_x, int ncols) {
   extern __shared__ double smem[];
   const Layout &L = a.L;
   const int Z = L.Z;
   const int t = threadIdx.x, nb = blockDim.x;
   double *dtdzw = smem;
-  double *Ds = smem + Z;
-  double *Bs = Ds + (size_t)Z * nb;
+  double *cps = smem + Z;
+  double *dps = cps + (size_t)Z * nb;  // [r][k][thread]
   for (int k = t; k < Z; k += nb) dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
   __syncthreads();
   const int col = blockIdx.x * nb + t;
@@ -249,55 +247,91 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, int ncols_x, i
   const int ks = a.kbot[L.at2(i, j)] - 1;  // create_water_masks (utilities.py:38-48)
   if (ks < 0 || ks >= Z) return;
   const long long base = L.at2(i, j);
+  double *trp[2] = {a.trp, b2.trp};
+  double *dtr[2] = {a.dtr_iso, b2.dtr_iso};
+  const double inv_dt = 1.0 / a.dt;
 
-  double delta_prev = 0.0, Dp = 0.0, Bp = 0.0, cp = 0.0;
-  bool interchange = false;
-  for (int k = ks; k < Z; ++k) {
-    const long long o = base + (long long)k * L.plane;
-    const double dzt = a.g.dzt[k];
-    const double delta = k < Z - 1 ? rmul(dtdzw[k], ld(a.K33, o)) : 0.0;
-    const double tr1 = a.trp[o];
-    double Dk, Bk;
-    if (k == ks) {
-      Dk = radd(1.0, rdiv(delta, dzt));
-      Bk = tr1;
-    } else {
-      const double dl = rdiv(-delta_prev, dzt);
-      const double bk = radd(1.0, rdiv(radd(delta, delta_prev), dzt));
-      if (fabs(Dp) < fabs(dl)) interchange = true;
-      const double fact = rdiv(dl, Dp);
-      Dk = rsub(bk, rmul(fact, cp));
-      Bk = rsub(tr1, rmul(fact, Bp));
-    }
-    Ds[(size_t)k * nb + t] = Dk;
-    Bs[(size_t)k * nb + t] = Bk;
-    Dp = Dk;
-    Bp = Bk;
-    cp = rdiv(-delta, dzt);
-    delta_prev = delta;
+  // Loads run PF levels ahead of the serial chain (software pipelining): the
+  // chain itself only waits for FP64 latency, not for global memory.
+  constexpr int PF = 4;
+  double qK[PF], qT[PF][NRHS];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = ks + u;
+    const long long o = base + (long long)min(k, Z - 1) * L.plane;
+    qK[u] = k < Z - 1 ? ld(a.K33, o) : 0.0;
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? trp[r][o] : 0.0;
   }
-  if (interchange) {
-    ColSrc src{a, dtdzw, base, ks, Z};
-    dgtsv_slow_solve(ColSrcView{src}, ks, Z, Ds + t, nb);
-  } else {
-    double x = 0.0;
-    for (int k = Z - 1; k >= ks; --k) {
-      const double Dk = Ds[(size_t)k * nb + t], Bk = Bs[(size_t)k * nb + t];
-      if (k == Z - 1) {
-        x = rdiv(Bk, Dk);
-      } else {
-        const double delta = rmul(dtdzw[k], ld(a.K33, base + (long long)k * L.plane));
-        x = rdiv(rsub(Bk, rmul(rdiv(-delta, a.g.dzt[k]), x)), Dk);
+  double delta_prev = 0.0, cp = 0.0, dp[NRHS];
+#pragma unroll
+  for (int r = 0; r < NRHS; ++r) dp[r] = 0.0;
+  for (int k0 = ks; k0 < Z; k0 += PF) {
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 + u;
+      if (k < Z) {
+        const double dzt = a.g.dzt[k];
+        const double delta = k < Z - 1 ? rmul(dtdzw[k], qK[u]) : 0.0;
+        double tr1[NRHS];
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) tr1[r] = qT[u][r];
+        // refill this slot with level k + PF
+        const int kn = k + PF;
+        if (kn < Z) {
+          const long long on = base + (long long)kn * L.plane;
+          qK[u] = kn < Z - 1 ? ld(a.K33, on) : 0.0;
+#pragma unroll
+          for (int r = 0; r < NRHS; ++r) qT[u][r] = trp[r][on];
+        }
+        const double ak = k == ks ? 0.0 : rdiv(-delta_prev, dzt);  // a_tri, zero at the edge (operators.py:72)
+        const double bk = k == ks ? radd(1.0, rdiv(delta, dzt)) : radd(1.0, rdiv(radd(delta, delta_prev), dzt));
+        const double ck = k < Z - 1 ? rdiv(-delta, dzt) : 0.0;
+        const double den = 1.0 / (bk - ak * cp);
+        cp = ck * den;
+        cps[(size_t)k * nb + t] = cp;
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) {
+          dp[r] = (tr1[r] - ak * dp[r]) * den;
+          dps[((size_t)r * Z + k) * nb + t] = dp[r];
+        }
+        delta_prev = delta;
       }
-      Ds[(size_t)k * nb + t] = x;
     }
   }
-  for (int k = Z - 1; k >= ks; --k) {
-    const long long o = base + (long long)k * L.plane;
-    const double x = Ds[(size_t)k * nb + t];
-    const double tr1 = a.trp[o];
-    a.trp[o] = x;
-    a.dtr_iso[o] = radd(a.dtr_iso[o], rdiv(rsub(x, tr1), a.dt));
+  double x[NRHS];
+#pragma unroll
+  for (int r = 0; r < NRHS; ++r) x[r] = 0.0;
+  const int nlev = Z - ks;
+  for (int m0 = 0; m0 < nlev; m0 += PF) {
+    // this group's old tracer values and partial tendencies, loaded together
+    double t1[PF][NRHS], d1[PF][NRHS];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = Z - 1 - (m0 + u);
+      if (k >= ks) {
+        const long long o = base + (long long)k * L.plane;
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) {
+          t1[u][r] = trp[r][o];
+          d1[u][r] = dtr[r][o];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = Z - 1 - (m0 + u);
+      if (k >= ks) {
+        const long long o = base + (long long)k * L.plane;
+        const double c = cps[(size_t)k * nb + t];
+#pragma unroll
+        for (int r = 0; r < NRHS; ++r) {
+          x[r] = dps[((size_t)r * Z + k) * nb + t] - c * x[r];
+          trp[r][o] = x[r];
+          dtr[r][o] = d1[u][r] + (x[r] - t1[u][r]) * inv_dt;  // diffusion.py:204
+        }
+      }
+    }
   }
 }
 
@@ -373,27 +407,22 @@ extern "C" size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom) {
   return 3 * (size_t)dom->plane * (size_t)dom->Z * sizeof(double);
 }
 
-extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
-                                           const VgTensorFields *ten, const double *K_field,
-                                           const uint8_t *mask_bits, const int32_t *kbot, const VgTracerArgs *tr,
-                                           int skew, void *scratch, size_t scratch_bytes, void *stream) {
-  clear_error();
-  int st = validate_domain(dom);
-  if (st) return st;
+namespace vg {
+namespace {
+
+// Validates one tracer's arguments and fills its DiffArgs.
+int make_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const VgTensorFields *ten,
+              const double *K_field, const uint8_t *mask_bits, const int32_t *kbot, const VgTracerArgs *tr, int skew,
+              double *scratch3, DiffArgs &a) {
   if (!grid_complete(grid) || !set || !ten || !K_field || !mask_bits || !kbot || !tr || !tr->tr_tau ||
       !tr->tr_taup1 || !tr->dtracer_iso || !ten->K_11 || !ten->K_22 || !ten->K_33 || !ten->Ai_ez ||
       !ten->Ai_nz || !ten->Ai_bx || !ten->Ai_by)
-    return fail(VG_ERR_ARG, "vg_isoneutral_diffusion_f64: NULL pointer argument");
+    return fail(VG_ERR_ARG, "isoneutral diffusion: NULL pointer argument");
   if (skew != 0 && skew != 1) return fail(VG_ERR_ARG, "skew must be 0 or 1");
   if (set->enable_conserve_energy && (!tr->int_drhodX_tau || !tr->P_diss))
     return fail(VG_ERR_ARG, "enable_conserve_energy needs int_drhodX_tau and P_diss");
   if (!(set->dt_tracer != 0.0)) return fail(VG_ERR_ARG, "dt_tracer must be non-zero");
   if (dom->Z > 512) return fail(VG_ERR_SHAPE, "Z=%d above the 512 levels supported", dom->Z);
-  const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
-  if (!scratch || scratch_bytes < need)
-    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
-
-  DiffArgs a;
   a.L = layout_of(dom);
   a.g = grid_of(grid);
   a.dt = set->dt_tracer;
@@ -420,38 +449,95 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
   a.P = tr->P_diss;
   a.save_fluxes = set->enable_conserve_energy ? 1 : 0;
   const size_t fsz = (size_t)a.L.plane * a.L.Z;
-  a.fe = static_cast<double *>(scratch);
-  a.fn = a.fe + fsz;
-  a.ft = a.fn + fsz;
+  a.fe = scratch3;
+  a.fn = scratch3 ? scratch3 + fsz : nullptr;
+  a.ft = scratch3 ? scratch3 + 2 * fsz : nullptr;
   a.iso = skew ? 0 : 1;
-  cudaStream_t s = as_stream(stream);
+  a.kchunk = 0;
+  return VG_OK;
+}
 
-  {
-    const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
-    int nchunks = 1;
-    while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
-    a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
-    const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
-    const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-    flux_div_kernel<<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
-    if ((st = check_launch("flux_div_kernel"))) return st;
+int launch_flux_div(DiffArgs &a, cudaStream_t s) {
+  const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
+  int nchunks = 1;
+  while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
+  a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
+  const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
+  const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
+  flux_div_kernel<<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
+  return check_launch("flux_div_kernel");
+}
+
+template <int NRHS>
+int launch_implicit(const DiffArgs &a, const DiffArgs &b, cudaStream_t s) {
+  const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
+  const int nb = 64;
+  const size_t smem = ((size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(implicit_kernel<NRHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
   }
-  if (a.iso) {
-    const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
-    const int nb = 64;
-    const size_t smem = ((size_t)a.L.Z + 2 * (size_t)a.L.Z * nb) * sizeof(double);
-    if (smem > 48 * 1024) {
-      cudaError_t e = cudaFuncSetAttribute(implicit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
-    }
-    implicit_kernel<<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, ncols_x, ncols);
-    if ((st = check_launch("implicit_kernel"))) return st;
-  }
-  if (set->enable_conserve_energy) {
-    dim3 block(128);
-    dim3 g((a.L.X - 2 + 127) / 128, a.L.Y - 2, a.L.Z);
-    energy_kernel<<<g, block, 0, s>>>(a);
-    if ((st = check_launch("energy_kernel"))) return st;
+  implicit_kernel<NRHS><<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, b, ncols_x, ncols);
+  return check_launch("implicit_kernel");
+}
+
+int launch_energy(const DiffArgs &a, cudaStream_t s) {
+  dim3 block(128);
+  dim3 g((a.L.X - 2 + 127) / 128, a.L.Y - 2, a.L.Z);
+  energy_kernel<<<g, block, 0, s>>>(a);
+  return check_launch("energy_kernel");
+}
+
+}  // namespace
+}  // namespace vg
+
+extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                           const VgTensorFields *ten, const double *K_field,
+                                           const uint8_t *mask_bits, const int32_t *kbot, const VgTracerArgs *tr,
+                                           int skew, void *scratch, size_t scratch_bytes, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
+  if (!scratch || scratch_bytes < need)
+    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
+  DiffArgs a;
+  if ((st = make_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<double *>(scratch), a)))
+    return st;
+  cudaStream_t s = as_stream(stream);
+  if ((st = launch_flux_div(a, s))) return st;
+  if (a.iso && (st = launch_implicit<1>(a, a, s))) return st;
+  if (a.save_fluxes && (st = launch_energy(a, s))) return st;
+  return VG_OK;
+}
+
+extern "C" size_t vg_isoneutral_diffusion_pair_scratch_bytes(const VgDomain *dom) {
+  return 2 * vg_isoneutral_diffusion_scratch_bytes(dom);
+}
+
+extern "C" int vg_isoneutral_diffusion_pair_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                                const VgTensorFields *ten, const double *K_iso,
+                                                const uint8_t *mask_bits, const int32_t *kbot,
+                                                const VgTracerArgs *temp, const VgTracerArgs *salt, void *scratch,
+                                                size_t scratch_bytes, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  const size_t one = vg_isoneutral_diffusion_scratch_bytes(dom);
+  if (!scratch || scratch_bytes < 2 * one)
+    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, 2 * one);
+  DiffArgs aT, aS;
+  double *sc = static_cast<double *>(scratch);
+  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
+  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
+    return st;
+  cudaStream_t s = as_stream(stream);
+  if ((st = launch_flux_div(aT, s))) return st;
+  if ((st = launch_flux_div(aS, s))) return st;
+  if ((st = launch_implicit<2>(aT, aS, s))) return st;
+  if (aT.save_fluxes) {
+    if ((st = launch_energy(aT, s))) return st;
+    if ((st = launch_energy(aS, s))) return st;
   }
   return VG_OK;
 }

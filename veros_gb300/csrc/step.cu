@@ -55,10 +55,7 @@ extern "C" int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, c
   if ((st = vg_isoneutral_pre_f64(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten, stream)))
     return st;
   VgTracerArgs trT{f->temp_tau, f->temp_taup1, f->dtemp_iso, f->int_drhodT_tau, f->P_diss_iso};
-  if ((st = vg_isoneutral_diffusion_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, 0, scratch,
-                                        scratch_bytes, stream)))
-    return st;
   VgTracerArgs trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
-  return vg_isoneutral_diffusion_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trS, 0, scratch,
-                                     scratch_bytes, stream);
+  return vg_isoneutral_diffusion_pair_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS, scratch,
+                                          scratch_bytes, stream);
 }

@@ -12,14 +12,14 @@ for each of the three phases and replayed in turn).
 import torch
 
 from . import _capi
-from .isoneutral import diffusion_scratch
 
 
 class IsoneutralStepper:
     def __init__(self, dev):
         self.dev = dev
         self.lib = _capi.load()
-        self.scratch = diffusion_scratch(dev)
+        nbytes = self.lib.vg_isoneutral_diffusion_pair_scratch_bytes(dev.domain())
+        self.scratch = torch.empty(nbytes // 8, dtype=torch.float64, device=dev.device)
         self._graphs = {}
 
     def _fields(self):
@@ -52,9 +52,9 @@ class IsoneutralStepper:
             self._rotate()
 
     def step_stages(self, events=None):
-        """One step as four C calls (prepare, pre, diffusion of temp, of salt).
+        """One step as three C calls: prepare, pre, diffusion of temp and salt.
 
-        ``events``: optional list of 5 ``torch.cuda.Event`` recorded on the
+        ``events``: optional list of 4 ``torch.cuda.Event`` recorded on the
         current stream before, between and after the stages.
         """
         dev, lib = self.dev, self.lib
@@ -70,12 +70,11 @@ class IsoneutralStepper:
         _capi.check(lib.vg_isoneutral_pre_f64(dom, grid, sett, f.temp_tau, f.salt_tau, f.K_iso, f.mask_bits,
                                               f.ten, stream), "pre")
         rec(2)
-        for n, (tau, taup1, dtr, idr) in enumerate(((f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau),
-                                                    (f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau))):
-            tra = _capi.VgTracerArgs(tau, taup1, dtr, idr, f.P_diss_iso)
-            _capi.check(lib.vg_isoneutral_diffusion_f64(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot, tra, 0,
-                                                        self.scratch.data_ptr(), nbytes, stream), "diffusion")
-            rec(3 + n)
+        trT = _capi.VgTracerArgs(f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau, f.P_diss_iso)
+        trS = _capi.VgTracerArgs(f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau, f.P_diss_iso)
+        _capi.check(lib.vg_isoneutral_diffusion_pair_f64(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot, trT, trS,
+                                                         self.scratch.data_ptr(), nbytes, stream), "diffusion")
+        rec(3)
         self._rotate()
 
     def step_host(self, temp_tau, salt_tau, out_temp, out_salt, out_dtemp, out_dsalt, staging=None):
@@ -108,6 +107,7 @@ class IsoneutralStepper:
         torch.cuda.current_stream(self.dev.device).synchronize()
 
     def launches_per_step(self):
-        """Kernels of this library one step enqueues (prepare + pre + 2 x diffusion)."""
-        per_diffusion = 3 if self.dev.settings.enable_conserve_energy else 2
-        return 1 + 1 + 2 * per_diffusion
+        """Kernels of this library one step enqueues: prepare, pre, two flux
+        kernels, one shared implicit solve and, with the energy branch, two
+        energy kernels."""
+        return 1 + 1 + 2 + 1 + (2 if self.dev.settings.enable_conserve_energy else 0)
