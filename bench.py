@@ -109,16 +109,22 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _profiled_traffic(name):
-    """dram read+write bytes per launch from the committed ncu summary, if any."""
+def _profiled(name, key):
+    """A figure from a committed ncu summary (``key: value`` line), if any."""
     path = os.path.join(REPO, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
-            if line.startswith("traffic_bytes_per_launch:"):
-                return int(line.split(":")[1])
+            if line.startswith(key + ":"):
+                return float(line.split(":")[1])
     return None
+
+
+def _profiled_traffic(name):
+    """dram read+write bytes per launch from the committed ncu summary, if any."""
+    v = _profiled(name, "traffic_bytes_per_launch")
+    return int(v) if v is not None else None
 
 
 def cpu_baseline_sample(nz_band=None, steps=1):
@@ -253,7 +259,7 @@ def run_gb300(args):
     pre_ms = float(stage_ms[:, 1].mean())
     pre_achieved = PRE_BYTES_PER_CELL * cells / (pre_ms / 1e3) / 1e9
     step_achieved = STEP_BYTES_PER_CELL * cells * args.steps / (ms / 1e3) / 1e9
-    traffic = _profiled_traffic("pre_cell_kernel_global1deg.md")
+    traffic = _profiled_traffic("pre_tile_kernel_global1deg.md")
     base = cpu_baseline_sample(steps=1)
     line = {
         "metric": "isoneutral step cells/s (FP64)", "value": value, "unit": "cells/s", "n_gpus": world,
@@ -268,7 +274,9 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": "pre_tile_kernel", "achieved": pre_achieved, "peak": peak,
                      "unit": "GB/s", "frac": pre_achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "algorithmic_bytes_per_cell": PRE_BYTES_PER_CELL,
-                     "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak},
+                     "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,
+                     "fp64_pipe_pct_ncu": _profiled("pre_tile_kernel_global1deg.md", "fp64_pipe_pct"),
+                     "note": "FP64-pipe bound on GB300 (~1 TFLOP/s FP64); HBM fraction reported as asked"},
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 2 * X * Y * Z * 8,
                 "d2h_bytes_per_step": 4 * X * Y * Z * 8, "steps": e2e_steps,
