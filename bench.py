@@ -229,6 +229,26 @@ def run_gb300(args):
         ms = float(t.item())
     value = world * cells * args.steps / (ms / 1e3)
 
+    # FP32/FP64-split form on the same workload: same number of steps from the
+    # same initial state; its tracers are compared with the FP64 run's
+    split = DeviceState.from_host(host, device=device, precision="f32split")
+    sstep = IsoneutralStepper(split)
+    sstep.step(args.warmup)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record()
+    sstep.step(args.steps)
+    s1.record()
+    torch.cuda.synchronize()
+    split_ms = s0.elapsed_time(s1)
+    split_err = {}
+    for name in ("temp", "salt"):
+        ref = getattr(dev.variables, name)
+        got = getattr(split.variables, name)
+        split_err[name] = float((got - ref).abs().max() / ref.abs().max())
+    split_value = world * cells * args.steps / (split_ms / 1e3)
+    del split, sstep
+
     # end to end through the host-buffer step API
     v = dev.variables
     pin = lambda: torch.empty((X, Y, Z), dtype=torch.float64).pin_memory()  # noqa: E731
@@ -281,6 +301,11 @@ def run_gb300(args):
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 2 * X * Y * Z * 8,
                 "d2h_bytes_per_step": 4 * X * Y * Z * 8, "steps": e2e_steps,
                 "api": "IsoneutralStepper.step_host (pinned host buffers, reference layout)"},
+        "f32split": {"value": split_value, "unit": "cells/s", "ms_per_step": split_ms / args.steps,
+                     "speedup_vs_f64": split_value / value,
+                     "tracer_rel_maxnorm_err_vs_f64": split_err,
+                     "precision": "FP64 tracers, gradients, slope denominators/slopes and implicit solve; "
+                                  "FP32 tensors, fluxes, taper, tendencies"},
         "gpu_launches": args.steps * stepper.launches_per_step(),
         "clocks": clocks.summary(),
     }

@@ -68,6 +68,24 @@ typedef struct VgTensorFields {
   long long ai_stride_p, ai_stride_r;
 } VgTensorFields;
 
+/* Derived fields of the split form (same layout, float elements). The
+ * tracers stay FP64 in the split form too: the slopes divide by vertical
+ * density gradients, differences of nearby tracer values, which FP32 storage
+ * would already blur at the 1e-6 K level. */
+typedef struct VgTensorFieldsF32 {
+  float *K_11, *K_22, *K_33;
+  float *Ai_ez, *Ai_nz, *Ai_bx, *Ai_by;
+  long long ai_stride_p, ai_stride_r;
+} VgTensorFieldsF32;
+
+typedef struct VgTracerArgsF32 {
+  const double *tr_tau;
+  double *tr_taup1;
+  float *dtracer_iso;
+  const float *int_drhodX_tau;
+  float *P_diss;
+} VgTracerArgsF32;
+
 typedef struct VgTracerArgs {
   const double *tr_tau;         /* tracer at level tau (read) */
   double *tr_taup1;             /* tracer at level taup1 (read, updated) */
@@ -96,6 +114,16 @@ int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSe
                           const double *temp_tau, const double *salt_tau, const double *K_iso,
                           const uint8_t *mask_bits, const VgTensorFields *out, void *stream);
 
+/* FP32/FP64-split form of vg_isoneutral_pre_f64: derived fields (K_iso in,
+ * K and Ai out) and their arithmetic in FP32; tracer gradients, the vertical
+ * density gradients (the clamped slope denominators), the slope numerators
+ * and the slopes in FP64; the taper evaluated in FP32 from the FP64 slope.
+ * Tracers and grid stay FP64. No reference counterpart (the reference runs in
+ * its float_type throughout). */
+int vg_isoneutral_pre_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                               const double *temp_tau, const double *salt_tau, const float *K_iso,
+                               const uint8_t *mask_bits, const VgTensorFieldsF32 *out, void *stream);
+
 /* Scratch bytes vg_isoneutral_diffusion_f64 needs for one domain. */
 size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom);
 
@@ -122,6 +150,21 @@ int vg_isoneutral_diffusion_pair_f64(const VgDomain *dom, const VgGrid *grid, co
                                      const uint8_t *mask_bits, const int32_t *kbot,
                                      const VgTracerArgs *temp, const VgTracerArgs *salt,
                                      void *scratch, size_t scratch_bytes, void *stream);
+
+/* FP32/FP64-split forms of the diffusion calls: fluxes and divergence in FP32
+ * from FP64 tracer differences, the tracer update and the implicit K_33 solve
+ * in FP64; tendencies and dissipation stored FP32.
+ * Same scratch sizes as the FP64 calls (of which they use half). */
+int vg_isoneutral_diffusion_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                     const VgTensorFieldsF32 *ten, const float *K_field,
+                                     const uint8_t *mask_bits, const int32_t *kbot,
+                                     const VgTracerArgsF32 *tr, int skew,
+                                     void *scratch, size_t scratch_bytes, void *stream);
+int vg_isoneutral_diffusion_pair_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                          const VgTensorFieldsF32 *ten, const float *K_iso,
+                                          const uint8_t *mask_bits, const int32_t *kbot,
+                                          const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
+                                          void *scratch, size_t scratch_bytes, void *stream);
 
 /* Scratch-free variant of vg_isoneutral_diffusion_f64 for callers that cannot
  * allocate device memory (an XLA custom-call or FFI handler working only with
@@ -162,6 +205,26 @@ typedef struct VgStepFields {
  * Scratch as for vg_isoneutral_diffusion_pair_f64. */
 int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                            const VgStepFields *f, void *scratch, size_t scratch_bytes, void *stream);
+
+/* FP32 fields of one rollout step of the split form. */
+typedef struct VgStepFieldsF32 {
+  const double *temp_tau;
+  double *temp_taup1;
+  const double *salt_tau;
+  double *salt_taup1;
+  const float *K_iso;
+  const uint8_t *mask_bits;
+  const int32_t *kbot;
+  VgTensorFieldsF32 ten;
+  float *dtemp_iso, *dsalt_iso;
+  const float *int_drhodT_tau, *int_drhodS_tau;
+  float *P_diss_iso;
+} VgStepFieldsF32;
+
+/* One isoneutral step of the FP32/FP64-split form (see vg_isoneutral_step_f64). */
+int vg_isoneutral_step_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                const VgStepFieldsF32 *f, void *scratch, size_t scratch_bytes, void *stream);
+int vg_isoneutral_step_prepare_f32split(const VgDomain *dom, const VgStepFieldsF32 *f, void *stream);
 
 /* First stage of vg_isoneutral_step_f64 alone (new time level and zeroed
  * tendencies), for callers that time or interleave the stages. */

@@ -46,6 +46,14 @@ class VgTensorFields(ctypes.Structure):
         ("ai_stride_p", ctypes.c_longlong), ("ai_stride_r", ctypes.c_longlong)]
 
 
+class VgTensorFieldsF32(ctypes.Structure):
+    _fields_ = VgTensorFields._fields_
+
+
+class VgTracerArgsF32(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("tr_tau", "tr_taup1", "dtracer_iso", "int_drhodX_tau", "P_diss")]
+
+
 class VgTracerArgs(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("tr_tau", "tr_taup1", "dtracer_iso", "int_drhodX_tau", "P_diss")]
 
@@ -53,6 +61,12 @@ class VgTracerArgs(ctypes.Structure):
 class VgStepFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
                                                 "mask_bits", "kbot")] + [("ten", VgTensorFields)] + [
+        (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso")]
+
+
+class VgStepFieldsF32(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
+                                                "mask_bits", "kbot")] + [("ten", VgTensorFieldsF32)] + [
         (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso")]
 
 
@@ -65,6 +79,28 @@ SIGNATURES = {
                                              ctypes.POINTER(VgIsoSettings), ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(VgTensorFields),
                                              ctypes.c_void_p]),
+    "vg_isoneutral_pre_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                  ctypes.POINTER(VgIsoSettings), ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(VgTensorFieldsF32),
+                                                  ctypes.c_void_p]),
+    "vg_isoneutral_diffusion_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                        ctypes.POINTER(VgIsoSettings),
+                                                        ctypes.POINTER(VgTensorFieldsF32), ctypes.c_void_p,
+                                                        ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.POINTER(VgTracerArgsF32), ctypes.c_int,
+                                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "vg_isoneutral_diffusion_pair_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                             ctypes.POINTER(VgIsoSettings),
+                                                             ctypes.POINTER(VgTensorFieldsF32), ctypes.c_void_p,
+                                                             ctypes.c_void_p, ctypes.c_void_p,
+                                                             ctypes.POINTER(VgTracerArgsF32),
+                                                             ctypes.POINTER(VgTracerArgsF32), ctypes.c_void_p,
+                                                             ctypes.c_size_t, ctypes.c_void_p]),
+    "vg_isoneutral_step_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                   ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgStepFieldsF32),
+                                                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "vg_isoneutral_step_prepare_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain),
+                                                           ctypes.POINTER(VgStepFieldsF32), ctypes.c_void_p]),
     "vg_isoneutral_diffusion_scratch_bytes": (ctypes.c_size_t, [ctypes.POINTER(VgDomain)]),
     "vg_isoneutral_diffusion_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                                    ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgTensorFields),

@@ -27,107 +27,124 @@ namespace {
 
 constexpr int TX = 32, TY = 8, NT = TX * TY;
 
+// F is the type of the derived fields (tensors, tendencies, dissipation) and of
+// the flux arithmetic: double for the FP64 drop-in, float for the split form.
+// Tracers stay FP64 in both (their differences feed the fluxes and their
+// increments are small against their values); the implicit solve is FP64.
+template <typename F>
 struct DiffArgs {
   Layout L;
   Grid g;
   double dt, grav, rho0;
-  const double *__restrict__ K;  // K_iso (iso) or K_gm (skew)
-  double s1, s2;                 // K1 = s1*K, K2 = s2*K (diffusion.py:15-16)
-  const double *__restrict__ K11;
-  const double *__restrict__ K22;
-  const double *__restrict__ K33;
-  const double *__restrict__ Aez;
-  const double *__restrict__ Anz;
-  const double *__restrict__ Abx;
-  const double *__restrict__ Aby;
+  const F *__restrict__ K;  // K_iso (iso) or K_gm (skew)
+  double s1, s2;            // K1 = s1*K, K2 = s2*K (diffusion.py:15-16)
+  const F *__restrict__ K11;
+  const F *__restrict__ K22;
+  const F *__restrict__ K33;
+  const F *__restrict__ Aez;
+  const F *__restrict__ Anz;
+  const F *__restrict__ Abx;
+  const F *__restrict__ Aby;
   long long sp, sr;
   const uint8_t *__restrict__ m;
   const int32_t *__restrict__ kbot;
   const double *__restrict__ tr;  // tau
   double *trp;                    // taup1
-  double *dtr_iso;
-  const double *__restrict__ idr;  // int_drhodX at tau
-  double *P;
-  double *fe, *fn, *ft;  // scratch fluxes (energy branch)
+  F *dtr_iso;
+  const F *__restrict__ idr;  // int_drhodX at tau
+  F *P;
+  F *fe, *fn, *ft;  // scratch fluxes (energy branch)
   int iso, save_fluxes, kchunk;
 };
 
-__device__ __forceinline__ double ld(const double *p, long long o) { return __ldg(p + o); }
+template <typename F>
+__device__ __forceinline__ F ld(const F *p, long long o) { return __ldg(p + o); }
+
+// x + y and x * y: explicitly rounded in FP64 (no contraction into the
+// explicit update, which feeds the tendency's differencing), plain in FP32.
+__device__ __forceinline__ double add_(double x, double y) { return radd(x, y); }
+__device__ __forceinline__ double mul_(double x, double y) { return rmul(x, y); }
+__device__ __forceinline__ float add_(float x, float y) { return x + y; }
+__device__ __forceinline__ float mul_(float x, float y) { return x * y; }
 
 // east-face flux at cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
-__device__ __forceinline__ double flux_east(const DiffArgs &a, int i, int j, int k, double inv_cost_dxu,
-                                            double q_dzt) {
+template <typename F>
+__device__ __forceinline__ F flux_east(const DiffArgs<F> &a, int i, int j, int k, F inv_cost_dxu, F q_dzt) {
   const Layout &L = a.L;
   const long long o = L.at(i, j, k);
   const int Z = L.Z;
   const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
   const long long dp = k < Z - 1 ? L.plane : 0;
-  double diffloc;
+  const F s1 = F(a.s1);
+  F diffloc;
   if (k >= 1)
-    diffloc = 0.25 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o - L.plane) + a.s1 * ld(a.K, o + 1) +
-                      a.s1 * ld(a.K, o + 1 - L.plane));
+    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + 1) +
+                         s1 * ld(a.K, o + 1 - L.plane));
   else
-    diffloc = 0.5 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o + 1));
+    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + 1));
   const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + 1);
   const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + 1 - dm);
   const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + 1 + dp);
-  double sumz = 0.0;
-  sumz += diffloc * ld(a.Aez, o) * (t0 - t0m);
-  sumz += diffloc * ld(a.Aez, o + a.sp) * (t1 - t1m);
-  sumz += diffloc * ld(a.Aez, o + a.sr) * (t0p - t0);
-  sumz += diffloc * ld(a.Aez, o + a.sp + a.sr) * (t1p - t1);
-  return sumz * q_dzt + (t1 - t0) * inv_cost_dxu * ld(a.K11, o);
+  F sumz = 0.0;
+  sumz += diffloc * ld(a.Aez, o) * F(t0 - t0m);
+  sumz += diffloc * ld(a.Aez, o + a.sp) * F(t1 - t1m);
+  sumz += diffloc * ld(a.Aez, o + a.sr) * F(t0p - t0);
+  sumz += diffloc * ld(a.Aez, o + a.sp + a.sr) * F(t1p - t1);
+  return sumz * q_dzt + F(t1 - t0) * inv_cost_dxu * ld(a.K11, o);
 }
 
 // north-face flux at cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
-__device__ __forceinline__ double flux_north(const DiffArgs &a, int i, int j, int k, double cosu, double inv_dyu,
-                                             double q_dzt) {
+template <typename F>
+__device__ __forceinline__ F flux_north(const DiffArgs<F> &a, int i, int j, int k, F cosu, F inv_dyu, F q_dzt) {
   const Layout &L = a.L;
   const long long o = L.at(i, j, k);
   const long long P = L.pitch;
   const int Z = L.Z;
   const long long dm = k > 0 ? L.plane : 0;
   const long long dp = k < Z - 1 ? L.plane : 0;
-  double diffloc;
+  const F s1 = F(a.s1);
+  F diffloc;
   if (k >= 1)
-    diffloc = 0.25 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o - L.plane) + a.s1 * ld(a.K, o + P) +
-                      a.s1 * ld(a.K, o + P - L.plane));
+    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + P) +
+                         s1 * ld(a.K, o + P - L.plane));
   else
-    diffloc = 0.5 * (a.s1 * ld(a.K, o) + a.s1 * ld(a.K, o + P));
+    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + P));
   const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + P);
   const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + P - dm);
   const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + P + dp);
-  double sumz = 0.0;
-  sumz += diffloc * ld(a.Anz, o) * (t0 - t0m);
-  sumz += diffloc * ld(a.Anz, o + a.sp) * (t1 - t1m);
-  sumz += diffloc * ld(a.Anz, o + a.sr) * (t0p - t0);
-  sumz += diffloc * ld(a.Anz, o + a.sp + a.sr) * (t1p - t1);
-  return cosu * (sumz * q_dzt + (t1 - t0) * inv_dyu * ld(a.K22, o));
+  F sumz = 0.0;
+  sumz += diffloc * ld(a.Anz, o) * F(t0 - t0m);
+  sumz += diffloc * ld(a.Anz, o + a.sp) * F(t1 - t1m);
+  sumz += diffloc * ld(a.Anz, o + a.sr) * F(t0p - t0);
+  sumz += diffloc * ld(a.Anz, o + a.sp + a.sr) * F(t1p - t1);
+  return cosu * (sumz * q_dzt + F(t1 - t0) * inv_dyu * ld(a.K22, o));
 }
 
 // top-face flux at interior cell (i, j, k < Z-1) (diffusion.py:85-111)
-__device__ __forceinline__ double flux_top(const DiffArgs &a, long long o, double inv_cost, double cosu_s,
-                                           double cosu_c, double q_dxt, double q_dyt_cost) {
+template <typename F>
+__device__ __forceinline__ F flux_top(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F q_dxt,
+                                      F q_dyt_cost) {
   const Layout &L = a.L;
   const long long P = L.pitch, Q = L.plane;
-  const double diffloc = a.s2 * ld(a.K, o);
+  const F diffloc = F(a.s2) * ld(a.K, o);
   const double tc = ld(a.tr, o), tcu = ld(a.tr, o + Q);
-  double sumx = 0.0;
-  sumx += diffloc * ld(a.Abx, o) * inv_cost * (tc - ld(a.tr, o - 1));
-  sumx += diffloc * ld(a.Abx, o + a.sr) * inv_cost * (tcu - ld(a.tr, o - 1 + Q));
-  sumx += diffloc * ld(a.Abx, o + a.sp) * inv_cost * (ld(a.tr, o + 1) - tc);
-  sumx += diffloc * ld(a.Abx, o + a.sp + a.sr) * inv_cost * (ld(a.tr, o + 1 + Q) - tcu);
-  double sumy = 0.0;
-  sumy += diffloc * ld(a.Aby, o) * cosu_s * (tc - ld(a.tr, o - P));
-  sumy += diffloc * ld(a.Aby, o + a.sr) * cosu_s * (tcu - ld(a.tr, o - P + Q));
-  sumy += diffloc * ld(a.Aby, o + a.sp) * cosu_c * (ld(a.tr, o + P) - tc);
-  sumy += diffloc * ld(a.Aby, o + a.sp + a.sr) * cosu_c * (ld(a.tr, o + P + Q) - tcu);
+  F sumx = 0.0;
+  sumx += diffloc * ld(a.Abx, o) * inv_cost * F(tc - ld(a.tr, o - 1));
+  sumx += diffloc * ld(a.Abx, o + a.sr) * inv_cost * F(tcu - ld(a.tr, o - 1 + Q));
+  sumx += diffloc * ld(a.Abx, o + a.sp) * inv_cost * F(ld(a.tr, o + 1) - tc);
+  sumx += diffloc * ld(a.Abx, o + a.sp + a.sr) * inv_cost * F(ld(a.tr, o + 1 + Q) - tcu);
+  F sumy = 0.0;
+  sumy += diffloc * ld(a.Aby, o) * cosu_s * F(tc - ld(a.tr, o - P));
+  sumy += diffloc * ld(a.Aby, o + a.sr) * cosu_s * F(tcu - ld(a.tr, o - P + Q));
+  sumy += diffloc * ld(a.Aby, o + a.sp) * cosu_c * F(ld(a.tr, o + P) - tc);
+  sumy += diffloc * ld(a.Aby, o + a.sp + a.sr) * cosu_c * F(ld(a.tr, o + P + Q) - tcu);
   return sumx * q_dxt + sumy * q_dyt_cost;
 }
 
-__global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
-  __shared__ double fe_s[2][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
-  __shared__ double fn_s[2][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
+template <typename F>
+__global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs<F> a) {
+  __shared__ F fe_s[2][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
+  __shared__ F fn_s[2][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
   extern __shared__ double zq_dzt[];      // 1/(4 dzt[k]), then 1/dzt[k]
   const Layout &L = a.L;
   const int Z = L.Z;
@@ -145,27 +162,27 @@ __global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
   const bool own = i < L.X - 2 && j < L.Y - 2;
   const int ic = min(i, L.X - 3), jc = min(j, L.Y - 3);
   const double cost = a.g.cost[jc];
-  const double inv_cost = 1.0 / cost;
-  const double inv_cost_dxu = 1.0 / (cost * a.g.dxu[ic]);
-  const double cosu_c = a.g.cosu[jc], cosu_s = a.g.cosu[jc - 1];
-  const double inv_dyu = 1.0 / a.g.dyu[jc];
-  const double inv_fx = 1.0 / (cost * a.g.dxt[ic]);  // divergence factors (diffusion.py:127, :129)
-  const double inv_fy = 1.0 / (cost * a.g.dyt[jc]);
-  const double q_dxt = 1.0 / (4.0 * a.g.dxt[ic]);
-  const double q_dyt_cost = 1.0 / (4.0 * a.g.dyt[jc] * cost);
+  const F inv_cost = F(1.0 / cost);
+  const F inv_cost_dxu = F(1.0 / (cost * a.g.dxu[ic]));
+  const F cosu_c = F(a.g.cosu[jc]), cosu_s = F(a.g.cosu[jc - 1]);
+  const F inv_dyu = F(1.0 / a.g.dyu[jc]);
+  const F inv_fx = F(1.0 / (cost * a.g.dxt[ic]));  // divergence factors (diffusion.py:127, :129)
+  const F inv_fy = F(1.0 / (cost * a.g.dyt[jc]));
+  const F q_dxt = F(1.0 / (4.0 * a.g.dxt[ic]));
+  const F q_dyt_cost = F(1.0 / (4.0 * a.g.dyt[jc] * cost));
   // halo faces: warp 0 the south row of north faces, warp 1 the west column of east faces
   const int hi_n = i0 + lane;  // north face (hi_n, j0-1)
   const bool halo_n = warp == 0 && hi_n < L.X - 2 && j0 - 1 < L.Y - 2;
   const int hj_e = j0 + lane;  // east face (i0-1, hj_e)
   const bool halo_e = warp == 1 && lane < TY && hj_e < L.Y - 2 && i0 - 1 < L.X - 2;
-  double h_cosu = 0, h_inv_dyu = 0, h_inv_cost_dxu = 0;
+  F h_cosu = 0, h_inv_dyu = 0, h_inv_cost_dxu = 0;
   if (halo_n) {
-    h_cosu = a.g.cosu[j0 - 1];
-    h_inv_dyu = 1.0 / a.g.dyu[j0 - 1];
+    h_cosu = F(a.g.cosu[j0 - 1]);
+    h_inv_dyu = F(1.0 / a.g.dyu[j0 - 1]);
   }
-  if (halo_e) h_inv_cost_dxu = 1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]);
+  if (halo_e) h_inv_cost_dxu = F(1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]));
 
-  double ft_prev = 0.0;
+  F ft_prev = 0.0;
   if (own && kb > 0) ft_prev = flux_top(a, L.at(i, j, kb - 1), inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
 
   for (int k = kb; k < ke; ++k) {
@@ -173,24 +190,24 @@ __global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
     // reads before level k+2's writes to the same buffer
     const int b = k & 1;
     const long long o = L.at(i, j, k);
-    double fe = 0, fn = 0, ft = 0;
+    F fe = 0, fn = 0, ft = 0;
     if (own) {
-      fe = flux_east(a, i, j, k, inv_cost_dxu, zq_dzt[k]);
-      fn = flux_north(a, i, j, k, cosu_c, inv_dyu, zq_dzt[k]);
+      fe = flux_east(a, i, j, k, inv_cost_dxu, F(zq_dzt[k]));
+      fn = flux_north(a, i, j, k, cosu_c, inv_dyu, F(zq_dzt[k]));
       if (k < Z - 1) ft = flux_top(a, o, inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
       fe_s[b][ty][tx + 1] = fe;
       fn_s[b][ty + 1][tx] = fn;
     }
-    if (halo_n) fn_s[b][0][lane] = flux_north(a, hi_n, j0 - 1, k, h_cosu, h_inv_dyu, zq_dzt[k]);
-    if (halo_e) fe_s[b][lane][0] = flux_east(a, i0 - 1, hj_e, k, h_inv_cost_dxu, zq_dzt[k]);
+    if (halo_n) fn_s[b][0][lane] = flux_north(a, hi_n, j0 - 1, k, h_cosu, h_inv_dyu, F(zq_dzt[k]));
+    if (halo_e) fe_s[b][lane][0] = flux_east(a, i0 - 1, hj_e, k, h_inv_cost_dxu, F(zq_dzt[k]));
     __syncthreads();
     if (own) {
-      const double mT = (__ldg(a.m + o) & VG_MASK_T) ? 1.0 : 0.0;
-      double e = mT * ((fe - fe_s[b][ty][tx]) * inv_fx + (fn - fn_s[b][ty][tx]) * inv_fy);
-      e = e + mT * (ft - ft_prev) * zinv_dzt[k];  // k = 0: ft_prev = 0 (diffusion.py:132-137)
+      const F mT = (__ldg(a.m + o) & VG_MASK_T) ? F(1.0) : F(0.0);
+      F e = mT * ((fe - fe_s[b][ty][tx]) * inv_fx + (fn - fn_s[b][ty][tx]) * inv_fy);
+      e = e + mT * (ft - ft_prev) * F(zinv_dzt[k]);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
       ft_prev = ft;
-      a.dtr_iso[o] = radd(a.dtr_iso[o], e);
-      a.trp[o] = radd(a.trp[o], rmul(a.dt, e));
+      a.dtr_iso[o] = add_(a.dtr_iso[o], e);
+      a.trp[o] = radd(a.trp[o], rmul(a.dt, (double)e));
       if (a.save_fluxes) {
         a.fe[o] = fe;
         a.fn[o] = fn;
@@ -204,23 +221,6 @@ __global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs a) {
   }
 }
 
-// Row source of one column's implicit system (diffusion.py:154-164): the
-// matrix entries from K_33 and the grid, in the reference's operation order.
-struct ColMatrix {
-  const DiffArgs &a;
-  const double *dtdzw;  // dt / dzw[k], per level
-  long long base;
-  int ks, Z;
-  __device__ double delta(int k) const {
-    return k < Z - 1 ? rmul(dtdzw[k], ld(a.K33, base + (long long)k * a.L.plane)) : 0.0;
-  }
-  __device__ double lower(int k) const { return rdiv(-delta(k - 1), a.g.dzt[k]); }  // a_tri[k], k > ks
-  __device__ double diag(int k) const {                                              // b_tri / b_tri_edge
-    return k == ks ? radd(1.0, rdiv(delta(k), a.g.dzt[k])) : radd(1.0, rdiv(radd(delta(k), delta(k - 1)), a.g.dzt[k]));
-  }
-  __device__ double upper(int k) const { return rdiv(-delta(k), a.g.dzt[k]); }  // c_tri[k], k < Z-1
-};
-
 // Implicit solve of NRHS tracers sharing one matrix, one thread per column.
 // The system (diffusion.py:154-164) is an M-matrix that is diagonally
 // dominant by columns (|b_k| >= |a_{k+1}| + |c_{k-1}|), for which elimination
@@ -229,8 +229,8 @@ struct ColMatrix {
 // back substitution. The matrix entries use the reference's divisions; the
 // factorisation is shared by the tracers. Shared memory holds c'_k and d'_k of
 // each tracer, [k][thread].
-template <int NRHS>
-__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, int ncols_x, int ncols) {
+template <typename F, int NRHS>
+__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs<F> a, DiffArgs<F> b2, int ncols_x, int ncols) {
   extern __shared__ double smem[];
   const Layout &L = a.L;
   const int Z = L.Z;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
   if (ks < 0 || ks >= Z) return;
   const long long base = L.at2(i, j);
   double *trp[2] = {a.trp, b2.trp};
-  double *dtr[2] = {a.dtr_iso, b2.dtr_iso};
+  F *dtr[2] = {a.dtr_iso, b2.dtr_iso};
   const double inv_dt = 1.0 / a.dt;
 
   // Loads run PF levels ahead of the serial chain (software pipelining): the
@@ -259,9 +259,9 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
   for (int u = 0; u < PF; ++u) {
     const int k = ks + u;
     const long long o = base + (long long)min(k, Z - 1) * L.plane;
-    qK[u] = k < Z - 1 ? ld(a.K33, o) : 0.0;
+    qK[u] = k < Z - 1 ? (double)ld(a.K33, o) : 0.0;
 #pragma unroll
-    for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? trp[r][o] : 0.0;
+    for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? (double)trp[r][o] : 0.0;
   }
   double delta_prev = 0.0, cp = 0.0, dp[NRHS];
 #pragma unroll
@@ -280,9 +280,9 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
         const int kn = k + PF;
         if (kn < Z) {
           const long long on = base + (long long)kn * L.plane;
-          qK[u] = kn < Z - 1 ? ld(a.K33, on) : 0.0;
+          qK[u] = kn < Z - 1 ? (double)ld(a.K33, on) : 0.0;
 #pragma unroll
-          for (int r = 0; r < NRHS; ++r) qT[u][r] = trp[r][on];
+          for (int r = 0; r < NRHS; ++r) qT[u][r] = (double)trp[r][on];
         }
         const double ak = k == ks ? 0.0 : rdiv(-delta_prev, dzt);  // a_tri, zero at the edge (operators.py:72)
         const double bk = k == ks ? radd(1.0, rdiv(delta, dzt)) : radd(1.0, rdiv(radd(delta, delta_prev), dzt));
@@ -313,8 +313,8 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
         const long long o = base + (long long)k * L.plane;
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
-          t1[u][r] = trp[r][o];
-          d1[u][r] = dtr[r][o];
+          t1[u][r] = (double)trp[r][o];
+          d1[u][r] = (double)dtr[r][o];
         }
       }
     }
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
         for (int r = 0; r < NRHS; ++r) {
           x[r] = dps[((size_t)r * Z + k) * nb + t] - c * x[r];
           trp[r][o] = x[r];
-          dtr[r][o] = d1[u][r] + (x[r] - t1[u][r]) * inv_dt;  // diffusion.py:204
+          dtr[r][o] = F(d1[u][r] + (x[r] - t1[u][r]) * inv_dt);  // diffusion.py:204
         }
       }
     }
@@ -336,27 +336,31 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs a, DiffArgs b2, i
 }
 
 // Scratch flux readers: zero outside the ranges the reference defines.
-__device__ __forceinline__ double fe_at(const DiffArgs &a, int i, int j, int k) {
-  return (i >= 1 && i < a.L.X - 2 && j >= 2 && j < a.L.Y - 2) ? a.fe[a.L.at(i, j, k)] : 0.0;
+template <typename F>
+__device__ __forceinline__ F fe_at(const DiffArgs<F> &a, int i, int j, int k) {
+  return (i >= 1 && i < a.L.X - 2 && j >= 2 && j < a.L.Y - 2) ? a.fe[a.L.at(i, j, k)] : F(0.0);
 }
-__device__ __forceinline__ double fn_at(const DiffArgs &a, int i, int j, int k) {
-  return (i >= 2 && i < a.L.X - 2 && j >= 1 && j < a.L.Y - 2) ? a.fn[a.L.at(i, j, k)] : 0.0;
+template <typename F>
+__device__ __forceinline__ F fn_at(const DiffArgs<F> &a, int i, int j, int k) {
+  return (i >= 2 && i < a.L.X - 2 && j >= 1 && j < a.L.Y - 2) ? a.fn[a.L.at(i, j, k)] : F(0.0);
 }
 
 // Dissipation at T points (veros/core/diffusion.py:9-36); zero on the outer ring.
-__device__ __forceinline__ double diss_at(const DiffArgs &a, int i, int j, int k) {
+template <typename F>
+__device__ __forceinline__ F diss_at(const DiffArgs<F> &a, int i, int j, int k) {
   const Layout &L = a.L;
   const long long o = L.at(i, j, k);
-  const double c = 0.5 * a.grav / a.rho0;
-  const double I0 = ld(a.idr, o);
-  const double ex = (ld(a.idr, o + 1) - I0) * fe_at(a, i, j, k) + (I0 - ld(a.idr, o - 1)) * fe_at(a, i - 1, j, k);
-  const double ny =
+  const F c = F(0.5 * a.grav / a.rho0);
+  const F I0 = ld(a.idr, o);
+  const F ex = (ld(a.idr, o + 1) - I0) * fe_at(a, i, j, k) + (I0 - ld(a.idr, o - 1)) * fe_at(a, i - 1, j, k);
+  const F ny =
       (ld(a.idr, o + L.pitch) - I0) * fn_at(a, i, j, k) + (I0 - ld(a.idr, o - L.pitch)) * fn_at(a, i, j - 1, k);
   const double cost = a.g.cost[j];
-  return c * ex / (a.g.dxt[i] * cost) + c * ny / (a.g.dyt[j] * cost);
+  return c * ex / F(a.g.dxt[i] * cost) + c * ny / F(a.g.dyt[j] * cost);
 }
 
-__global__ void __launch_bounds__(128) energy_kernel(DiffArgs a) {
+template <typename F>
+__global__ void __launch_bounds__(128) energy_kernel(DiffArgs<F> a) {
   const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   const int j = 1 + blockIdx.y;
   const int k = blockIdx.z;
@@ -368,27 +372,27 @@ __global__ void __launch_bounds__(128) energy_kernel(DiffArgs a) {
   const bool land = ks >= 0;  // "land_mask" of create_water_masks: column has water
 
   // dissipation_on_wgrid (veros/core/diffusion.py:39-62)
-  const double d0 = diss_at(a, i, j, k);
-  double dw;
+  const F d0 = diss_at(a, i, j, k);
+  F dw;
   if (k < Z - 1) {
-    const double d1 = diss_at(a, i, j, k + 1);
-    const double edge = (land && k == ks) ? 1.0 : 0.0;
-    const double water = (land && k > ks) ? 1.0 : 0.0;
-    const double dzw_pad = a.g.dzw[k > 0 ? k - 1 : 0];
-    dw = (0.5 * (d0 + d1) + 0.5 * (d0 * dzw_pad / a.g.dzw[k])) * edge + 0.5 * (d0 + d1) * water;
+    const F d1 = diss_at(a, i, j, k + 1);
+    const F edge = (land && k == ks) ? F(1.0) : F(0.0);
+    const F water = (land && k > ks) ? F(1.0) : F(0.0);
+    const F dzw_pad = F(a.g.dzw[k > 0 ? k - 1 : 0]);
+    dw = (F(0.5) * (d0 + d1) + F(0.5) * (d0 * dzw_pad / F(a.g.dzw[k]))) * edge + F(0.5) * (d0 + d1) * water;
   } else {
-    dw = d0 * (land ? 1.0 : 0.0);
+    dw = d0 * (land ? F(1.0) : F(0.0));
   }
-  double P = a.P[o] + dw;
+  F P = a.P[o] + dw;
 
   // vertical-mixing term (diffusion.py:254-279)
   if (i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2 && k < Z - 1) {
-    const double mW = (__ldg(a.m + o) & VG_MASK_W) ? 1.0 : 0.0;
-    const double fxa = (-ld(a.idr, o + L.plane) + ld(a.idr, o)) / a.g.dzw[k];
-    const double g = -a.grav / a.rho0 * fxa;
+    const F mW = (__ldg(a.m + o) & VG_MASK_W) ? F(1.0) : F(0.0);
+    const F fxa = (-ld(a.idr, o + L.plane) + ld(a.idr, o)) / F(a.g.dzw[k]);
+    const F g = F(-a.grav / a.rho0) * fxa;
     if (a.iso) {
-      const double dtrz = a.trp[o + L.plane] - a.trp[o];
-      P = P + g * (a.ft[o] * mW + ld(a.K33, o) * dtrz / a.g.dzw[k] * mW);
+      const F dtrz = F(a.trp[o + L.plane] - a.trp[o]);
+      P = P + g * (a.ft[o] * mW + ld(a.K33, o) * dtrz / F(a.g.dzw[k]) * mW);
     } else {
       P = P + g * a.ft[o] * mW;
     }
@@ -411,9 +415,9 @@ namespace vg {
 namespace {
 
 // Validates one tracer's arguments and fills its DiffArgs.
-int make_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const VgTensorFields *ten,
-              const double *K_field, const uint8_t *mask_bits, const int32_t *kbot, const VgTracerArgs *tr, int skew,
-              double *scratch3, DiffArgs &a) {
+template <typename F, typename Ten, typename Tr>
+int make_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten, const F *K_field,
+              const uint8_t *mask_bits, const int32_t *kbot, const Tr *tr, int skew, F *scratch3, DiffArgs<F> &a) {
   if (!grid_complete(grid) || !set || !ten || !K_field || !mask_bits || !kbot || !tr || !tr->tr_tau ||
       !tr->tr_taup1 || !tr->dtracer_iso || !ten->K_11 || !ten->K_22 || !ten->K_33 || !ten->Ai_ez ||
       !ten->Ai_nz || !ten->Ai_bx || !ten->Ai_by)
@@ -457,35 +461,84 @@ int make_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
   return VG_OK;
 }
 
-int launch_flux_div(DiffArgs &a, cudaStream_t s) {
+template <typename F>
+int launch_flux_div(DiffArgs<F> &a, cudaStream_t s) {
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
   int nchunks = 1;
   while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
   a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
   const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
   const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-  flux_div_kernel<<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
+  flux_div_kernel<F><<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
   return check_launch("flux_div_kernel");
 }
 
-template <int NRHS>
-int launch_implicit(const DiffArgs &a, const DiffArgs &b, cudaStream_t s) {
+template <typename F, int NRHS>
+int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) {
   const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
   const int nb = 64;
   const size_t smem = ((size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(implicit_kernel<NRHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(implicit_kernel<F, NRHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
   }
-  implicit_kernel<NRHS><<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, b, ncols_x, ncols);
+  implicit_kernel<F, NRHS><<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, b, ncols_x, ncols);
   return check_launch("implicit_kernel");
 }
 
-int launch_energy(const DiffArgs &a, cudaStream_t s) {
+template <typename F>
+int launch_energy(const DiffArgs<F> &a, cudaStream_t s) {
   dim3 block(128);
   dim3 g((a.L.X - 2 + 127) / 128, a.L.Y - 2, a.L.Z);
-  energy_kernel<<<g, block, 0, s>>>(a);
+  energy_kernel<F><<<g, block, 0, s>>>(a);
   return check_launch("energy_kernel");
+}
+
+template <typename F, typename Ten, typename Tr>
+int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten,
+                  const F *K_field, const uint8_t *mask_bits, const int32_t *kbot, const Tr *tr, int skew,
+                  void *scratch, size_t scratch_bytes, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
+  if (!scratch || scratch_bytes < need)
+    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
+  DiffArgs<F> a;
+  if ((st = make_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<F *>(scratch), a)))
+    return st;
+  cudaStream_t s = as_stream(stream);
+  if ((st = launch_flux_div(a, s))) return st;
+  if (a.iso && (st = launch_implicit<F, 1>(a, a, s))) return st;
+  if (a.save_fluxes && (st = launch_energy(a, s))) return st;
+  return VG_OK;
+}
+
+template <typename F, typename Ten, typename Tr>
+int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten,
+                   const F *K_iso, const uint8_t *mask_bits, const int32_t *kbot, const Tr *temp, const Tr *salt,
+                   void *scratch, size_t scratch_bytes, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  const size_t one = vg_isoneutral_diffusion_scratch_bytes(dom);
+  if (!scratch || scratch_bytes < 2 * one)
+    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, 2 * one);
+  DiffArgs<F> aT, aS;
+  F *sc = static_cast<F *>(scratch);
+  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
+  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
+    return st;
+  cudaStream_t s = as_stream(stream);
+  if ((st = launch_flux_div(aT, s))) return st;
+  if ((st = launch_flux_div(aS, s))) return st;
+  if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
+  if (aT.save_fluxes) {
+    if ((st = launch_energy(aT, s))) return st;
+    if ((st = launch_energy(aS, s))) return st;
+  }
+  return VG_OK;
 }
 
 }  // namespace
@@ -495,20 +548,17 @@ extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *gr
                                            const VgTensorFields *ten, const double *K_field,
                                            const uint8_t *mask_bits, const int32_t *kbot, const VgTracerArgs *tr,
                                            int skew, void *scratch, size_t scratch_bytes, void *stream) {
-  clear_error();
-  int st = validate_domain(dom);
-  if (st) return st;
-  const size_t need = vg_isoneutral_diffusion_scratch_bytes(dom);
-  if (!scratch || scratch_bytes < need)
-    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
-  DiffArgs a;
-  if ((st = make_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<double *>(scratch), a)))
-    return st;
-  cudaStream_t s = as_stream(stream);
-  if ((st = launch_flux_div(a, s))) return st;
-  if (a.iso && (st = launch_implicit<1>(a, a, s))) return st;
-  if (a.save_fluxes && (st = launch_energy(a, s))) return st;
-  return VG_OK;
+  return diffusion_one<double>(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, scratch, scratch_bytes,
+                               stream);
+}
+
+extern "C" int vg_isoneutral_diffusion_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                                const VgTensorFieldsF32 *ten, const float *K_field,
+                                                const uint8_t *mask_bits, const int32_t *kbot,
+                                                const VgTracerArgsF32 *tr, int skew, void *scratch,
+                                                size_t scratch_bytes, void *stream) {
+  return diffusion_one<float>(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, scratch, scratch_bytes,
+                              stream);
 }
 
 extern "C" size_t vg_isoneutral_diffusion_pair_scratch_bytes(const VgDomain *dom) {
@@ -520,26 +570,18 @@ extern "C" int vg_isoneutral_diffusion_pair_f64(const VgDomain *dom, const VgGri
                                                 const uint8_t *mask_bits, const int32_t *kbot,
                                                 const VgTracerArgs *temp, const VgTracerArgs *salt, void *scratch,
                                                 size_t scratch_bytes, void *stream) {
-  clear_error();
-  int st = validate_domain(dom);
-  if (st) return st;
-  const size_t one = vg_isoneutral_diffusion_scratch_bytes(dom);
-  if (!scratch || scratch_bytes < 2 * one)
-    return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, 2 * one);
-  DiffArgs aT, aS;
-  double *sc = static_cast<double *>(scratch);
-  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
-  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
-    return st;
-  cudaStream_t s = as_stream(stream);
-  if ((st = launch_flux_div(aT, s))) return st;
-  if ((st = launch_flux_div(aS, s))) return st;
-  if ((st = launch_implicit<2>(aT, aS, s))) return st;
-  if (aT.save_fluxes) {
-    if ((st = launch_energy(aT, s))) return st;
-    if ((st = launch_energy(aS, s))) return st;
-  }
-  return VG_OK;
+  return diffusion_pair<double>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                                stream);
+}
+
+extern "C" int vg_isoneutral_diffusion_pair_f32split(const VgDomain *dom, const VgGrid *grid,
+                                                     const VgIsoSettings *set, const VgTensorFieldsF32 *ten,
+                                                     const float *K_iso, const uint8_t *mask_bits,
+                                                     const int32_t *kbot, const VgTracerArgsF32 *temp,
+                                                     const VgTracerArgsF32 *salt, void *scratch,
+                                                     size_t scratch_bytes, void *stream) {
+  return diffusion_pair<float>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                               stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -38,6 +38,12 @@ constexpr int PX = TX + 2, PY = TY + 2, NP = PX * PY;  // point region: tile + 1
 constexpr int kPtSlots = (NP + NT - 1) / NT;
 enum { Q_RT, Q_RS, Q_TX, Q_SX, Q_TY, Q_SY, Q_R0, Q_R1, NQ };
 
+// F is the type of the derived fields (K_iso in, K and Ai out) and of their
+// arithmetic: double for the FP64 drop-in, float for the split form. The
+// tracers stay FP64 in both: the vertical density gradient that every slope
+// divides by is a difference of nearby tracer values, and FP32 storage alone
+// would cost it ~1e-6 K of absolute accuracy.
+template <typename F>
 struct PreArgs {
   Layout L;
   Grid g;
@@ -45,9 +51,9 @@ struct PreArgs {
   double slopec, inv_dslope, ksteep;
   const double *__restrict__ T;
   const double *__restrict__ S;
-  const double *__restrict__ K;
+  const F *__restrict__ K;
   const uint8_t *__restrict__ m;
-  double *K11, *K22, *K33, *Aez, *Anz, *Abx, *Aby;
+  F *K11, *K22, *K33, *Aez, *Anz, *Abx, *Aby;
   long long sp, sr;
   int kchunk;
 };
@@ -78,7 +84,38 @@ __device__ __forceinline__ double taper_of(double s, double slopec, double inv_d
   return 0.5 * (1.0 + tanh(x));
 }
 
-__global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
+// Split form: the slope and the taper argument are FP64; the taper itself, a
+// bounded smooth function, is evaluated in FP32.
+__device__ __forceinline__ float taper_of_split(double s, double slopec, double inv_dslope) {
+  const float x = (float)((slopec - fabs(s)) * inv_dslope);
+  return 0.5f * (1.0f + tanhf(x));
+}
+
+template <typename F>
+__device__ __forceinline__ F taper_t(double s, double slopec, double inv_dslope);
+template <>
+__device__ __forceinline__ double taper_t<double>(double s, double slopec, double inv_dslope) {
+  return taper_of(s, slopec, inv_dslope);
+}
+template <>
+__device__ __forceinline__ float taper_t<float>(double s, double slopec, double inv_dslope) {
+  return taper_of_split(s, slopec, inv_dslope);
+}
+
+// taper * s^2 for the K_33 sums
+template <typename F>
+__device__ __forceinline__ F sq_term(F tp, F ai, double s);
+template <>
+__device__ __forceinline__ double sq_term<double>(double tp, double ai, double s) {
+  return tp * (s * s);
+}
+template <>
+__device__ __forceinline__ float sq_term<float>(float tp, float ai, double s) {
+  return ai * (float)s;
+}
+
+template <typename F>
+__global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs<F> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   double *zdzw = reinterpret_cast<double *>(smem_raw + sizeof(Smem));
@@ -138,19 +175,21 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
       if (p >= NP) break;
       const int pi = p % PX, pj = p / PX;
       const int i = i0 - 1 + pi, j = j0 - 1 + pj;
-      double rT = 0, rS = 0, dTx = 0, dSx = 0, dTy = 0, dSy = 0, dTz = 0, dSz = 0;
+      F rT = 0, rS = 0;
+      double dTx = 0, dSx = 0, dTy = 0, dSy = 0, dTz = 0, dSz = 0;
       if (i < L.X && j < L.Y) {
         const long long o = L.at(i, j, lev);
         const unsigned mk = __ldg(a.m + o);
         const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
         if (mk & VG_MASK_T) {
+          const F Tf = F(Tc);
           if (a.eos_type == 1)
-            rT = -Eos::betaT * Eos::rho0;
+            rT = F(-Eos::betaT * Eos::rho0);
           else if (a.eos_type == 3)
-            rT = -(Eos::betaTs3 * (Tc - Eos::theta0) + zeos[lev]) * Eos::rho0;
+            rT = -(F(Eos::betaTs3) * (Tf - F(Eos::theta0)) + F(zeos[lev])) * F(Eos::rho0);
           else
-            rT = -(Eos::betaT + 2.0 * Eos::betaTs24 * (Tc - Eos::theta0)) * Eos::rho0;
-          rS = a.eos_type == 4 ? 0.0 : Eos::betaS * Eos::rho0;
+            rT = -(F(Eos::betaT) + F(2.0 * Eos::betaTs24) * (Tf - F(Eos::theta0))) * F(Eos::rho0);
+          rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
         }
         if ((mk & VG_MASK_U) && i < L.X - 1) {
           const double f = sm.inv_dxu[pi] * sm.inv_cost[pj];
@@ -167,8 +206,9 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
         }
       }
       if (store) {
-        const double G0 = rT * carryT[s] + rS * carryS[s];  // face below (kr = 0)
-        const double G1 = rT * dTz + rS * dSz;              // face above (kr = 1)
+        // vertical density gradients in FP64 (exact products of the split form's FP32 values)
+        const double G0 = (double)rT * carryT[s] + (double)rS * carryS[s];  // face below (kr = 0)
+        const double G1 = (double)rT * dTz + (double)rS * dSz;                   // face above (kr = 1)
         double(*q)[NP] = sm.q[buf];
         q[Q_RT][p] = rT;
         q[Q_RS][p] = rS;
@@ -204,14 +244,14 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
 
     // east face: Ai_ez, K_11 (isoneutral.py:100-132)
     if (east) {
-      double sumz = 0.0;
+      F sumz = 0.0;
       if (mk & VG_MASK_U) {
-        double diffloc;
+        F diffloc;
         if (k >= 1)
-          diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + 1) +
-                            __ldg(a.K + o + 1 - L.plane));
+          diffloc = F(0.25) * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + 1) +
+                               __ldg(a.K + o + 1 - L.plane));
         else
-          diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + o + 1));
+          diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + 1));
         const double dTx = q[Q_TX][pc], dSx = q[Q_SX][pc];
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
@@ -220,9 +260,9 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           for (int ip = 0; ip < 2; ++ip) {
             const int pp = pc + ip;
             const double s = -(q[Q_RT][pp] * dTx + q[Q_RS][pp] * dSx) * q[kr ? Q_R1 : Q_R0][pp];
-            const double tp = taper_of(s, a.slopec, a.inv_dslope);
-            sumz += zdzw[k - 1 + kr] * fmax(a.ksteep, diffloc * tp);
-            a.Aez[o + ip * a.sp + kr * a.sr] = tp * s;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
+            a.Aez[o + ip * a.sp + kr * a.sr] = tp * F(s);
           }
         }
       } else {
@@ -233,19 +273,19 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           a.Aez[o + a.sp + kr * a.sr] = 0.0;
         }
       }
-      a.K11[o] = sumz * zq_dzt[k];
+      a.K11[o] = sumz * F(zq_dzt[k]);
     }
 
     // north face: Ai_nz, K_22 (isoneutral.py:137-168)
     if (north) {
-      double sumz = 0.0;
+      F sumz = 0.0;
       if (mk & VG_MASK_V) {
-        double diffloc;
+        F diffloc;
         if (k >= 1)
-          diffloc = 0.25 * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + L.pitch) +
-                            __ldg(a.K + o + L.pitch - L.plane));
+          diffloc = F(0.25) * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + L.pitch) +
+                               __ldg(a.K + o + L.pitch - L.plane));
         else
-          diffloc = 0.5 * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
+          diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
         const double dTy = q[Q_TY][pc], dSy = q[Q_SY][pc];
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
@@ -254,9 +294,9 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           for (int jp = 0; jp < 2; ++jp) {
             const int pp = pc + jp * PX;
             const double s = -(q[Q_RT][pp] * dTy + q[Q_RS][pp] * dSy) * q[kr ? Q_R1 : Q_R0][pp];
-            const double tp = taper_of(s, a.slopec, a.inv_dslope);
-            sumz += zdzw[k - 1 + kr] * fmax(a.ksteep, diffloc * tp);
-            a.Anz[o + jp * a.sp + kr * a.sr] = tp * s;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
+            a.Anz[o + jp * a.sp + kr * a.sr] = tp * F(s);
           }
         }
       } else {
@@ -267,14 +307,14 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           a.Anz[o + a.sp + kr * a.sr] = 0.0;
         }
       }
-      a.K22[o] = sumz * zq_dzt[k];
+      a.K22[o] = sumz * F(zq_dzt[k]);
     }
 
     // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224)
     if (top && k < Z - 1) {
-      double sumx = 0.0, sumy = 0.0;
+      F sumx = 0.0, sumy = 0.0;
       if (mk & VG_MASK_W) {
-        const double Kc = __ldg(a.K + o);
+        const F Kc = __ldg(a.K + o);
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
           const double(*qq)[NP] = kr ? qn : q;
@@ -284,17 +324,21 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           for (int ip = 0; ip < 2; ++ip) {
             const int pp = pc - 1 + ip;
             const double s = -(rT * qq[Q_TX][pp] + rS * qq[Q_SX][pp]) * Rz;
-            const double tp = taper_of(s, a.slopec, a.inv_dslope);
-            sumx += sm.dxu[tx + ip] * Kc * tp * (s * s);
-            a.Abx[o + ip * a.sp + kr * a.sr] = tp * s;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            const F ai = tp * F(s);
+            // FP64: dxu*K*taper*s^2 in the reference's order; split: (taper*s)*s, which stays
+            // finite where an FP32 s^2 would overflow under a vanishing taper
+            sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(tp, ai, s);
+            a.Abx[o + ip * a.sp + kr * a.sr] = ai;
           }
 #pragma unroll
           for (int jp = 0; jp < 2; ++jp) {
             const int pp = pc - PX + jp * PX;
             const double s = -(rT * qq[Q_TY][pp] + rS * qq[Q_SY][pp]) * Rz;
-            const double tp = taper_of(s, a.slopec, a.inv_dslope);
-            sumy += sm.facty[ty + jp] * Kc * tp * (s * s);
-            a.Aby[o + jp * a.sp + kr * a.sr] = tp * s;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            const F ai = tp * F(s);
+            sumy += F(sm.facty[ty + jp]) * Kc * sq_term<F>(tp, ai, s);
+            a.Aby[o + jp * a.sp + kr * a.sr] = ai;
           }
         }
       } else {
@@ -305,7 +349,7 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
           a.Aby[oc] = 0.0;
         }
       }
-      a.K33[o] = sumx * sm.qinv_dxt[tx + 1] + sumy * sm.qinv_dyt_cost[ty + 1];
+      a.K33[o] = sumx * F(sm.qinv_dxt[tx + 1]) + sumy * F(sm.qinv_dyt_cost[ty + 1]);
     }
     __syncthreads();
   }
@@ -317,20 +361,24 @@ __global__ void __launch_bounds__(NT, 2) pre_tile_kernel(PreArgs a) {
 
 using namespace vg;
 
-extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
-                                     const double *temp_tau, const double *salt_tau, const double *K_iso,
-                                     const uint8_t *mask_bits, const VgTensorFields *out, void *stream) {
+namespace vg {
+namespace {
+
+template <typename F, typename Out>
+int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+               const double *salt_tau, const F *K_iso, const uint8_t *mask_bits, const Out *out, void *stream,
+               const char *name) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
   if (!grid_complete(grid) || !set || !temp_tau || !salt_tau || !K_iso || !mask_bits || !out || !out->K_11 ||
       !out->K_22 || !out->K_33 || !out->Ai_ez || !out->Ai_nz || !out->Ai_bx || !out->Ai_by)
-    return fail(VG_ERR_ARG, "vg_isoneutral_pre_f64: NULL pointer argument");
+    return fail(VG_ERR_ARG, "%s: NULL pointer argument", name);
   if (set->eq_of_state_type < 1 || set->eq_of_state_type > 4)
     return fail(VG_ERR_UNSUPPORTED, "eq_of_state_type %d not implemented (1-4 are)", set->eq_of_state_type);
   if (!(set->iso_dslope != 0.0)) return fail(VG_ERR_ARG, "iso_dslope must be non-zero");
   if (dom->Z > 512) return fail(VG_ERR_SHAPE, "Z=%d above the 512 levels the per-CTA tables hold", dom->Z);
-  PreArgs a;
+  PreArgs<F> a;
   a.L = layout_of(dom);
   a.g = grid_of(grid);
   a.eos_type = set->eq_of_state_type;
@@ -357,8 +405,25 @@ extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, co
   a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
   const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
   const size_t smem = sizeof(Smem) + 4 * (size_t)a.L.Z * sizeof(double);
-  cudaError_t e = cudaFuncSetAttribute(pre_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(pre_tile_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_tile_kernel smem %zu: %s", smem, cudaGetErrorString(e));
-  pre_tile_kernel<<<dim3(nbx, nby, nbz), NT, smem, as_stream(stream)>>>(a);
+  pre_tile_kernel<F><<<dim3(nbx, nby, nbz), NT, smem, as_stream(stream)>>>(a);
   return check_launch("pre_tile_kernel");
+}
+
+}  // namespace
+}  // namespace vg
+
+extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                     const double *temp_tau, const double *salt_tau, const double *K_iso,
+                                     const uint8_t *mask_bits, const VgTensorFields *out, void *stream) {
+  return launch_pre<double>(dom, grid, set, temp_tau, salt_tau, K_iso, mask_bits, out, stream,
+                            "vg_isoneutral_pre_f64");
+}
+
+extern "C" int vg_isoneutral_pre_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                          const double *temp_tau, const double *salt_tau, const float *K_iso,
+                                          const uint8_t *mask_bits, const VgTensorFieldsF32 *out, void *stream) {
+  return launch_pre<float>(dom, grid, set, temp_tau, salt_tau, K_iso, mask_bits, out, stream,
+                           "vg_isoneutral_pre_f32split");
 }

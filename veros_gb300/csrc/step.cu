@@ -8,8 +8,9 @@
 namespace vg {
 namespace {
 
+template <typename F>
 __global__ void prepare_kernel(Layout L, const uint8_t *__restrict__ m, const double *__restrict__ T0, double *T1,
-                               const double *__restrict__ S0, double *S1, double *dT, double *dS, double *P) {
+                               const double *__restrict__ S0, double *S1, F *dT, F *dS, F *P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y, k = blockIdx.z;
   if (i >= L.X) return;
@@ -17,9 +18,24 @@ __global__ void prepare_kernel(Layout L, const uint8_t *__restrict__ m, const do
   const double mT = (__ldg(m + o) & VG_MASK_T) ? 1.0 : 0.0;
   T1[o] = T0[o] * mT;
   S1[o] = S0[o] * mT;
-  dT[o] = 0.0;
-  dS[o] = 0.0;
-  if (P) P[o] = 0.0;
+  dT[o] = F(0.0);
+  dS[o] = F(0.0);
+  if (P) P[o] = F(0.0);
+}
+
+template <typename F, typename Fields>
+int prepare(const VgDomain *dom, const Fields *f, void *stream, const char *name) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  if (!f || !f->temp_tau || !f->temp_taup1 || !f->salt_tau || !f->salt_taup1 || !f->mask_bits || !f->dtemp_iso ||
+      !f->dsalt_iso)
+    return fail(VG_ERR_ARG, "%s: NULL pointer argument", name);
+  Layout L = layout_of(dom);
+  dim3 block(128), g((L.X + 127) / 128, L.Y, L.Z);
+  prepare_kernel<F><<<g, block, 0, as_stream(stream)>>>(L, f->mask_bits, f->temp_tau, f->temp_taup1, f->salt_tau,
+                                                        f->salt_taup1, f->dtemp_iso, f->dsalt_iso, f->P_diss_iso);
+  return check_launch("prepare_kernel");
 }
 
 }  // namespace
@@ -28,28 +44,17 @@ __global__ void prepare_kernel(Layout L, const uint8_t *__restrict__ m, const do
 using namespace vg;
 
 extern "C" int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, void *stream) {
-  clear_error();
-  int st = validate_domain(dom);
-  if (st) return st;
-  if (!f || !f->temp_tau || !f->temp_taup1 || !f->salt_tau || !f->salt_taup1 || !f->mask_bits || !f->dtemp_iso ||
-      !f->dsalt_iso)
-    return fail(VG_ERR_ARG, "vg_isoneutral_step_prepare_f64: NULL pointer argument");
-  Layout L = layout_of(dom);
-  dim3 block(128), g((L.X + 127) / 128, L.Y, L.Z);
-  prepare_kernel<<<g, block, 0, as_stream(stream)>>>(L, f->mask_bits, f->temp_tau, f->temp_taup1, f->salt_tau,
-                                                     f->salt_taup1, f->dtemp_iso, f->dsalt_iso, f->P_diss_iso);
-  return check_launch("prepare_kernel");
+  return prepare<double>(dom, f, stream, "vg_isoneutral_step_prepare_f64");
+}
+
+extern "C" int vg_isoneutral_step_prepare_f32split(const VgDomain *dom, const VgStepFieldsF32 *f, void *stream) {
+  return prepare<float>(dom, f, stream, "vg_isoneutral_step_prepare_f32split");
 }
 
 extern "C" int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                       const VgStepFields *f, void *scratch, size_t scratch_bytes, void *stream) {
-  clear_error();
-  int st = validate_domain(dom);
-  if (st) return st;
-  if (!f || !f->temp_tau || !f->temp_taup1 || !f->salt_tau || !f->salt_taup1 || !f->mask_bits || !f->dtemp_iso ||
-      !f->dsalt_iso)
-    return fail(VG_ERR_ARG, "vg_isoneutral_step_f64: NULL pointer argument");
-  if (set && set->enable_conserve_energy && (!f->P_diss_iso || !f->int_drhodT_tau || !f->int_drhodS_tau))
+  int st;
+  if (set && set->enable_conserve_energy && f && (!f->P_diss_iso || !f->int_drhodT_tau || !f->int_drhodS_tau))
     return fail(VG_ERR_ARG, "enable_conserve_energy needs P_diss_iso and int_drhodT/S");
   if ((st = vg_isoneutral_step_prepare_f64(dom, f, stream))) return st;
   if ((st = vg_isoneutral_pre_f64(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten, stream)))
@@ -58,4 +63,20 @@ extern "C" int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, c
   VgTracerArgs trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
   return vg_isoneutral_diffusion_pair_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS, scratch,
                                           scratch_bytes, stream);
+}
+
+extern "C" int vg_isoneutral_step_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                           const VgStepFieldsF32 *f, void *scratch, size_t scratch_bytes,
+                                           void *stream) {
+  int st;
+  if (set && set->enable_conserve_energy && f && (!f->P_diss_iso || !f->int_drhodT_tau || !f->int_drhodS_tau))
+    return fail(VG_ERR_ARG, "enable_conserve_energy needs P_diss_iso and int_drhodT/S");
+  if ((st = vg_isoneutral_step_prepare_f32split(dom, f, stream))) return st;
+  if ((st = vg_isoneutral_pre_f32split(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten,
+                                       stream)))
+    return st;
+  VgTracerArgsF32 trT{f->temp_tau, f->temp_taup1, f->dtemp_iso, f->int_drhodT_tau, f->P_diss_iso};
+  VgTracerArgsF32 trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
+  return vg_isoneutral_diffusion_pair_f32split(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
+                                               scratch, scratch_bytes, stream);
 }

@@ -38,9 +38,9 @@ def run_pre(dev):
     v = dev.variables
     dev.check_layout(("temp", "salt", "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by"))
     lib = _capi.load()
-    st = lib.vg_isoneutral_pre_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), _level(v.temp, v.tau),
-                                   _level(v.salt, v.tau), v.K_iso.data_ptr(), dev.mask_bits().data_ptr(),
-                                   dev.tensor_fields(), _stream(dev))
+    fn = lib.vg_isoneutral_pre_f64 if dev.precision == "f64" else lib.vg_isoneutral_pre_f32split
+    st = fn(dev.domain(), dev.grid(), dev.settings.to_struct(), _level(v.temp, v.tau), _level(v.salt, v.tau),
+            v.K_iso.data_ptr(), dev.mask_bits().data_ptr(), dev.tensor_fields(), _stream(dev))
     _capi.check(st, "isoneutral_diffusion_pre")
 
 
@@ -61,22 +61,23 @@ def run_diffusion(dev, istemp, skew=False, scratch=None):
     if energy:
         names += ["int_drhodT" if istemp else "int_drhodS", "P_diss_skew" if skew else "P_diss_iso"]
     dev.check_layout(names)
+    targs = _capi.VgTracerArgs if dev.precision == "f64" else _capi.VgTracerArgsF32
     if energy:
         idr = (v.int_drhodT if istemp else v.int_drhodS)
         P = v.P_diss_skew if skew else v.P_diss_iso
-        tra = _capi.VgTracerArgs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), _level(idr, v.tau),
-                                 P.data_ptr())
+        tra = targs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), _level(idr, v.tau), P.data_ptr())
     else:
-        tra = _capi.VgTracerArgs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), None, None)
+        tra = targs(_level(tr, v.tau), _level(tr, v.taup1), dtr.data_ptr(), None, None)
     if scratch is None:
         scratch = diffusion_scratch(dev)
     kb = v.kbot
     if kb.stride(0) != 1 or kb.stride(1) != dev.pitch:
         raise ValueError("kbot is not in the canonical layout")
     lib = _capi.load()
-    st = lib.vg_isoneutral_diffusion_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), dev.tensor_fields(),
-                                         kfield.data_ptr(), dev.mask_bits().data_ptr(), kb.data_ptr(), tra,
-                                         1 if skew else 0, scratch.data_ptr(), scratch.numel() * 8, _stream(dev))
+    fn = lib.vg_isoneutral_diffusion_f64 if dev.precision == "f64" else lib.vg_isoneutral_diffusion_f32split
+    st = fn(dev.domain(), dev.grid(), dev.settings.to_struct(), dev.tensor_fields(), kfield.data_ptr(),
+            dev.mask_bits().data_ptr(), kb.data_ptr(), tra, 1 if skew else 0, scratch.data_ptr(),
+            scratch.numel() * 8, _stream(dev))
     _capi.check(st, "isoneutral_skew_diffusion" if skew else "isoneutral_diffusion")
 
 

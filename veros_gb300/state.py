@@ -133,10 +133,23 @@ class DeviceVariables:
             setattr(self, k, v)
 
 
-class DeviceState:
-    """One ocean domain resident on a CUDA device in the canonical layout."""
+PRECISIONS = ("f64", "f32split")
 
-    def __init__(self, nx, ny, nz, settings, device="cuda"):
+
+class DeviceState:
+    """One ocean domain resident on a CUDA device in the canonical layout.
+
+    ``precision``: ``"f64"`` (the drop-in: every field float64) or
+    ``"f32split"`` (diffusivities, tensors, tendencies and dissipation stored
+    as float32; tracers, grid, the slope denominators and slopes and the
+    implicit vertical solve stay float64).
+    """
+
+    def __init__(self, nx, ny, nz, settings, device="cuda", precision="f64"):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {PRECISIONS}")
+        self.precision = precision
+        self.fdtype = torch.float64 if precision == "f64" else torch.float32
         self.nx, self.ny, self.nz = nx, ny, nz
         self.X, self.Y, self.Z = nx + 4, ny + 4, nz
         device = torch.device(device)
@@ -155,12 +168,14 @@ class DeviceState:
     def alloc_fields(self):
         X, Y, Z, dev = self.X, self.Y, self.Z, self.device
         v = self.variables
+        fd = self.fdtype
         for n in FIELDS_3D:
-            setattr(v, n, canonical_zeros(X, Y, Z, device=dev))
+            setattr(v, n, canonical_zeros(X, Y, Z, dtype=fd, device=dev))
         for n in FIELDS_TIME:
-            setattr(v, n, canonical_zeros(X, Y, Z, (3,), device=dev))
+            dt_ = torch.float64 if n in ("temp", "salt") else fd
+            setattr(v, n, canonical_zeros(X, Y, Z, (3,), dtype=dt_, device=dev))
         for n in FIELDS_TENSOR:
-            setattr(v, n, canonical_zeros(X, Y, Z, (2, 2), device=dev))
+            setattr(v, n, canonical_zeros(X, Y, Z, (2, 2), dtype=fd, device=dev))
         for n in FIELDS_MASK:
             setattr(v, n, canonical_zeros(X, Y, Z, dtype=torch.bool, device=dev))
         kb = canonical_empty_2d(X, Y, device=dev)
@@ -174,7 +189,7 @@ class DeviceState:
             setattr(v, n, torch.zeros(Z, dtype=torch.float64, device=dev))
 
     @classmethod
-    def from_host(cls, host, device="cuda", fields=None):
+    def from_host(cls, host, device="cuda", fields=None, precision="f64"):
         """Upload a ``synthetic.HostState`` or a NumPy ``VerosState``."""
         if hasattr(host, "variables"):  # a VerosState
             vs = host.variables
@@ -187,7 +202,7 @@ class DeviceState:
             settings = {n: host.settings[n] for n in SETTING_NAMES if n in host.settings}
             get = lambda n: host.arrays.get(n)  # noqa: E731
             taus = (host.tau, host.taup1, host.taum1)
-        st = cls(nx, ny, nz, settings, device=device)
+        st = cls(nx, ny, nz, settings, device=device, precision=precision)
         st.alloc_fields()
         v = st.variables
         v.tau, v.taup1, v.taum1 = (int(t) for t in taus)
@@ -242,11 +257,15 @@ class DeviceState:
     def tensor_fields(self):
         v = self.variables
         ai = v.Ai_ez
-        for n in FIELDS_TENSOR:
+        for n in FIELDS_TENSOR + ("K_11", "K_22", "K_33"):
             t = getattr(v, n)
-            if t.stride()[3:] != ai.stride()[3:]:
+            want = torch.float64 if n in ("temp", "salt") else self.fdtype
+            if t.dtype != want:
+                raise ValueError(f"{n}: dtype {t.dtype} but the state's precision needs {want}")
+            if n in FIELDS_TENSOR and t.stride()[3:] != ai.stride()[3:]:
                 raise ValueError(f"{n}: component strides {t.stride()[3:]} differ from Ai_ez {ai.stride()[3:]}")
-        return _capi.VgTensorFields(v.K_11.data_ptr(), v.K_22.data_ptr(), v.K_33.data_ptr(), v.Ai_ez.data_ptr(),
+        cls = _capi.VgTensorFields if self.precision == "f64" else _capi.VgTensorFieldsF32
+        return cls(v.K_11.data_ptr(), v.K_22.data_ptr(), v.K_33.data_ptr(), v.Ai_ez.data_ptr(),
                                     v.Ai_nz.data_ptr(), v.Ai_bx.data_ptr(), v.Ai_by.data_ptr(),
                                     ai.stride(3), ai.stride(4))
 
@@ -256,6 +275,9 @@ class DeviceState:
             t = getattr(v, n)
             if not t.is_cuda or t.device != self.device:
                 raise ValueError(f"{n} is not on {self.device}")
+            want = torch.float64 if n in ("temp", "salt") else self.fdtype
+            if t.dtype != want:
+                raise ValueError(f"{n}: dtype {t.dtype} but the state's precision needs {want}")
             if not is_canonical(t, self.X, self.Y, self.Z) or t.stride(1) != self.pitch:
                 raise ValueError(f"{n}: strides {t.stride()} are not the canonical layout (pitch {self.pitch})")
 

@@ -28,17 +28,22 @@ class IsoneutralStepper:
         energy = bool(dev.settings.enable_conserve_energy)
         dev.check_layout(("temp", "salt", "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by",
                           "dtemp_iso", "dsalt_iso", "P_diss_iso", "int_drhodT", "int_drhodS"))
-        return _capi.VgStepFields(
+        cls = _capi.VgStepFields if dev.precision == "f64" else _capi.VgStepFieldsF32
+        return cls(
             lvl(v.temp, v.tau), lvl(v.temp, v.taup1), lvl(v.salt, v.tau), lvl(v.salt, v.taup1), v.K_iso.data_ptr(),
             dev.mask_bits().data_ptr(), v.kbot.data_ptr(), dev.tensor_fields(), v.dtemp_iso.data_ptr(),
             v.dsalt_iso.data_ptr(), lvl(v.int_drhodT, v.tau) if energy else None,
             lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr())
 
+    def _fn(self, name):
+        suffix = "_f64" if self.dev.precision == "f64" else "_f32split"
+        return getattr(self.lib, name + suffix)
+
     def _launch(self, stream):
         dev = self.dev
-        st = self.lib.vg_isoneutral_step_f64(dev.domain(), dev.grid(), dev.settings.to_struct(), self._fields(),
-                                             self.scratch.data_ptr(), self.scratch.numel() * 8, stream)
-        _capi.check(st, "vg_isoneutral_step_f64")
+        st = self._fn("vg_isoneutral_step")(dev.domain(), dev.grid(), dev.settings.to_struct(), self._fields(),
+                                            self.scratch.data_ptr(), self.scratch.numel() * 8, stream)
+        _capi.check(st, "isoneutral step")
 
     def _rotate(self):
         v = self.dev.variables
@@ -65,15 +70,17 @@ class IsoneutralStepper:
         nbytes = self.scratch.numel() * 8
         rec = (lambda n: events[n].record(stream_obj)) if events else (lambda n: None)
         rec(0)
-        _capi.check(lib.vg_isoneutral_step_prepare_f64(dom, f, stream), "step prepare")
+        _capi.check(self._fn("vg_isoneutral_step_prepare")(dom, f, stream), "step prepare")
         rec(1)
-        _capi.check(lib.vg_isoneutral_pre_f64(dom, grid, sett, f.temp_tau, f.salt_tau, f.K_iso, f.mask_bits,
-                                              f.ten, stream), "pre")
+        _capi.check(self._fn("vg_isoneutral_pre")(dom, grid, sett, f.temp_tau, f.salt_tau, f.K_iso, f.mask_bits,
+                                                  f.ten, stream), "pre")
         rec(2)
-        trT = _capi.VgTracerArgs(f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau, f.P_diss_iso)
-        trS = _capi.VgTracerArgs(f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau, f.P_diss_iso)
-        _capi.check(lib.vg_isoneutral_diffusion_pair_f64(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot, trT, trS,
-                                                         self.scratch.data_ptr(), nbytes, stream), "diffusion")
+        targs = _capi.VgTracerArgs if dev.precision == "f64" else _capi.VgTracerArgsF32
+        trT = targs(f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau, f.P_diss_iso)
+        trS = targs(f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau, f.P_diss_iso)
+        _capi.check(self._fn("vg_isoneutral_diffusion_pair")(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot,
+                                                             trT, trS, self.scratch.data_ptr(), nbytes, stream),
+                    "diffusion")
         rec(3)
         self._rotate()
 

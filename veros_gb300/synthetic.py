@@ -199,7 +199,7 @@ def eos_int_drhodS(eq_type, p):
 
 def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_origin=-60.0,
                dz_top=10.0, dz_bottom=400.0, land_fraction=0.15, eq_of_state_type=1,
-               k_iso_lognormal_sigma=None, settings=None):
+               k_iso_lognormal_sigma=None, settings=None, stable_caps=False):
     """Build one seeded synthetic state.
 
     * ``kbot``: each interior column is land with probability ``land_fraction``,
@@ -208,6 +208,11 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
       identical on the three time levels and multiplied by ``maskT``.
     * ``K_iso``: constant ``K_iso_0``, or lognormal with median ``K_iso_0`` when
       ``k_iso_lognormal_sigma`` is given.
+    * ``stable_caps``: rows whose zonal spacing is below the stability limit
+      of the explicit horizontal diffusion, ``K_iso dt / dx^2 <= 1/4`` with
+      ``dx = dxt cos(lat)``, are land (the polar caps of a global grid, where
+      cos(lat) -> 0; the reference's own 1-degree setup stops at 79S/81N,
+      veros/setups/global_1deg/global_1deg.py:29-36).
     """
     rng = np.random.default_rng(seed)
     X, Y, Z = nx + 4, ny + 4, nz
@@ -222,6 +227,10 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
     land = rng.random((nx, ny)) < land_fraction
     depth = rng.integers(1, nz + 1, size=(nx, ny))
     kb[2:-2, 2:-2] = np.where(land, 0, depth)
+    if stable_caps:
+        dx_min = np.minimum(grid["dxt"].min() * np.abs(grid["cost"]), grid["dyt"].min())
+        unstable = s["K_iso_0"] * s["dt_tracer"] / dx_min**2 > 0.25
+        kb[:, unstable] = 0
     kbot, maskT, maskU, maskV, maskW = calc_topo(kb, nz)
 
     zt = grid["zt"]
@@ -266,13 +275,13 @@ def small_linear_state(seed=0):
 
 
 def global_1deg_state(seed=0, nz=60, k_iso_lognormal_sigma=None):
-    """360 x 180 x nz at 1 degree, global latitude band, dz 10-250 m, ~30% land, nonlinear EOS."""
+    """360 x 180 x nz at 1 degree, -90..90, dz 10-250 m, ~30% land plus polar caps beyond 83 deg, nonlinear EOS."""
     return make_state(360, 180, nz, seed=seed, dx_deg=1.0, dy_deg=1.0, y_origin=-90.0, dz_top=10.0,
                       dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3,
-                      k_iso_lognormal_sigma=k_iso_lognormal_sigma)
+                      k_iso_lognormal_sigma=k_iso_lognormal_sigma, stable_caps=True)
 
 
 def global_quarter_deg_state(seed=0):
-    """1440 x 720 x 60 at 0.25 degree, dz 10-250 m, ~30% land, nonlinear EOS."""
+    """1440 x 720 x 60 at 0.25 degree, -90..90, dz 10-250 m, ~30% land plus polar caps beyond 62 deg, nonlinear EOS."""
     return make_state(1440, 720, 60, seed=seed, dx_deg=0.25, dy_deg=0.25, y_origin=-90.0, dz_top=10.0,
-                      dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3)
+                      dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3, stable_caps=True)
