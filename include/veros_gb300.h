@@ -230,6 +230,44 @@ int vg_isoneutral_step_prepare_f32split(const VgDomain *dom, const VgStepFieldsF
  * tendencies), for callers that time or interleave the stages. */
 int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, void *stream);
 
+/* ---- Batched ensemble ------------------------------------------------------
+ * One isoneutral step of many domains (uneven extents and kbot) with one
+ * persistent launch per stage. No reference counterpart: Veros steps one
+ * domain per process. Each member gives its domain, grid, settings and its
+ * step fields for the three time-level phases (phase p = the pointers after p
+ * rotations). The energy branch is not batched (VG_ERR_UNSUPPORTED). */
+typedef struct VgEnsembleTuning {
+  int pre_rows;       /* columns per CTA / 32 of the slope kernel: 4 or 8 */
+  int pre_kchunk;     /* levels per CTA of the slope kernel, 0 = whole column */
+  int flux_rows;      /* columns per CTA / 32 of the flux kernel: 4 or 8 */
+  int flux_kchunk;    /* levels per CTA of the flux kernel, 0 = whole column */
+  int solve_threads;  /* columns per CTA of the implicit solve: 32 or 64 */
+} VgEnsembleTuning;
+
+typedef struct VgEnsembleMember {
+  VgDomain dom;
+  VgGrid grid;
+  VgIsoSettings set;
+  VgStepFields phase[3];
+} VgEnsembleMember;
+
+typedef struct VgEnsembleMemberF32 {
+  VgDomain dom;
+  VgGrid grid;
+  VgIsoSettings set;
+  VgStepFieldsF32 phase[3];
+} VgEnsembleMemberF32;
+
+/* Build the device tables (allocates device memory); *handle receives the ensemble. */
+int vg_ensemble_create_f64(const VgEnsembleMember *members, int n, const VgEnsembleTuning *tuning, void **handle);
+int vg_ensemble_create_f32split(const VgEnsembleMemberF32 *members, int n, const VgEnsembleTuning *tuning,
+                                void **handle);
+/* Re-tile the work lists (the autotuner's knob). */
+int vg_ensemble_tune(void *handle, const VgEnsembleTuning *tuning);
+/* One step of every member at time-level phase 0..2: a counter reset and four launches. */
+int vg_ensemble_step(void *handle, int phase, void *stream);
+int vg_ensemble_destroy(void *handle);
+
 /* Replaces veros.core.utilities.solve_implicit (veros/core/utilities.py:51-59)
  * and veros.core.operators.solve_tridiagonal (veros/core/operators.py:60-77,
  * :102-156). nsys columns of nz levels; element (s, k) of every array is at

@@ -70,6 +70,18 @@ class VgStepFieldsF32(ctypes.Structure):
         (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso")]
 
 
+class VgEnsembleTuning(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("pre_rows", "pre_kchunk", "flux_rows", "flux_kchunk", "solve_threads")]
+
+
+class VgEnsembleMember(ctypes.Structure):
+    _fields_ = [("dom", VgDomain), ("grid", VgGrid), ("set", VgIsoSettings), ("phase", VgStepFields * 3)]
+
+
+class VgEnsembleMemberF32(ctypes.Structure):
+    _fields_ = [("dom", VgDomain), ("grid", VgGrid), ("set", VgIsoSettings), ("phase", VgStepFieldsF32 * 3)]
+
+
 # name -> (restype, argtypes); the exported C ABI
 SIGNATURES = {
     "vg_last_error": (ctypes.c_char_p, []),
@@ -125,6 +137,14 @@ SIGNATURES = {
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_isoneutral_step_prepare_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgStepFields),
                                                       ctypes.c_void_p]),
+    "vg_ensemble_create_f64": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMember), ctypes.c_int,
+                                              ctypes.POINTER(VgEnsembleTuning), ctypes.POINTER(ctypes.c_void_p)]),
+    "vg_ensemble_create_f32split": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMemberF32), ctypes.c_int,
+                                                   ctypes.POINTER(VgEnsembleTuning),
+                                                   ctypes.POINTER(ctypes.c_void_p)]),
+    "vg_ensemble_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(VgEnsembleTuning)]),
+    "vg_ensemble_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "vg_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "vg_solve_implicit_f64": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
                                              ctypes.c_longlong, ctypes.c_longlong] + [ctypes.c_void_p] * 11),
     "vg_tdma_cuda_double": (None, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,

@@ -35,7 +35,7 @@ def main():
         fh.write("constexpr double kTaperPerUnit = %d.0;\n" % PER_UNIT)
         fh.write("constexpr int kTaperN = %d;\n" % n)
         fh.write("constexpr int kTaperDeg = %d;\n" % DEG)
-        fh.write("__device__ const double kTaperCoef[%d][%d] = {\n" % (n, DEG + 1))
+        fh.write("static __device__ const double kTaperCoef[%d][%d] = {\n" % (n, DEG + 1))
         fh.write("\n".join(rows))
         fh.write("\n};\n")
     print(out)

@@ -1,410 +1,8 @@
-// Isoneutral tracer diffusion (FP64), the work of
-// veros/core/isoneutral/diffusion.py:9-295 and veros/core/diffusion.py:9-62.
-//
-// Two launches per tracer (three with the energy branch):
-//  1. flux_div_kernel  2.5-D tiled: a CTA owns 32 x 8 interior columns and
-//                      walks k upward. Per level it forms the east, north and
-//                      top fluxes (diffusion.py:9-113) of its faces plus the
-//                      west/south halo faces, exchanges them through shared
-//                      memory, and applies the divergence (:116-139), the
-//                      explicit update of tr[taup1] and the dtracer_iso
-//                      accumulation (:196-197). Grid divisions are
-//                      multiplications by per-thread reciprocals.
-//  2. implicit_kernel  (iso only) one thread per interior column: the
-//                      implicit K_33 solve (:142-169) as a Thomas sweep whose
-//                      c'/d' live in shared memory, shared by temp and salt
-//                      when both are diffused together, and the second
-//                      dtracer_iso term (:204).
-//  3. energy_kernel    (enable_conserve_energy) dissipation on the W grid and
-//                      the vertical-mixing term added to P_diss (:234-281),
-//                      from the fluxes step 1 saved in the scratch buffer.
-#include "common.cuh"
-#include "dgtsv.cuh"  // rounded arithmetic helpers
-
-namespace vg {
-
-namespace {
-
-constexpr int TX = 32, TY = 8, NT = TX * TY;
-
-// F is the type of the derived fields (tensors, tendencies, dissipation) and of
-// the flux arithmetic: double for the FP64 drop-in, float for the split form.
-// Tracers stay FP64 in both (their differences feed the fluxes and their
-// increments are small against their values); the implicit solve is FP64.
-template <typename F>
-struct DiffArgs {
-  Layout L;
-  Grid g;
-  double dt, grav, rho0;
-  const F *__restrict__ K;  // K_iso (iso) or K_gm (skew)
-  double s1, s2;            // K1 = s1*K, K2 = s2*K (diffusion.py:15-16)
-  const F *__restrict__ K11;
-  const F *__restrict__ K22;
-  const F *__restrict__ K33;
-  const F *__restrict__ Aez;
-  const F *__restrict__ Anz;
-  const F *__restrict__ Abx;
-  const F *__restrict__ Aby;
-  long long sp, sr;
-  const uint8_t *__restrict__ m;
-  const int32_t *__restrict__ kbot;
-  const double *__restrict__ tr;  // tau
-  double *trp;                    // taup1
-  F *dtr_iso;
-  const F *__restrict__ idr;  // int_drhodX at tau
-  F *P;
-  F *fe, *fn, *ft;  // scratch fluxes (energy branch)
-  int iso, save_fluxes, kchunk;
-};
-
-template <typename F>
-__device__ __forceinline__ F ld(const F *p, long long o) { return __ldg(p + o); }
-
-// x + y and x * y: explicitly rounded in FP64 (no contraction into the
-// explicit update, which feeds the tendency's differencing), plain in FP32.
-__device__ __forceinline__ double add_(double x, double y) { return radd(x, y); }
-__device__ __forceinline__ double mul_(double x, double y) { return rmul(x, y); }
-__device__ __forceinline__ float add_(float x, float y) { return x + y; }
-__device__ __forceinline__ float mul_(float x, float y) { return x * y; }
-
-// east-face flux at cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
-template <typename F>
-__device__ __forceinline__ F flux_east(const DiffArgs<F> &a, int i, int j, int k, F inv_cost_dxu, F q_dzt) {
-  const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
-  const int Z = L.Z;
-  const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
-  const long long dp = k < Z - 1 ? L.plane : 0;
-  const F s1 = F(a.s1);
-  F diffloc;
-  if (k >= 1)
-    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + 1) +
-                         s1 * ld(a.K, o + 1 - L.plane));
-  else
-    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + 1));
-  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + 1);
-  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + 1 - dm);
-  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + 1 + dp);
-  F sumz = 0.0;
-  sumz += diffloc * ld(a.Aez, o) * F(t0 - t0m);
-  sumz += diffloc * ld(a.Aez, o + a.sp) * F(t1 - t1m);
-  sumz += diffloc * ld(a.Aez, o + a.sr) * F(t0p - t0);
-  sumz += diffloc * ld(a.Aez, o + a.sp + a.sr) * F(t1p - t1);
-  return sumz * q_dzt + F(t1 - t0) * inv_cost_dxu * ld(a.K11, o);
-}
-
-// north-face flux at cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
-template <typename F>
-__device__ __forceinline__ F flux_north(const DiffArgs<F> &a, int i, int j, int k, F cosu, F inv_dyu, F q_dzt) {
-  const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
-  const long long P = L.pitch;
-  const int Z = L.Z;
-  const long long dm = k > 0 ? L.plane : 0;
-  const long long dp = k < Z - 1 ? L.plane : 0;
-  const F s1 = F(a.s1);
-  F diffloc;
-  if (k >= 1)
-    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + P) +
-                         s1 * ld(a.K, o + P - L.plane));
-  else
-    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + P));
-  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + P);
-  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + P - dm);
-  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + P + dp);
-  F sumz = 0.0;
-  sumz += diffloc * ld(a.Anz, o) * F(t0 - t0m);
-  sumz += diffloc * ld(a.Anz, o + a.sp) * F(t1 - t1m);
-  sumz += diffloc * ld(a.Anz, o + a.sr) * F(t0p - t0);
-  sumz += diffloc * ld(a.Anz, o + a.sp + a.sr) * F(t1p - t1);
-  return cosu * (sumz * q_dzt + F(t1 - t0) * inv_dyu * ld(a.K22, o));
-}
-
-// top-face flux at interior cell (i, j, k < Z-1) (diffusion.py:85-111)
-template <typename F>
-__device__ __forceinline__ F flux_top(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F q_dxt,
-                                      F q_dyt_cost) {
-  const Layout &L = a.L;
-  const long long P = L.pitch, Q = L.plane;
-  const F diffloc = F(a.s2) * ld(a.K, o);
-  const double tc = ld(a.tr, o), tcu = ld(a.tr, o + Q);
-  F sumx = 0.0;
-  sumx += diffloc * ld(a.Abx, o) * inv_cost * F(tc - ld(a.tr, o - 1));
-  sumx += diffloc * ld(a.Abx, o + a.sr) * inv_cost * F(tcu - ld(a.tr, o - 1 + Q));
-  sumx += diffloc * ld(a.Abx, o + a.sp) * inv_cost * F(ld(a.tr, o + 1) - tc);
-  sumx += diffloc * ld(a.Abx, o + a.sp + a.sr) * inv_cost * F(ld(a.tr, o + 1 + Q) - tcu);
-  F sumy = 0.0;
-  sumy += diffloc * ld(a.Aby, o) * cosu_s * F(tc - ld(a.tr, o - P));
-  sumy += diffloc * ld(a.Aby, o + a.sr) * cosu_s * F(tcu - ld(a.tr, o - P + Q));
-  sumy += diffloc * ld(a.Aby, o + a.sp) * cosu_c * F(ld(a.tr, o + P) - tc);
-  sumy += diffloc * ld(a.Aby, o + a.sp + a.sr) * cosu_c * F(ld(a.tr, o + P + Q) - tcu);
-  return sumx * q_dxt + sumy * q_dyt_cost;
-}
-
-template <typename F>
-__global__ void __launch_bounds__(NT, 2) flux_div_kernel(DiffArgs<F> a) {
-  __shared__ F fe_s[2][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
-  __shared__ F fn_s[2][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
-  extern __shared__ double zq_dzt[];      // 1/(4 dzt[k]), then 1/dzt[k]
-  const Layout &L = a.L;
-  const int Z = L.Z;
-  double *zinv_dzt = zq_dzt + Z;
-  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX, warp = tid / 32, lane = tid % 32;
-  const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
-  const int kb = blockIdx.z * a.kchunk, ke = min(Z, kb + a.kchunk);
-  for (int k = tid; k < Z; k += NT) {
-    zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
-    zinv_dzt[k] = 1.0 / a.g.dzt[k];
-  }
-  __syncthreads();
-
-  const int i = i0 + tx, j = j0 + ty;
-  const bool own = i < L.X - 2 && j < L.Y - 2;
-  const int ic = min(i, L.X - 3), jc = min(j, L.Y - 3);
-  const double cost = a.g.cost[jc];
-  const F inv_cost = F(1.0 / cost);
-  const F inv_cost_dxu = F(1.0 / (cost * a.g.dxu[ic]));
-  const F cosu_c = F(a.g.cosu[jc]), cosu_s = F(a.g.cosu[jc - 1]);
-  const F inv_dyu = F(1.0 / a.g.dyu[jc]);
-  const F inv_fx = F(1.0 / (cost * a.g.dxt[ic]));  // divergence factors (diffusion.py:127, :129)
-  const F inv_fy = F(1.0 / (cost * a.g.dyt[jc]));
-  const F q_dxt = F(1.0 / (4.0 * a.g.dxt[ic]));
-  const F q_dyt_cost = F(1.0 / (4.0 * a.g.dyt[jc] * cost));
-  // halo faces: warp 0 the south row of north faces, warp 1 the west column of east faces
-  const int hi_n = i0 + lane;  // north face (hi_n, j0-1)
-  const bool halo_n = warp == 0 && hi_n < L.X - 2 && j0 - 1 < L.Y - 2;
-  const int hj_e = j0 + lane;  // east face (i0-1, hj_e)
-  const bool halo_e = warp == 1 && lane < TY && hj_e < L.Y - 2 && i0 - 1 < L.X - 2;
-  F h_cosu = 0, h_inv_dyu = 0, h_inv_cost_dxu = 0;
-  if (halo_n) {
-    h_cosu = F(a.g.cosu[j0 - 1]);
-    h_inv_dyu = F(1.0 / a.g.dyu[j0 - 1]);
-  }
-  if (halo_e) h_inv_cost_dxu = F(1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]));
-
-  F ft_prev = 0.0;
-  if (own && kb > 0) ft_prev = flux_top(a, L.at(i, j, kb - 1), inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
-
-  for (int k = kb; k < ke; ++k) {
-    // double-buffered exchange: the barrier of level k+1 orders level k's
-    // reads before level k+2's writes to the same buffer
-    const int b = k & 1;
-    const long long o = L.at(i, j, k);
-    F fe = 0, fn = 0, ft = 0;
-    if (own) {
-      fe = flux_east(a, i, j, k, inv_cost_dxu, F(zq_dzt[k]));
-      fn = flux_north(a, i, j, k, cosu_c, inv_dyu, F(zq_dzt[k]));
-      if (k < Z - 1) ft = flux_top(a, o, inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
-      fe_s[b][ty][tx + 1] = fe;
-      fn_s[b][ty + 1][tx] = fn;
-    }
-    if (halo_n) fn_s[b][0][lane] = flux_north(a, hi_n, j0 - 1, k, h_cosu, h_inv_dyu, F(zq_dzt[k]));
-    if (halo_e) fe_s[b][lane][0] = flux_east(a, i0 - 1, hj_e, k, h_inv_cost_dxu, F(zq_dzt[k]));
-    __syncthreads();
-    if (own) {
-      const F mT = (__ldg(a.m + o) & VG_MASK_T) ? F(1.0) : F(0.0);
-      F e = mT * ((fe - fe_s[b][ty][tx]) * inv_fx + (fn - fn_s[b][ty][tx]) * inv_fy);
-      e = e + mT * (ft - ft_prev) * F(zinv_dzt[k]);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
-      ft_prev = ft;
-      a.dtr_iso[o] = add_(a.dtr_iso[o], e);
-      a.trp[o] = radd(a.trp[o], rmul(a.dt, (double)e));
-      if (a.save_fluxes) {
-        a.fe[o] = fe;
-        a.fn[o] = fn;
-        a.ft[o] = ft;
-      }
-    }
-    if (a.save_fluxes) {
-      if (halo_n) a.fn[L.at(hi_n, j0 - 1, k)] = fn_s[b][0][lane];
-      if (halo_e) a.fe[L.at(i0 - 1, hj_e, k)] = fe_s[b][lane][0];
-    }
-  }
-}
-
-// Implicit solve of NRHS tracers sharing one matrix, one thread per column.
-// The system (diffusion.py:154-164) is an M-matrix that is diagonally
-// dominant by columns (|b_k| >= |a_{k+1}| + |c_{k-1}|), for which elimination
-// without interchanges is backward stable; the Thomas sweep in reciprocal form
-// keeps one division per level on the column's serial chain and none in the
-// back substitution. The matrix entries use the reference's divisions; the
-// factorisation is shared by the tracers. Shared memory holds c'_k and d'_k of
-// each tracer, [k][thread].
-template <typename F, int NRHS>
-__global__ void __launch_bounds__(64) implicit_kernel(DiffArgs<F> a, DiffArgs<F> b2, int ncols_x, int ncols) {
-  extern __shared__ double smem[];
-  const Layout &L = a.L;
-  const int Z = L.Z;
-  const int t = threadIdx.x, nb = blockDim.x;
-  double *dtdzw = smem;
-  double *cps = smem + Z;
-  double *dps = cps + (size_t)Z * nb;  // [r][k][thread]
-  for (int k = t; k < Z; k += nb) dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
-  __syncthreads();
-  const int col = blockIdx.x * nb + t;
-  if (col >= ncols) return;
-  const int i = 2 + col % ncols_x;
-  const int j = 2 + col / ncols_x;
-  const int ks = a.kbot[L.at2(i, j)] - 1;  // create_water_masks (utilities.py:38-48)
-  if (ks < 0 || ks >= Z) return;
-  const long long base = L.at2(i, j);
-  double *trp[2] = {a.trp, b2.trp};
-  F *dtr[2] = {a.dtr_iso, b2.dtr_iso};
-  const double inv_dt = 1.0 / a.dt;
-
-  // Loads run PF levels ahead of the serial chain (software pipelining): the
-  // chain itself only waits for FP64 latency, not for global memory.
-  constexpr int PF = 4;
-  double qK[PF], qT[PF][NRHS];
-#pragma unroll
-  for (int u = 0; u < PF; ++u) {
-    const int k = ks + u;
-    const long long o = base + (long long)min(k, Z - 1) * L.plane;
-    qK[u] = k < Z - 1 ? (double)ld(a.K33, o) : 0.0;
-#pragma unroll
-    for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? (double)trp[r][o] : 0.0;
-  }
-  double delta_prev = 0.0, cp = 0.0, dp[NRHS];
-#pragma unroll
-  for (int r = 0; r < NRHS; ++r) dp[r] = 0.0;
-  for (int k0 = ks; k0 < Z; k0 += PF) {
-#pragma unroll
-    for (int u = 0; u < PF; ++u) {
-      const int k = k0 + u;
-      if (k < Z) {
-        const double dzt = a.g.dzt[k];
-        const double delta = k < Z - 1 ? rmul(dtdzw[k], qK[u]) : 0.0;
-        double tr1[NRHS];
-#pragma unroll
-        for (int r = 0; r < NRHS; ++r) tr1[r] = qT[u][r];
-        // refill this slot with level k + PF
-        const int kn = k + PF;
-        if (kn < Z) {
-          const long long on = base + (long long)kn * L.plane;
-          qK[u] = kn < Z - 1 ? (double)ld(a.K33, on) : 0.0;
-#pragma unroll
-          for (int r = 0; r < NRHS; ++r) qT[u][r] = (double)trp[r][on];
-        }
-        const double ak = k == ks ? 0.0 : rdiv(-delta_prev, dzt);  // a_tri, zero at the edge (operators.py:72)
-        const double bk = k == ks ? radd(1.0, rdiv(delta, dzt)) : radd(1.0, rdiv(radd(delta, delta_prev), dzt));
-        const double ck = k < Z - 1 ? rdiv(-delta, dzt) : 0.0;
-        const double den = 1.0 / (bk - ak * cp);
-        cp = ck * den;
-        cps[(size_t)k * nb + t] = cp;
-#pragma unroll
-        for (int r = 0; r < NRHS; ++r) {
-          dp[r] = (tr1[r] - ak * dp[r]) * den;
-          dps[((size_t)r * Z + k) * nb + t] = dp[r];
-        }
-        delta_prev = delta;
-      }
-    }
-  }
-  double x[NRHS];
-#pragma unroll
-  for (int r = 0; r < NRHS; ++r) x[r] = 0.0;
-  const int nlev = Z - ks;
-  for (int m0 = 0; m0 < nlev; m0 += PF) {
-    // this group's old tracer values and partial tendencies, loaded together
-    double t1[PF][NRHS], d1[PF][NRHS];
-#pragma unroll
-    for (int u = 0; u < PF; ++u) {
-      const int k = Z - 1 - (m0 + u);
-      if (k >= ks) {
-        const long long o = base + (long long)k * L.plane;
-#pragma unroll
-        for (int r = 0; r < NRHS; ++r) {
-          t1[u][r] = (double)trp[r][o];
-          d1[u][r] = (double)dtr[r][o];
-        }
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < PF; ++u) {
-      const int k = Z - 1 - (m0 + u);
-      if (k >= ks) {
-        const long long o = base + (long long)k * L.plane;
-        const double c = cps[(size_t)k * nb + t];
-#pragma unroll
-        for (int r = 0; r < NRHS; ++r) {
-          x[r] = dps[((size_t)r * Z + k) * nb + t] - c * x[r];
-          trp[r][o] = x[r];
-          dtr[r][o] = F(d1[u][r] + (x[r] - t1[u][r]) * inv_dt);  // diffusion.py:204
-        }
-      }
-    }
-  }
-}
-
-// Scratch flux readers: zero outside the ranges the reference defines.
-template <typename F>
-__device__ __forceinline__ F fe_at(const DiffArgs<F> &a, int i, int j, int k) {
-  return (i >= 1 && i < a.L.X - 2 && j >= 2 && j < a.L.Y - 2) ? a.fe[a.L.at(i, j, k)] : F(0.0);
-}
-template <typename F>
-__device__ __forceinline__ F fn_at(const DiffArgs<F> &a, int i, int j, int k) {
-  return (i >= 2 && i < a.L.X - 2 && j >= 1 && j < a.L.Y - 2) ? a.fn[a.L.at(i, j, k)] : F(0.0);
-}
-
-// Dissipation at T points (veros/core/diffusion.py:9-36); zero on the outer ring.
-template <typename F>
-__device__ __forceinline__ F diss_at(const DiffArgs<F> &a, int i, int j, int k) {
-  const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
-  const F c = F(0.5 * a.grav / a.rho0);
-  const F I0 = ld(a.idr, o);
-  const F ex = (ld(a.idr, o + 1) - I0) * fe_at(a, i, j, k) + (I0 - ld(a.idr, o - 1)) * fe_at(a, i - 1, j, k);
-  const F ny =
-      (ld(a.idr, o + L.pitch) - I0) * fn_at(a, i, j, k) + (I0 - ld(a.idr, o - L.pitch)) * fn_at(a, i, j - 1, k);
-  const double cost = a.g.cost[j];
-  return c * ex / F(a.g.dxt[i] * cost) + c * ny / F(a.g.dyt[j] * cost);
-}
-
-template <typename F>
-__global__ void __launch_bounds__(128) energy_kernel(DiffArgs<F> a) {
-  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = 1 + blockIdx.y;
-  const int k = blockIdx.z;
-  const Layout &L = a.L;
-  if (i >= L.X - 1) return;
-  const int Z = L.Z;
-  const long long o = L.at(i, j, k);
-  const int ks = a.kbot[L.at2(i, j)] - 1;
-  const bool land = ks >= 0;  // "land_mask" of create_water_masks: column has water
-
-  // dissipation_on_wgrid (veros/core/diffusion.py:39-62)
-  const F d0 = diss_at(a, i, j, k);
-  F dw;
-  if (k < Z - 1) {
-    const F d1 = diss_at(a, i, j, k + 1);
-    const F edge = (land && k == ks) ? F(1.0) : F(0.0);
-    const F water = (land && k > ks) ? F(1.0) : F(0.0);
-    const F dzw_pad = F(a.g.dzw[k > 0 ? k - 1 : 0]);
-    dw = (F(0.5) * (d0 + d1) + F(0.5) * (d0 * dzw_pad / F(a.g.dzw[k]))) * edge + F(0.5) * (d0 + d1) * water;
-  } else {
-    dw = d0 * (land ? F(1.0) : F(0.0));
-  }
-  F P = a.P[o] + dw;
-
-  // vertical-mixing term (diffusion.py:254-279)
-  if (i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2 && k < Z - 1) {
-    const F mW = (__ldg(a.m + o) & VG_MASK_W) ? F(1.0) : F(0.0);
-    const F fxa = (-ld(a.idr, o + L.plane) + ld(a.idr, o)) / F(a.g.dzw[k]);
-    const F g = F(-a.grav / a.rho0) * fxa;
-    if (a.iso) {
-      const F dtrz = F(a.trp[o + L.plane] - a.trp[o]);
-      P = P + g * (a.ft[o] * mW + ld(a.K33, o) * dtrz / F(a.g.dzw[k]) * mW);
-    } else {
-      P = P + g * a.ft[o] * mW;
-    }
-  }
-  a.P[o] = P;
-}
-
-}  // namespace
-
-}  // namespace vg
+// Launchers and C entry points of the tracer diffusion kernels (diffusion_kernels.cuh).
+#include "diffusion_kernels.cuh"
 
 using namespace vg;
+using namespace vg::detail;
 
 extern "C" size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom) {
   if (!dom || dom->plane <= 0 || dom->Z <= 0) return 0;
@@ -414,62 +12,16 @@ extern "C" size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom) {
 namespace vg {
 namespace {
 
-// Validates one tracer's arguments and fills its DiffArgs.
-template <typename F, typename Ten, typename Tr>
-int make_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten, const F *K_field,
-              const uint8_t *mask_bits, const int32_t *kbot, const Tr *tr, int skew, F *scratch3, DiffArgs<F> &a) {
-  if (!grid_complete(grid) || !set || !ten || !K_field || !mask_bits || !kbot || !tr || !tr->tr_tau ||
-      !tr->tr_taup1 || !tr->dtracer_iso || !ten->K_11 || !ten->K_22 || !ten->K_33 || !ten->Ai_ez ||
-      !ten->Ai_nz || !ten->Ai_bx || !ten->Ai_by)
-    return fail(VG_ERR_ARG, "isoneutral diffusion: NULL pointer argument");
-  if (skew != 0 && skew != 1) return fail(VG_ERR_ARG, "skew must be 0 or 1");
-  if (set->enable_conserve_energy && (!tr->int_drhodX_tau || !tr->P_diss))
-    return fail(VG_ERR_ARG, "enable_conserve_energy needs int_drhodX_tau and P_diss");
-  if (!(set->dt_tracer != 0.0)) return fail(VG_ERR_ARG, "dt_tracer must be non-zero");
-  if (dom->Z > 512) return fail(VG_ERR_SHAPE, "Z=%d above the 512 levels supported", dom->Z);
-  a.L = layout_of(dom);
-  a.g = grid_of(grid);
-  a.dt = set->dt_tracer;
-  a.grav = set->grav;
-  a.rho0 = set->rho_0;
-  a.K = K_field;
-  a.s1 = skew ? -1.0 : 1.0;
-  a.s2 = 1.0;
-  a.K11 = ten->K_11;
-  a.K22 = ten->K_22;
-  a.K33 = ten->K_33;
-  a.Aez = ten->Ai_ez;
-  a.Anz = ten->Ai_nz;
-  a.Abx = ten->Ai_bx;
-  a.Aby = ten->Ai_by;
-  a.sp = ten->ai_stride_p;
-  a.sr = ten->ai_stride_r;
-  a.m = mask_bits;
-  a.kbot = kbot;
-  a.tr = tr->tr_tau;
-  a.trp = tr->tr_taup1;
-  a.dtr_iso = tr->dtracer_iso;
-  a.idr = tr->int_drhodX_tau;
-  a.P = tr->P_diss;
-  a.save_fluxes = set->enable_conserve_energy ? 1 : 0;
-  const size_t fsz = (size_t)a.L.plane * a.L.Z;
-  a.fe = scratch3;
-  a.fn = scratch3 ? scratch3 + fsz : nullptr;
-  a.ft = scratch3 ? scratch3 + 2 * fsz : nullptr;
-  a.iso = skew ? 0 : 1;
-  a.kchunk = 0;
-  return VG_OK;
-}
-
 template <typename F>
 int launch_flux_div(DiffArgs<F> &a, cudaStream_t s) {
+  constexpr int TY = 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
   int nchunks = 1;
   while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
   a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
   const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
   const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-  flux_div_kernel<F><<<dim3(nbx, nby, nbz), NT, smem, s>>>(a);
+  flux_div_kernel<F, TY><<<dim3(nbx, nby, nbz), TX * TY, smem, s>>>(a);
   return check_launch("flux_div_kernel");
 }
 
@@ -483,7 +35,7 @@ int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) 
         cudaFuncSetAttribute(implicit_kernel<F, NRHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
   }
-  implicit_kernel<F, NRHS><<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, b, ncols_x, ncols);
+  implicit_kernel<F, NRHS><<<(ncols + nb - 1) / nb, nb, smem, s>>>(a, b);
   return check_launch("implicit_kernel");
 }
 
@@ -506,7 +58,7 @@ int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *
   if (!scratch || scratch_bytes < need)
     return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, need);
   DiffArgs<F> a;
-  if ((st = make_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<F *>(scratch), a)))
+  if ((st = make_diff_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<F *>(scratch), a)))
     return st;
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div(a, s))) return st;
@@ -527,8 +79,8 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
     return fail(VG_ERR_SCRATCH, "scratch of %zu bytes given, %zu needed", scratch_bytes, 2 * one);
   DiffArgs<F> aT, aS;
   F *sc = static_cast<F *>(scratch);
-  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
-  if ((st = make_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
+  if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
+  if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
     return st;
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div(aT, s))) return st;

@@ -1,0 +1,383 @@
+// Isoneutral slopes and diffusion tensor (FP64), the work of
+// veros/core/isoneutral/isoneutral.py:18-229.
+//
+// On GB300 the FP64 pipe (about 1 TFLOP/s) bounds this kernel, not HBM, so
+// the design minimises FP64 instructions per cell:
+//
+// * 2.5-D tiling. A CTA owns a TX x TY tile of columns and walks k upward.
+//   For every T point of the tile plus a one-cell ring it computes, once per
+//   level, the quantities several faces share: drho/dT and drho/dS
+//   (isoneutral.py:40-41), the east/north face gradients of T and S
+//   (:64-95), and the reciprocals of the two clamped vertical density
+//   gradients min(0, drho/dz) - epsln that every slope divides by (:121, :158,
+//   :188, :207): one for the face below the point (kr = 0) and one above
+//   (kr = 1). Two planes (k and k+1) live in shared memory.
+// * Grid divisions become multiplications by reciprocals computed once per
+//   CTA; slope divisions become multiplications by the shared reciprocals.
+// * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
+//   Taylor polynomial on [-4, 2) (taper_table.inc, truncation error < 5e-17),
+//   the library tanh elsewhere, and an FP32 exp below x = -10 where the taper
+//   is below 2e-9 and the reference itself carries ~1e-16 absolute error.
+// * Faces whose mask is zero skip the slope work and store the zeros the
+//   reference's mask multiplication produces.
+//
+// Outputs are written only on the reference's sub-ranges (K_11[1:-2,2:-2],
+// K_22[2:-2,1:-2], K_33[2:-2,2:-2,:-1], K_33[...,-1] = 0, Ai_* likewise); all
+// other cells keep their contents.
+#pragma once
+
+#include "common.cuh"
+
+namespace vg {
+namespace detail {
+
+#include "taper_table.inc"
+
+
+constexpr double kEpsln = 1e-20;  // isoneutral.py:28
+enum { Q_RT, Q_RS, Q_TX, Q_SX, Q_TY, Q_SY, Q_R0, Q_R1, NQ };
+
+// Tile of TX = 32 (one warp along x) by TY columns; the point region adds a
+// one-cell ring. TY (the columns per CTA) is chosen by the autotuner.
+template <int TY_>
+struct Tile {
+  static constexpr int TX = 32, TY = TY_, NT = TX * TY;
+  static constexpr int PX = TX + 2, PY = TY + 2, NP = PX * PY;
+  static constexpr int kPtSlots = (NP + NT - 1) / NT;
+};
+
+// F is the type of the derived fields (K_iso in, K and Ai out) and of their
+// arithmetic: double for the FP64 drop-in, float for the split form. The
+// tracers stay FP64 in both: the vertical density gradient that every slope
+// divides by is a difference of nearby tracer values, and FP32 storage alone
+// would cost it ~1e-6 K of absolute accuracy.
+template <typename F>
+struct PreArgs {
+  Layout L;
+  Grid g;
+  int eos_type;
+  double slopec, inv_dslope, ksteep;
+  const double *__restrict__ T;
+  const double *__restrict__ S;
+  const F *__restrict__ K;
+  const uint8_t *__restrict__ m;
+  F *K11, *K22, *K33, *Aez, *Anz, *Abx, *Aby;
+  long long sp, sr;
+  int kchunk;
+};
+
+template <int TY>
+struct Smem {
+  static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
+  double q[2][NQ][NP];
+  double inv_dxu[PX], inv_dyu[PY], inv_cost[PY], facty[PY];
+  double qinv_dxt[PX], qinv_dyt_cost[PY], dxu[PX];
+  // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant
+};
+
+template <int TY>
+constexpr size_t pre_smem_bytes(int Z) {
+  return sizeof(Smem<TY>) + 4 * (size_t)Z * sizeof(double);
+}
+
+static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
+  const double x = (slopec - fabs(s)) * inv_dslope;
+  if (x >= kTaperX0 && x < kTaperX1) {
+    int idx = (int)((x - kTaperX0) * kTaperPerUnit);
+    idx = idx < kTaperN - 1 ? idx : kTaperN - 1;
+    const double b = x - (kTaperX0 + ((double)idx + 0.5) * (1.0 / kTaperPerUnit));
+    const double *c = kTaperCoef[idx];
+    double r = __ldg(c + 6);
+    r = fma(r, b, __ldg(c + 5));
+    r = fma(r, b, __ldg(c + 4));
+    r = fma(r, b, __ldg(c + 3));
+    r = fma(r, b, __ldg(c + 2));
+    r = fma(r, b, __ldg(c + 1));
+    return fma(r, b, __ldg(c + 0));
+  }
+  if (x < -10.0) return (double)expf(2.0f * (float)x);
+  return 0.5 * (1.0 + tanh(x));
+}
+
+// Split form: the slope and the taper argument are FP64; the taper itself, a
+// bounded smooth function, is evaluated in FP32.
+static __device__ __forceinline__ float taper_of_split(double s, double slopec, double inv_dslope) {
+  const float x = (float)((slopec - fabs(s)) * inv_dslope);
+  return 0.5f * (1.0f + tanhf(x));
+}
+
+template <typename F>
+__device__ __forceinline__ F taper_t(double s, double slopec, double inv_dslope);
+template <>
+__device__ __forceinline__ double taper_t<double>(double s, double slopec, double inv_dslope) {
+  return taper_of(s, slopec, inv_dslope);
+}
+template <>
+__device__ __forceinline__ float taper_t<float>(double s, double slopec, double inv_dslope) {
+  return taper_of_split(s, slopec, inv_dslope);
+}
+
+// taper * s^2 for the K_33 sums
+template <typename F>
+__device__ __forceinline__ F sq_term(F tp, F ai, double s);
+template <>
+__device__ __forceinline__ double sq_term<double>(double tp, double ai, double s) {
+  return tp * (s * s);
+}
+template <>
+__device__ __forceinline__ float sq_term<float>(float tp, float ai, double s) {
+  return ai * (float)s;
+}
+
+// One tile (bx, by) and k-chunk bz of one domain; the whole CTA takes part.
+template <typename F, int TY>
+__device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char *smem_raw, int bx, int by, int bz) {
+  using Sm = Smem<TY>;
+  constexpr int TX = Tile<TY>::TX, NT = Tile<TY>::NT, PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
+  constexpr int kPtSlots = Tile<TY>::kPtSlots;
+  Sm &sm = *reinterpret_cast<Sm *>(smem_raw);
+  double *zdzw = reinterpret_cast<double *>(smem_raw + sizeof(Sm));
+  const Layout &L = a.L;
+  const int Z = L.Z;
+  double *zinv_dzw = zdzw + Z;
+  double *zq_dzt = zinv_dzw + Z;
+  double *zeos = zq_dzt + Z;
+
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
+  const int kb = bz * a.kchunk;
+  const int ke = min(Z, kb + a.kchunk);
+
+  // ---- per-CTA grid tables ------------------------------------------------
+  for (int p = tid; p < PX; p += NT) {
+    const int i = min(max(i0 - 1 + p, 0), L.X - 1);
+    sm.inv_dxu[p] = 1.0 / a.g.dxu[i];
+    sm.qinv_dxt[p] = 1.0 / (4.0 * a.g.dxt[i]);
+    sm.dxu[p] = a.g.dxu[i];
+  }
+  for (int p = tid; p < PY; p += NT) {
+    const int j = min(max(j0 - 1 + p, 0), L.Y - 1);
+    sm.inv_dyu[p] = 1.0 / a.g.dyu[j];
+    sm.inv_cost[p] = 1.0 / a.g.cost[j];
+    sm.facty[p] = a.g.cosu[j] * a.g.dyu[j];  // isoneutral.py:202
+    sm.qinv_dyt_cost[p] = 1.0 / (4.0 * a.g.dyt[j] * a.g.cost[j]);
+  }
+  for (int k = tid; k < Z; k += NT) {
+    zdzw[k] = a.g.dzw[k];
+    zinv_dzw[k] = 1.0 / a.g.dzw[k];
+    zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
+    // eq type 3: drho/dT = -(betaTs*(T - theta0) + betaT*(1 - gammas*grav*zz*rho0))*rho0
+    const double zz = -fabs(a.g.zt[k]) - 0.0;
+    zeos[k] = Eos::betaT * (1.0 - Eos::gammas * Eos::grav * zz * Eos::rho0);
+  }
+
+  // K_33 on the top level is zero on the whole plane (isoneutral.py:225)
+  if (ke == Z) {
+    for (int p = tid; p < (PX + 1) * (PY + 1); p += NT) {
+      const int i = i0 - 1 + p % (PX + 1), j = j0 - 1 + p / (PX + 1);
+      if (i < L.X && j < L.Y) a.K33[L.at(i, j, Z - 1)] = 0.0;
+    }
+  }
+  __syncthreads();
+
+  // ---- per-point plane quantities ------------------------------------------
+  double carryT[kPtSlots], carryS[kPtSlots];  // dT/dz, dS/dz of the previous level per point slot
+#pragma unroll
+  for (int s = 0; s < kPtSlots; ++s) carryT[s] = carryS[s] = 0.0;
+
+  auto compute_plane = [&](int lev, int buf, bool store) {
+#pragma unroll
+    for (int s = 0; s < kPtSlots; ++s) {
+      const int p = tid + s * NT;
+      if (p >= NP) break;
+      const int pi = p % PX, pj = p / PX;
+      const int i = i0 - 1 + pi, j = j0 - 1 + pj;
+      F rT = 0, rS = 0;
+      double dTx = 0, dSx = 0, dTy = 0, dSy = 0, dTz = 0, dSz = 0;
+      if (i < L.X && j < L.Y) {
+        const long long o = L.at(i, j, lev);
+        const unsigned mk = __ldg(a.m + o);
+        const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
+        if (mk & VG_MASK_T) {
+          const F Tf = F(Tc);
+          if (a.eos_type == 1)
+            rT = F(-Eos::betaT * Eos::rho0);
+          else if (a.eos_type == 3)
+            rT = -(F(Eos::betaTs3) * (Tf - F(Eos::theta0)) + F(zeos[lev])) * F(Eos::rho0);
+          else
+            rT = -(F(Eos::betaT) + F(2.0 * Eos::betaTs24) * (Tf - F(Eos::theta0))) * F(Eos::rho0);
+          rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
+        }
+        if ((mk & VG_MASK_U) && i < L.X - 1) {
+          const double f = sm.inv_dxu[pi] * sm.inv_cost[pj];
+          dTx = (__ldg(a.T + o + 1) - Tc) * f;
+          dSx = (__ldg(a.S + o + 1) - Sc) * f;
+        }
+        if ((mk & VG_MASK_V) && j < L.Y - 1) {
+          dTy = (__ldg(a.T + o + L.pitch) - Tc) * sm.inv_dyu[pj];
+          dSy = (__ldg(a.S + o + L.pitch) - Sc) * sm.inv_dyu[pj];
+        }
+        if ((mk & VG_MASK_W) && lev < Z - 1) {
+          dTz = (__ldg(a.T + o + L.plane) - Tc) * zinv_dzw[lev];
+          dSz = (__ldg(a.S + o + L.plane) - Sc) * zinv_dzw[lev];
+        }
+      }
+      if (store) {
+        // vertical density gradients in FP64 (exact products of the split form's FP32 values)
+        const double G0 = (double)rT * carryT[s] + (double)rS * carryS[s];  // face below (kr = 0)
+        const double G1 = (double)rT * dTz + (double)rS * dSz;                   // face above (kr = 1)
+        double(*q)[NP] = sm.q[buf];
+        q[Q_RT][p] = rT;
+        q[Q_RS][p] = rS;
+        q[Q_TX][p] = dTx;
+        q[Q_SX][p] = dSx;
+        q[Q_TY][p] = dTy;
+        q[Q_SY][p] = dSy;
+        q[Q_R0][p] = 1.0 / (fmin(0.0, G0) - kEpsln);
+        q[Q_R1][p] = 1.0 / (fmin(0.0, G1) - kEpsln);
+      }
+      carryT[s] = dTz;
+      carryS[s] = dSz;
+    }
+  };
+
+  if (kb > 0) compute_plane(kb - 1, 0, false);  // only the carries
+  compute_plane(kb, kb & 1, true);
+
+  const int i = i0 + tx, j = j0 + ty;
+  const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
+  const bool east = i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  const bool north = i >= 2 && i < L.X - 2 && j < L.Y - 2;
+  const bool top = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
+
+  for (int k = kb; k < ke; ++k) {
+    if (k + 1 < Z) compute_plane(k + 1, (k + 1) & 1, true);
+    __syncthreads();
+    const double(*q)[NP] = sm.q[k & 1];
+    const double(*qn)[NP] = sm.q[(k + 1) & 1];
+    const long long o = L.at(i, j, k);
+    unsigned mk = 0;
+    if (east || north) mk = __ldg(a.m + o);
+
+    // east face: Ai_ez, K_11 (isoneutral.py:100-132)
+    if (east) {
+      F sumz = 0.0;
+      if (mk & VG_MASK_U) {
+        F diffloc;
+        if (k >= 1)
+          diffloc = F(0.25) * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + 1) +
+                               __ldg(a.K + o + 1 - L.plane));
+        else
+          diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + 1));
+        const double dTx = q[Q_TX][pc], dSx = q[Q_SX][pc];
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+#pragma unroll
+          for (int ip = 0; ip < 2; ++ip) {
+            const int pp = pc + ip;
+            const double s = -(q[Q_RT][pp] * dTx + q[Q_RS][pp] * dSx) * q[kr ? Q_R1 : Q_R0][pp];
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
+            a.Aez[o + ip * a.sp + kr * a.sr] = tp * F(s);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+          a.Aez[o + kr * a.sr] = 0.0;
+          a.Aez[o + a.sp + kr * a.sr] = 0.0;
+        }
+      }
+      a.K11[o] = sumz * F(zq_dzt[k]);
+    }
+
+    // north face: Ai_nz, K_22 (isoneutral.py:137-168)
+    if (north) {
+      F sumz = 0.0;
+      if (mk & VG_MASK_V) {
+        F diffloc;
+        if (k >= 1)
+          diffloc = F(0.25) * (__ldg(a.K + o) + __ldg(a.K + o - L.plane) + __ldg(a.K + o + L.pitch) +
+                               __ldg(a.K + o + L.pitch - L.plane));
+        else
+          diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
+        const double dTy = q[Q_TY][pc], dSy = q[Q_SY][pc];
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+#pragma unroll
+          for (int jp = 0; jp < 2; ++jp) {
+            const int pp = pc + jp * PX;
+            const double s = -(q[Q_RT][pp] * dTy + q[Q_RS][pp] * dSy) * q[kr ? Q_R1 : Q_R0][pp];
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
+            a.Anz[o + jp * a.sp + kr * a.sr] = tp * F(s);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          if (kr == 0 && k == 0) continue;
+          a.Anz[o + kr * a.sr] = 0.0;
+          a.Anz[o + a.sp + kr * a.sr] = 0.0;
+        }
+      }
+      a.K22[o] = sumz * F(zq_dzt[k]);
+    }
+
+    // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224)
+    if (top && k < Z - 1) {
+      F sumx = 0.0, sumy = 0.0;
+      if (mk & VG_MASK_W) {
+        const F Kc = __ldg(a.K + o);
+#pragma unroll
+        for (int kr = 0; kr < 2; ++kr) {
+          const double(*qq)[NP] = kr ? qn : q;
+          const double rT = qq[Q_RT][pc], rS = qq[Q_RS][pc];
+          const double Rz = kr ? qn[Q_R0][pc] : q[Q_R1][pc];
+#pragma unroll
+          for (int ip = 0; ip < 2; ++ip) {
+            const int pp = pc - 1 + ip;
+            const double s = -(rT * qq[Q_TX][pp] + rS * qq[Q_SX][pp]) * Rz;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            const F ai = tp * F(s);
+            // FP64: dxu*K*taper*s^2 in the reference's order; split: (taper*s)*s, which stays
+            // finite where an FP32 s^2 would overflow under a vanishing taper
+            sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(tp, ai, s);
+            a.Abx[o + ip * a.sp + kr * a.sr] = ai;
+          }
+#pragma unroll
+          for (int jp = 0; jp < 2; ++jp) {
+            const int pp = pc - PX + jp * PX;
+            const double s = -(rT * qq[Q_TY][pp] + rS * qq[Q_SY][pp]) * Rz;
+            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
+            const F ai = tp * F(s);
+            sumy += F(sm.facty[ty + jp]) * Kc * sq_term<F>(tp, ai, s);
+            a.Aby[o + jp * a.sp + kr * a.sr] = ai;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const long long oc = o + (c >> 1) * a.sp + (c & 1) * a.sr;
+          a.Abx[oc] = 0.0;
+          a.Aby[oc] = 0.0;
+        }
+      }
+      a.K33[o] = sumx * F(sm.qinv_dxt[tx + 1]) + sumy * F(sm.qinv_dyt_cost[ty + 1]);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename F, int TY>
+__global__ void __launch_bounds__(32 * TY, 2) pre_tile_kernel(PreArgs<F> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  pre_tile_body<F, TY>(a, smem_raw, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+}  // namespace detail
+}  // namespace vg
