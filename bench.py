@@ -183,6 +183,55 @@ def run_reference(args):
     return 0
 
 
+def run_ensemble(device, steps=20):
+    """48 members of uneven extents: looping the single-domain step versus the
+    batched persistent launches replayed from a CUDA graph of ``steps`` steps,
+    in FP64 and in the split form. Returns the report dict."""
+    import torch
+
+    from veros_gb300 import synthetic
+    from veros_gb300.ensemble import Ensemble
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    hosts = synthetic.ensemble_states(48)
+    cells = sum(h.nx * h.ny * h.nz for h in hosts)
+    out = {"members": len(hosts), "cells": cells, "graph_steps": steps}
+    for precision in ("f64", "f32split"):
+        states = [DeviceState.from_host(h, device=device, precision=precision) for h in hosts]
+        steppers = [IsoneutralStepper(st) for st in states]
+        for st in steppers:
+            st.step(1)
+        torch.cuda.synchronize()
+        nloop = 3
+        t0 = time.perf_counter()
+        for _ in range(nloop):
+            for st in steppers:
+                st.step(1)
+        torch.cuda.synchronize()
+        loop_value = cells * nloop / (time.perf_counter() - t0)
+        ens = Ensemble(states)
+        tuning, timings = ens.autotune(steps=1)
+        ens.replay(steps)  # records the graph for this phase and warms it
+        ens.capture(steps)  # records the graph for the phase the timed replay starts from
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        ens.replay(steps)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out[precision] = {"batched_graph_cells_per_s": cells * steps / (ms / 1e3),
+                          "ms_per_step": ms / steps,
+                          "looped_single_domain_cells_per_s": loop_value,
+                          "speedup_vs_loop": cells * steps / (ms / 1e3) / loop_value,
+                          "tuning": tuning, "candidates_timed": len(timings)}
+        ens.close()
+        del ens, steppers, states
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -273,6 +322,12 @@ def run_gb300(args):
         e2e_s = float(t.item())
     e2e_value = world * cells * e2e_steps / e2e_s
 
+    launches = args.steps * stepper.launches_per_step()
+    ensemble = None
+    if not args.no_ensemble:
+        del dev, stepper
+        torch.cuda.empty_cache()
+        ensemble = run_ensemble(device)
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -306,7 +361,8 @@ def run_gb300(args):
                      "tracer_rel_maxnorm_err_vs_f64": split_err,
                      "precision": "FP64 tracers, gradients, slope denominators/slopes and implicit solve; "
                                   "FP32 tensors, fluxes, taper, tendencies"},
-        "gpu_launches": args.steps * stepper.launches_per_step(),
+        "gpu_launches": launches,
+        "ensemble": ensemble,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))
@@ -321,6 +377,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the 48-member batched-ensemble measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -199,7 +199,7 @@ def eos_int_drhodS(eq_type, p):
 
 def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_origin=-60.0,
                dz_top=10.0, dz_bottom=400.0, land_fraction=0.15, eq_of_state_type=1,
-               k_iso_lognormal_sigma=None, settings=None, stable_caps=False):
+               k_iso_lognormal_sigma=None, settings=None, stable_caps=False, lean=False):
     """Build one seeded synthetic state.
 
     * ``kbot``: each interior column is land with probability ``land_fraction``,
@@ -213,6 +213,8 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
       ``dx = dxt cos(lat)``, are land (the polar caps of a global grid, where
       cos(lat) -> 0; the reference's own 1-degree setup stops at 79S/81N,
       veros/setups/global_1deg/global_1deg.py:29-36).
+    * ``lean``: leave out the all-zero output fields and ``int_drhodT/S``
+      (a device state allocates its outputs itself); for large ensembles.
     """
     rng = np.random.default_rng(seed)
     X, Y, Z = nx + 4, ny + 4, nz
@@ -247,6 +249,13 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
         K_iso = s["K_iso_0"] * np.exp(rng.normal(0.0, k_iso_lognormal_sigma, size=(X, Y, Z)))
     K_gm = np.full((X, Y, Z), s["K_gm_0"])
 
+    meta = dict(seed=seed, land_fraction_realised=float(1.0 - (kbot[2:-2, 2:-2] > 0).mean()))
+    if lean:
+        arrays = dict(grid)
+        arrays.update(kbot=kbot, maskT=maskT, maskU=maskU, maskV=maskV, maskW=maskW, temp=temp, salt=salt,
+                      K_iso=K_iso, K_gm=K_gm)
+        return HostState(nx, ny, nz, s, arrays, meta=meta)
+
     p = np.abs(zt)[None, None, :, None]
     int_drhodT = eos_int_drhodT(s["eq_of_state_type"], temp, p) * np.ones_like(temp)
     int_drhodS = eos_int_drhodS(s["eq_of_state_type"], p) * np.ones_like(salt)
@@ -262,7 +271,6 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
         Ai_bx=np.zeros((X, Y, Z, 2, 2)), Ai_by=np.zeros((X, Y, Z, 2, 2)),
         dtemp_iso=z3(), dsalt_iso=z3(), P_diss_iso=z3(), P_diss_skew=z3(),
     )
-    meta = dict(seed=seed, land_fraction_realised=float(1.0 - (kbot[2:-2, 2:-2] > 0).mean()))
     return HostState(nx, ny, nz, s, arrays, meta=meta)
 
 
@@ -285,3 +293,19 @@ def global_quarter_deg_state(seed=0):
     """1440 x 720 x 60 at 0.25 degree, -90..90, dz 10-250 m, ~30% land plus polar caps beyond 62 deg, nonlinear EOS."""
     return make_state(1440, 720, 60, seed=seed, dx_deg=0.25, dy_deg=0.25, y_origin=-90.0, dz_top=10.0,
                       dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3, stable_caps=True)
+
+
+def ensemble_states(n=48, seed0=0, lean=True):
+    """Ensemble members: nx ~ U{32..512}, ny ~ U{32..256}, nz from {15, 30, 45, 60},
+    each with its own seed; kbot and tracers as in the small linear state
+    (1 degree in x from 60S, dy = min(1, 120/ny) degrees, linear EOS)."""
+    rng = np.random.default_rng(1234 + seed0)
+    members = []
+    for m in range(n):
+        nx = int(rng.integers(32, 513))
+        ny = int(rng.integers(32, 257))
+        nz = int(rng.choice([15, 30, 45, 60]))
+        dy = min(1.0, 120.0 / ny)  # every member stays within 60S..60N
+        members.append(make_state(nx, ny, nz, seed=seed0 + m, dy_deg=dy, y_origin=-60.0, dz_top=10.0,
+                                  dz_bottom=400.0, land_fraction=0.15, eq_of_state_type=1, lean=lean))
+    return members
