@@ -230,6 +230,24 @@ int vg_isoneutral_step_prepare_f32split(const VgDomain *dom, const VgStepFieldsF
  * tendencies), for callers that time or interleave the stages. */
 int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, void *stream);
 
+/* Replaces veros.core.thermodynamics.vertmix_tempsalt
+ * (veros/core/thermodynamics.py:248-300): implicit vertical mixing of temp and
+ * salt at level taup1 with the diffusivity kappaH and the surface forcing
+ * forc_temp_surface / forc_salt_surface ((X, Y) planes, canonical pitch);
+ * writes the new levels and dtemp_vmix / dsalt_vmix on the whole array.
+ * Single process, non-cyclic (the closing boundary exchange is a no-op). */
+int vg_vertmix_tempsalt_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                            const double *kappaH, const int32_t *kbot, double *temp_taup1, double *salt_taup1,
+                            const double *forc_temp_surface, const double *forc_salt_surface,
+                            double *dtemp_vmix, double *dsalt_vmix, void *stream);
+
+/* Replaces isoneutral_diag_streamfunction_kernel
+ * (veros/core/isoneutral/isoneutral.py:232-254): B1_gm[2:-2,1:-2] and
+ * B2_gm[1:-2,2:-2] from K_gm and Ai_nz / Ai_ez; other cells untouched. */
+int vg_isoneutral_streamfunction_f64(const VgDomain *dom, const double *K_gm, const double *Ai_ez,
+                                     const double *Ai_nz, long long ai_stride_p, long long ai_stride_r,
+                                     double *B1_gm, double *B2_gm, void *stream);
+
 /* ---- Batched ensemble ------------------------------------------------------
  * One isoneutral step of many domains (uneven extents and kbot) with one
  * persistent launch per stage. No reference counterpart: Veros steps one

@@ -21,10 +21,14 @@ trailing ``(ip|jp, kr)`` pair), the Veros NumPy-backend algorithm for:
 * ``pad_z_edges / create_water_masks / solve_implicit``
                                     veros/core/utilities.py:24-59
 * ``solve_tridiagonal_numpy``       veros/core/operators.py:60-77
+* ``vertmix_tempsalt``              veros/core/thermodynamics.py:248-300
+* ``isoneutral_diag_streamfunction_kernel``
+                                    veros/core/isoneutral/isoneutral.py:232-254
 
-The tridiagonal solve calls LAPACK ``dgtsv`` through ``scipy.linalg.lapack``
-exactly as the reference does (same concatenation of the wet cells with the
-column couplings cut).
+The tridiagonal solve is LAPACK ``dgtsv`` (the routine the reference calls
+through ``scipy.linalg.lapack``), restated column-parallel in ``dgtsv_columns``
+for masks of the ``create_water_masks`` form and called through SciPy for any
+other form, as the reference does.
 
 Pinning: ``tests/golden/make_golden.py`` runs the reference NumPy backend on
 seeded states and stores inputs and outputs; ``tests/test_oracle_golden.py``
@@ -525,3 +529,56 @@ def isoneutral_step(vs, settings):
     vs.__dict__.update(isoneutral_diffusion(vs, settings, True))
     vs.__dict__.update(isoneutral_diffusion(vs, settings, False))
     vs.taum1, vs.tau, vs.taup1 = vs.tau, vs.taup1, vs.taum1
+
+
+def vertmix_tempsalt(vs, settings):
+    """``vertmix_tempsalt`` (veros/core/thermodynamics.py:248-300), non-cyclic,
+    single process (the closing boundary exchange is then a no-op).
+
+    Returns a dict with ``temp``, ``salt``, ``dtemp_vmix``, ``dsalt_vmix``.
+    """
+    dt = _settings_get(settings, "dt_tracer")
+    nz = vs.dzt.shape[0]
+    tp1 = vs.taup1
+    dtemp_vmix = vs.temp[:, :, :, tp1].copy()
+    dsalt_vmix = vs.salt[:, :, :, tp1].copy()
+    shape = vs.kappaH[2:-2, 2:-2].shape
+    a_tri = np.zeros(shape)
+    b_tri = np.zeros(shape)
+    c_tri = np.zeros(shape)
+    delta = np.zeros(shape)
+    _, water_mask, edge_mask = create_water_masks(vs.kbot[2:-2, 2:-2], nz)
+    delta[:, :, :-1] = dt / vs.dzw[None, None, :-1] * vs.kappaH[2:-2, 2:-2, :-1]
+    delta[:, :, -1] = 0.0
+    a_tri[:, :, 1:] = -delta[:, :, :-1] / vs.dzt[None, None, 1:]
+    b_tri[:, :, 1:] = 1 + (delta[:, :, 1:] + delta[:, :, :-1]) / vs.dzt[None, None, 1:]
+    b_tri_edge = 1 + delta / vs.dzt[None, None, :]
+    c_tri[:, :, :-1] = -delta[:, :, :-1] / vs.dzt[None, None, :-1]
+    temp = vs.temp.copy()
+    salt = vs.salt.copy()
+    for tr, forc in ((temp, vs.forc_temp_surface), (salt, vs.forc_salt_surface)):
+        d_tri = tr[2:-2, 2:-2, :, tp1].copy()
+        d_tri[:, :, -1] += dt * forc[2:-2, 2:-2] / vs.dzt[-1]
+        sol = solve_implicit(a_tri, b_tri, c_tri, d_tri, water_mask, edge_mask, b_edge=b_tri_edge)
+        tr[2:-2, 2:-2, :, tp1] = np.where(water_mask, sol, tr[2:-2, 2:-2, :, tp1])
+    dtemp_vmix = (temp[:, :, :, tp1] - dtemp_vmix) / dt
+    dsalt_vmix = (salt[:, :, :, tp1] - dsalt_vmix) / dt
+    return dict(temp=temp, salt=salt, dtemp_vmix=dtemp_vmix, dsalt_vmix=dsalt_vmix)
+
+
+def isoneutral_diag_streamfunction(vs):
+    """``isoneutral_diag_streamfunction_kernel`` (veros/core/isoneutral/isoneutral.py:232-254).
+
+    Returns a dict with ``B1_gm`` and ``B2_gm``; cells outside the written
+    ranges keep the values of ``vs``.
+    """
+    K_gm_pad = pad_z_edges(vs.K_gm)
+    B1 = vs.B1_gm.copy()
+    B2 = vs.B2_gm.copy()
+    diffloc = 0.25 * (K_gm_pad[1:-2, 2:-2, 1:-1] + K_gm_pad[1:-2, 2:-2, :-2]
+                      + K_gm_pad[2:-1, 2:-2, 1:-1] + K_gm_pad[2:-1, 2:-2, :-2])
+    B2[1:-2, 2:-2, :] = 0.25 * diffloc * np.sum(vs.Ai_ez[1:-2, 2:-2, ...], axis=(3, 4))
+    diffloc = 0.25 * (K_gm_pad[2:-2, 1:-2, 1:-1] + K_gm_pad[2:-2, 1:-2, :-2]
+                      + K_gm_pad[2:-2, 2:-1, 1:-1] + K_gm_pad[2:-2, 2:-1, :-2])
+    B1[2:-2, 1:-2, :] = -0.25 * diffloc * np.sum(vs.Ai_nz[2:-2, 1:-2, ...], axis=(3, 4))
+    return dict(B1_gm=B1, B2_gm=B2)

@@ -22,6 +22,9 @@ Cases (all float64, reference layout):
   (test/pyom_consistency/tridiag_test.py:40-67) at a small size.
 * ``grid_topo``: reference ``numerics.calc_grid`` / ``calc_topo`` outputs for the
   spacings and ``kbot`` the synthetic builder uses.
+* ``vertmix_random``: ``vertmix_tempsalt`` (veros/core/thermodynamics.py:248-300)
+  and ``isoneutral_diag_streamfunction_kernel`` (veros/core/isoneutral/isoneutral.py:232-254)
+  on the random-state fixture, with a non-negative vertical diffusivity.
 """
 
 import os
@@ -141,6 +144,34 @@ def make_synth_case(seed, eq_type, conserve_energy, sigma):
     return blob
 
 
+def make_vertmix_case(nx, ny, nz, seed):
+    """vertmix_tempsalt and isoneutral_diag_streamfunction on the reference's random state."""
+    from veros.core.isoneutral.isoneutral import isoneutral_diag_streamfunction_kernel
+    from veros.core.thermodynamics import vertmix_tempsalt
+    from veros.pyom_compat import get_random_state
+
+    np.random.seed(seed)
+    settings = dict(nx=nx, ny=ny, nz=nz, dt_tracer=3600, dt_mom=3600, enable_neutral_diffusion=True,
+                    enable_skew_diffusion=True)
+    state = get_random_state(extra_settings=settings)
+    vs = state.variables
+    # a physical (non-negative) vertical diffusivity, as the TKE/IDEMIX closures produce
+    vs.kappaH = np.abs(np.asarray(vs.kappaH)) * 1e-2
+    names = ("dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt", "kbot", "maskT", "maskU", "maskV",
+             "maskW", "temp", "salt", "kappaH", "forc_temp_surface", "forc_salt_surface", "dtemp_vmix",
+             "dsalt_vmix", "K_gm", "Ai_ez", "Ai_nz", "B1_gm", "B2_gm")
+    blob = {f"in_{k}": v for k, v in _snapshot(vs, names).items()}
+    blob.update(_settings_blob(state.settings))
+    blob.update(tau=np.array(vs.tau), taup1=np.array(vs.taup1), taum1=np.array(vs.taum1))
+    out = vertmix_tempsalt(state)
+    for k in ("temp", "salt", "dtemp_vmix", "dsalt_vmix"):
+        blob[f"vmix_{k}"] = np.array(getattr(out, k)).copy()
+    out = isoneutral_diag_streamfunction_kernel(state)
+    blob["sf_B1_gm"] = np.array(out.B1_gm).copy()
+    blob["sf_B2_gm"] = np.array(out.B2_gm).copy()
+    return blob
+
+
 def make_tridiag_case():
     from veros.core.operators import solve_tridiagonal_numpy
     from veros.core.utilities import create_water_masks, solve_implicit
@@ -202,6 +233,7 @@ def main():
         "iso_synth_eq1": make_synth_case(0, 1, False, None),
         "iso_synth_eq3": make_synth_case(1, 3, True, 0.3),
         "tridiag": make_tridiag_case(),
+        "vertmix_random": make_vertmix_case(12, 10, 9, 17),
         "grid_topo": make_grid_case(),
     }
     for name, blob in cases.items():

@@ -310,3 +310,50 @@ def test_host_buffer_step_matches_device_step():
     v = a.variables
     assert np.array_equal(outs[0].numpy(), a.download("temp")[..., v.tau])
     assert np.array_equal(outs[3].numpy(), a.download("dsalt_iso"))
+
+
+def test_vertmix_and_streamfunction_vs_reference_golden():
+    """vertmix_tempsalt and the GM streamfunction diagnostics against the reference's outputs."""
+    from veros_gb300.isoneutral import isoneutral_diag_streamfunction_kernel
+    from veros_gb300.thermodynamics import vertmix_tempsalt
+
+    g = load_golden("vertmix_random")
+    dev = _golden_device_state(g)
+    for n in ("kappaH", "forc_temp_surface", "forc_salt_surface", "dtemp_vmix", "dsalt_vmix", "B1_gm", "B2_gm"):
+        dev.upload(n, g[f"in_{n}"])
+    out = vertmix_tempsalt(dev)
+    assert out._fields == ("dtemp_vmix", "temp", "dsalt_vmix", "salt")
+    torch.cuda.synchronize()
+    dt = float(g["setting_dt_tracer"])
+    for n, tr in (("temp", None), ("salt", None), ("dtemp_vmix", "temp"), ("dsalt_vmix", "salt")):
+        name = {"dtemp_vmix": "dtemp_iso", "dsalt_vmix": "dsalt_iso"}.get(n, n)  # same differencing floor
+        assert_field_close(name, dev.download(n), g[f"vmix_{n}"], tracer=None if tr is None else g[f"vmix_{tr}"],
+                           dt=dt)
+    out = isoneutral_diag_streamfunction_kernel(dev)
+    torch.cuda.synchronize()
+    for n in ("B1_gm", "B2_gm"):
+        got, ref = dev.download(n), g[f"sf_{n}"]
+        assert _rel(got, ref) <= TOL, n
+    # untouched cells keep their contents
+    before = g["in_B2_gm"]
+    w = np.zeros(before.shape, dtype=bool)
+    w[1:-2, 2:-2] = True
+    assert np.array_equal(dev.download("B2_gm")[~w], before[~w])
+
+
+def test_vertmix_on_synthetic_state_vs_oracle():
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.thermodynamics import vertmix_tempsalt
+
+    host = synthetic.make_state(70, 50, 30, seed=8, eq_of_state_type=3, dz_bottom=250.0)
+    dev = DeviceState.from_host(host)
+    vertmix_tempsalt(dev)
+    torch.cuda.synchronize()
+    vs = orc.OracleState({k: v.copy() for k, v in host.arrays.items()})
+    out = orc.vertmix_tempsalt(vs, host.settings)
+    dt = host.settings["dt_tracer"]
+    for n, tr in (("temp", None), ("salt", None), ("dtemp_vmix", "temp"), ("dsalt_vmix", "salt")):
+        name = {"dtemp_vmix": "dtemp_iso", "dsalt_vmix": "dsalt_iso"}.get(n, n)
+        assert_field_close(name, dev.download(n), out[n], tracer=None if tr is None else out[tr], dt=dt)

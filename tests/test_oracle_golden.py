@@ -63,3 +63,14 @@ def test_water_masks_match_reference_semantics():
     _, wm, em = orc.create_water_masks(g["kbot"], g["a"].shape[-1])
     assert np.array_equal(wm, g["water_mask"])
     assert np.array_equal(em, g["edge_mask"])
+
+
+def test_vertmix_and_streamfunction_match_reference():
+    g = load_golden("vertmix_random")
+    vs, s = _state_and_settings(g)
+    out = orc.vertmix_tempsalt(vs, s)
+    for k in ("temp", "salt", "dtemp_vmix", "dsalt_vmix"):
+        assert np.array_equal(out[k], g[f"vmix_{k}"]), k
+    out = orc.isoneutral_diag_streamfunction(vs)
+    for k in ("B1_gm", "B2_gm"):
+        _close(out[k], g[f"sf_{k}"], k)

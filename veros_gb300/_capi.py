@@ -137,6 +137,11 @@ SIGNATURES = {
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_isoneutral_step_prepare_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgStepFields),
                                                       ctypes.c_void_p]),
+    "vg_vertmix_tempsalt_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                               ctypes.POINTER(VgIsoSettings)] + [ctypes.c_void_p] * 9),
+    "vg_isoneutral_streamfunction_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_void_p, ctypes.c_void_p,
+                                                        ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
+                                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "vg_ensemble_create_f64": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMember), ctypes.c_int,
                                               ctypes.POINTER(VgEnsembleTuning), ctypes.POINTER(ctypes.c_void_p)]),
     "vg_ensemble_create_f32split": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMemberF32), ctypes.c_int,

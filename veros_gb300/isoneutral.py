@@ -137,3 +137,39 @@ def isoneutral_diffusion(state, tr, istemp):
 def isoneutral_skew_diffusion(state, tr, istemp):
     """Skew (GM) diffusion of ``tr``; mutates the state."""
     return _diffusion_entry(state, tr, istemp, skew=True)
+
+
+def isoneutral_diag_streamfunction_kernel(state):
+    """GM streamfunction diagnostics (veros/core/isoneutral/isoneutral.py:232-254):
+    ``KernelOutput(B1_gm, B2_gm)``."""
+    if not _is_device_state(state):
+        dev = DeviceState.from_host(state, fields=("K_gm", "Ai_ez", "Ai_nz", "B1_gm", "B2_gm"))
+        _run_streamfunction(dev)
+        return KernelOutput(B1_gm=dev.download("B1_gm"), B2_gm=dev.download("B2_gm"))
+    _run_streamfunction(state)
+    v = state.variables
+    return KernelOutput(B1_gm=v.B1_gm, B2_gm=v.B2_gm)
+
+
+def _run_streamfunction(dev):
+    v = dev.variables
+    dev.check_layout(("B1_gm", "B2_gm"))
+    if v.K_gm.dtype != torch.float64 or v.Ai_ez.dtype != torch.float64:
+        raise ValueError("the streamfunction diagnostics run on float64 fields")
+    ai = v.Ai_ez
+    lib = _capi.load()
+    st = lib.vg_isoneutral_streamfunction_f64(dev.domain(), v.K_gm.data_ptr(), v.Ai_ez.data_ptr(), v.Ai_nz.data_ptr(),
+                                              ai.stride(3), ai.stride(4), v.B1_gm.data_ptr(), v.B2_gm.data_ptr(),
+                                              _stream(dev))
+    _capi.check(st, "isoneutral_diag_streamfunction")
+
+
+def isoneutral_diag_streamfunction(state):
+    """Routine form (veros/core/isoneutral/isoneutral.py:257-269): runs only with
+    neutral and skew diffusion enabled; mutates the state, returns None."""
+    s = state.settings
+    if not (getattr(s, "enable_neutral_diffusion", False) and getattr(s, "enable_skew_diffusion", False)):
+        return None
+    out = isoneutral_diag_streamfunction_kernel(state)
+    state.variables.update(out)
+    return None

@@ -11,6 +11,7 @@ reload Veros must install inside the test.
 """
 
 from . import isoneutral as _iso
+from . import thermodynamics as _thermo
 from . import utilities as _util
 
 _TARGETS = (
@@ -20,6 +21,11 @@ _TARGETS = (
     ("veros.core.isoneutral.isoneutral", "isoneutral_diffusion_pre", _iso.isoneutral_diffusion_pre),
     ("veros.core.isoneutral.diffusion", "isoneutral_diffusion", _iso.isoneutral_diffusion),
     ("veros.core.isoneutral.diffusion", "isoneutral_skew_diffusion", _iso.isoneutral_skew_diffusion),
+    ("veros.core.isoneutral", "isoneutral_diag_streamfunction", _iso.isoneutral_diag_streamfunction),
+    ("veros.core.isoneutral.isoneutral", "isoneutral_diag_streamfunction", _iso.isoneutral_diag_streamfunction),
+    ("veros.core.isoneutral.isoneutral", "isoneutral_diag_streamfunction_kernel",
+     _iso.isoneutral_diag_streamfunction_kernel),
+    ("veros.core.thermodynamics", "vertmix_tempsalt", _thermo.vertmix_tempsalt),
     ("veros.core.utilities", "solve_implicit", _util.solve_implicit),
     ("veros.core.utilities", "solve_tridiagonal", _util.solve_tridiagonal),
     ("veros.core.operators", "solve_tridiagonal", _util.solve_tridiagonal),

@@ -21,6 +21,9 @@ from . import _capi
 PITCH_ALIGN = 16
 
 FIELDS_3D = ("K_iso", "K_gm", "K_11", "K_22", "K_33", "dtemp_iso", "dsalt_iso", "P_diss_iso", "P_diss_skew")
+# fields of the neighbouring routines (vertical mixing, streamfunction diagnostics): always float64
+FIELDS_3D_F64 = ("kappaH", "dtemp_vmix", "dsalt_vmix", "B1_gm", "B2_gm")
+FIELDS_2D = ("forc_temp_surface", "forc_salt_surface")
 FIELDS_TIME = ("temp", "salt", "int_drhodT", "int_drhodS")
 FIELDS_TENSOR = ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by")
 FIELDS_MASK = ("maskT", "maskU", "maskV", "maskW")
@@ -176,6 +179,12 @@ class DeviceState:
             setattr(v, n, canonical_zeros(X, Y, Z, (3,), dtype=dt_, device=dev))
         for n in FIELDS_TENSOR:
             setattr(v, n, canonical_zeros(X, Y, Z, (2, 2), dtype=fd, device=dev))
+        for n in FIELDS_3D_F64:
+            setattr(v, n, canonical_zeros(X, Y, Z, dtype=torch.float64, device=dev))
+        for n in FIELDS_2D:
+            t2 = canonical_empty_2d(X, Y, dtype=torch.float64, device=dev)
+            t2.zero_()
+            setattr(v, n, t2)
         for n in FIELDS_MASK:
             setattr(v, n, canonical_zeros(X, Y, Z, dtype=torch.bool, device=dev))
         kb = canonical_empty_2d(X, Y, device=dev)
@@ -259,7 +268,7 @@ class DeviceState:
         ai = v.Ai_ez
         for n in FIELDS_TENSOR + ("K_11", "K_22", "K_33"):
             t = getattr(v, n)
-            want = torch.float64 if n in ("temp", "salt") else self.fdtype
+            want = torch.float64 if n in ("temp", "salt") + FIELDS_3D_F64 else self.fdtype
             if t.dtype != want:
                 raise ValueError(f"{n}: dtype {t.dtype} but the state's precision needs {want}")
             if n in FIELDS_TENSOR and t.stride()[3:] != ai.stride()[3:]:
@@ -275,7 +284,7 @@ class DeviceState:
             t = getattr(v, n)
             if not t.is_cuda or t.device != self.device:
                 raise ValueError(f"{n} is not on {self.device}")
-            want = torch.float64 if n in ("temp", "salt") else self.fdtype
+            want = torch.float64 if n in ("temp", "salt") + FIELDS_3D_F64 else self.fdtype
             if t.dtype != want:
                 raise ValueError(f"{n}: dtype {t.dtype} but the state's precision needs {want}")
             if not is_canonical(t, self.X, self.Y, self.Z) or t.stride(1) != self.pitch:

@@ -261,6 +261,11 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
     int_drhodS = eos_int_drhodS(s["eq_of_state_type"], p) * np.ones_like(salt)
 
     z3 = lambda: np.zeros((X, Y, Z))  # noqa: E731
+    # inputs of the neighbouring vertical mixing: a vertical diffusivity of
+    # 1e-4..1e-3 m^2/s on W points and small surface fluxes
+    kappaH = 1e-4 * (1.0 + 9.0 * rng.random((X, Y, Z))) * maskW
+    forc_temp_surface = 1e-5 * rng.standard_normal((X, Y))
+    forc_salt_surface = 1e-6 * rng.standard_normal((X, Y))
     arrays = dict(grid)
     arrays.update(
         kbot=kbot, maskT=maskT, maskU=maskU, maskV=maskV, maskW=maskW,
@@ -270,6 +275,8 @@ def make_state(nx, ny, nz, *, seed=0, dx_deg=1.0, dy_deg=1.0, x_origin=0.0, y_or
         Ai_ez=np.zeros((X, Y, Z, 2, 2)), Ai_nz=np.zeros((X, Y, Z, 2, 2)),
         Ai_bx=np.zeros((X, Y, Z, 2, 2)), Ai_by=np.zeros((X, Y, Z, 2, 2)),
         dtemp_iso=z3(), dsalt_iso=z3(), P_diss_iso=z3(), P_diss_skew=z3(),
+        kappaH=kappaH, forc_temp_surface=forc_temp_surface, forc_salt_surface=forc_salt_surface,
+        dtemp_vmix=z3(), dsalt_vmix=z3(), B1_gm=z3(), B2_gm=z3(),
     )
     return HostState(nx, ny, nz, s, arrays, meta=meta)
 
