@@ -262,6 +262,62 @@ def run_ensemble(device, steps=20):
     return out
 
 
+def run_adjoint(device, reps=5):
+    """Adjoint of an 8-step FP64 rollout at 360 x 180 x 30 (nonlinear EOS,
+    lognormal K_iso with sigma 0.3): loss = sum over wet cells of
+    (temp after 8 steps - target)^2 with target = initial temp + N(0, 0.05),
+    gradients with respect to the initial temp, salt and K_iso through the
+    autograd Function with per-step checkpoints. Returns the report dict."""
+    import torch
+
+    from veros_gb300 import synthetic
+    from veros_gb300.adjoint import IsoneutralAdjoint
+    from veros_gb300.state import DeviceState
+
+    nsteps = 8
+    host = synthetic.global_1deg_state(seed=0, nz=30, k_iso_lognormal_sigma=0.3)
+    rng = np.random.default_rng(4)
+    T0 = host.arrays["temp"][..., 1]
+    wet = np.zeros_like(T0)
+    wet[2:-2, 2:-2] = host.arrays["maskT"][2:-2, 2:-2]
+    target = T0 + rng.normal(0.0, 0.05, T0.shape) * wet
+    model = IsoneutralAdjoint(DeviceState.from_host(host, device=device))
+    T0d, S0d, Kd = (model.field(x) for x in (T0, host.arrays["salt"][..., 1], host.arrays["K_iso"]))
+    tgt, w = model.field(target), model.field(wet)
+
+    def once():
+        leaves = [model.field(x).requires_grad_() for x in (T0d, S0d, Kd)]
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        T, _ = model.rollout(*leaves, nsteps)
+        loss = ((T - tgt) ** 2 * w).sum()
+        e[1].record()
+        loss.backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+
+    for _ in range(2):
+        once()
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(device)
+    before = torch.cuda.memory_allocated(device)
+    times = np.array([once() for _ in range(reps)])
+    peak = torch.cuda.max_memory_allocated(device) - before
+    fwd, bwd = (float(np.median(times[:, n])) for n in range(2))
+    field_mib = model.dev.plane * model.dev.Z * 8 / 2**20
+    cells = host.nx * host.ny * host.nz
+    return {"workload": f"adjoint of an {nsteps}-step FP64 rollout, {host.nx}x{host.ny}x{host.nz}, eq 3, "
+                        "lognormal K_iso (sigma 0.3)",
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "forward_plus_backward_over_forward": (fwd + bwd) / fwd,
+            "backward_cells_per_s": cells * nsteps / (bwd / 1e3),
+            "peak_extra_mib": peak / 2**20, "checkpoint_mib_per_step": 2 * field_mib,
+            "workspace_mib": model._work.numel() * 8 / 2**20,
+            "gpu_launches_per_rollout": nsteps * (model.forward_launches + model.backward_launches),
+            "timing": "CUDA events, median of 5 after 2 warm-up rollouts"}
+
+
 def run_gb300(args):
     import torch
 
@@ -348,11 +404,14 @@ def run_gb300(args):
     e2e_value = e2e_cells / e2e_s
 
     launches = args.steps * stepper.launches_per_step()
-    ensemble = None
-    if not args.no_ensemble:
+    ensemble = adjoint = None
+    if not (args.no_ensemble and args.no_adjoint):
         del dev, stepper
         torch.cuda.empty_cache()
+    if not args.no_ensemble:
         ensemble = run_ensemble(device)
+    if not args.no_adjoint:
+        adjoint = run_adjoint(device)
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -388,6 +447,7 @@ def run_gb300(args):
                                   "FP32 tensors, fluxes, taper, tendencies"},
         "gpu_launches": launches,
         "ensemble": ensemble,
+        "adjoint": adjoint,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))
@@ -403,6 +463,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 48-member batched-ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the 8-step rollout adjoint measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

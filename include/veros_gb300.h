@@ -286,6 +286,30 @@ int vg_ensemble_tune(void *handle, const VgEnsembleTuning *tuning);
 int vg_ensemble_step(void *handle, int phase, void *stream);
 int vg_ensemble_destroy(void *handle);
 
+/* Adjoint of one FP64 step of vg_isoneutral_step_f64 (no reference
+ * counterpart: Veros defines no derivative of this path). The step maps
+ * (temp, salt, K_iso) to (temp_new, salt_new); given dL/dtemp_new and
+ * dL/dsalt_new this writes dL/dtemp and dL/dsalt and ADDS dL/dK_iso into
+ * gK_iso (so a rollout accumulates it over its steps). temp/salt and
+ * temp_new/salt_new are the step's input and output levels (the caller's
+ * per-step checkpoints); the diffusion tensor is recomputed from them. The
+ * energy branch does not change the tracers and takes no part. All fields
+ * canonical; the gradients may not alias the inputs. */
+typedef struct VgAdjointFields {
+  const double *temp, *salt;
+  const double *temp_new, *salt_new;
+  const double *K_iso;
+  const uint8_t *mask_bits;
+  const int32_t *kbot;
+  const double *gtemp_new, *gsalt_new;
+  double *gtemp, *gsalt;
+  double *gK_iso;
+} VgAdjointFields;
+
+size_t vg_isoneutral_step_adjoint_scratch_bytes(const VgDomain *dom);
+int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                   const VgAdjointFields *f, void *scratch, size_t scratch_bytes, void *stream);
+
 /* Replaces veros.core.utilities.solve_implicit (veros/core/utilities.py:51-59)
  * and veros.core.operators.solve_tridiagonal (veros/core/operators.py:60-77,
  * :102-156). nsys columns of nz levels; element (s, k) of every array is at

@@ -75,6 +75,33 @@ def central_difference(loss_of, signs_of, x, u, eps, shrink=2):
     return (loss_of(x + h * u) - loss_of(x - h * u)) / (2 * h), eps
 
 
+def directional_checks(loss_of, signs_of, inputs, grads, eps0, ndir, rng):
+    """Directional derivatives of ``loss_of(**inputs)`` along seeded random
+    unit directions of one input at a time, as central differences
+    (``central_difference``) and from the gradients ``grads``.
+
+    ``ndir`` maps input names to direction counts and ``eps0`` to relative
+    steps. Yields ``(name, fd, ad, scale)`` with ``scale = max(|ad|,
+    |grad| / sqrt(n))``, the typical size of a directional derivative along a
+    random unit direction in n dimensions.
+    """
+    for which, count in ndir.items():
+        def with_(x, which=which):
+            a = dict(inputs)
+            a[which] = x
+            return a
+
+        for _ in range(count):
+            x = inputs[which]
+            u = rng.standard_normal(x.shape)
+            u /= np.linalg.norm(u)
+            fd, _ = central_difference(lambda y: loss_of(**with_(y)), lambda y: signs_of(**with_(y)), x, u,
+                                       eps0[which])
+            g = np.asarray(grads[which])
+            ad = float(np.sum(g * u))
+            yield which, fd, ad, max(abs(ad), float(np.linalg.norm(g)) / np.sqrt(g.size))
+
+
 def wet_interior(base):
     m = _g(base, "maskT").astype(np.float64)
     w = np.zeros_like(m)

@@ -42,35 +42,19 @@ def _case(eq, seed=3, nsteps=3):
     return host, T0, S0, K, target, wet, rng, nsteps
 
 
-def directional_checks(host, T0, S0, K, target, wet, rng, n, grads, ndir=(6, 5, 5)):
-    """Yields (input, fd, ad, scale) for seeded random unit directions."""
-    gT, gS, gK = grads
-    base = {"T": T0, "S": S0, "K": K}
-    eps0 = {"T": 1e-6, "S": 1e-6, "K": 1e-4}
-    grad = {"T": gT, "S": gS, "K": gK}
-    for which, count in zip("TSK", ndir):
-        def with_(x, which=which):
-            a = dict(base)
-            a[which] = x
-            return a
+EPS = {"T": 1e-6, "S": 1e-6, "K": 1e-4}
+NDIR = {"T": 6, "S": 5, "K": 5}  # 16 directions
 
-        def loss_of(x, with_=with_):
-            a = with_(x)
-            Ts, _ = A.rollout(host, a["T"], a["S"], a["K"], n)
-            return A.loss(Ts[-1], target, wet)
 
-        def signs_of(x, with_=with_):
-            a = with_(x)
-            return A.rollout_slope_signs(host, a["T"], a["S"], a["K"], n)
+def oracle_loss_and_signs(host, target, wet, n):
+    def loss_of(T, S, K):
+        Ts, _ = A.rollout(host, T, S, K, n)
+        return A.loss(Ts[-1], target, wet)
 
-        for _ in range(count):
-            x = base[which]
-            u = rng.standard_normal(x.shape)
-            u /= np.linalg.norm(u)
-            fd, _ = A.central_difference(loss_of, signs_of, x, u, eps0[which])
-            g = grad[which]
-            ad = float(np.sum(g * u))
-            yield which, fd, ad, max(abs(ad), np.linalg.norm(g) / np.sqrt(g.size))
+    def signs_of(T, S, K):
+        return A.rollout_slope_signs(host, T, S, K, n)
+
+    return loss_of, signs_of
 
 
 @pytest.mark.parametrize("eq", [1, 3])
@@ -79,7 +63,9 @@ def test_adjoint_oracle_matches_central_differences(eq):
     L, gT, gS, gK = A.rollout_grad(host, T0, S0, K, target, n)
     Ts, _ = A.rollout(host, T0, S0, K, n)
     assert L == pytest.approx(A.loss(Ts[-1], target, wet), rel=1e-14)
-    for which, fd, ad, scale in directional_checks(host, T0, S0, K, target, wet, rng, n, (gT, gS, gK)):
+    loss_of, signs_of = oracle_loss_and_signs(host, target, wet, n)
+    checks = A.directional_checks(loss_of, signs_of, dict(T=T0, S=S0, K=K), dict(T=gT, S=gS, K=gK), EPS, NDIR, rng)
+    for which, fd, ad, scale in checks:
         assert abs(fd - ad) <= RTOL * scale, (which, fd, ad)
 
 

@@ -82,6 +82,11 @@ class VgEnsembleMemberF32(ctypes.Structure):
     _fields_ = [("dom", VgDomain), ("grid", VgGrid), ("set", VgIsoSettings), ("phase", VgStepFieldsF32 * 3)]
 
 
+class VgAdjointFields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("temp", "salt", "temp_new", "salt_new", "K_iso", "mask_bits", "kbot",
+                                                "gtemp_new", "gsalt_new", "gtemp", "gsalt", "gK_iso")]
+
+
 # name -> (restype, argtypes); the exported C ABI
 SIGNATURES = {
     "vg_last_error": (ctypes.c_char_p, []),
@@ -142,6 +147,10 @@ SIGNATURES = {
     "vg_isoneutral_streamfunction_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_void_p, ctypes.c_void_p,
                                                         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "vg_isoneutral_step_adjoint_scratch_bytes": (ctypes.c_size_t, [ctypes.POINTER(VgDomain)]),
+    "vg_isoneutral_step_adjoint_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                      ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgAdjointFields),
+                                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_ensemble_create_f64": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMember), ctypes.c_int,
                                               ctypes.POINTER(VgEnsembleTuning), ctypes.POINTER(ctypes.c_void_p)]),
     "vg_ensemble_create_f32split": (ctypes.c_int, [ctypes.POINTER(VgEnsembleMemberF32), ctypes.c_int,

@@ -1,0 +1,653 @@
+// Adjoint of one FP64 isoneutral step (the step of vg_isoneutral_step_f64:
+// veros/core/thermodynamics.py:226-241 with zero advection, then
+// isoneutral_diffusion_pre and isoneutral_diffusion of temp and salt,
+// veros/core/isoneutral/isoneutral.py:18-229 and diffusion.py:9-283).
+//
+// Given dL/dT_{n+1} and dL/dS_{n+1} it returns dL/dT_n and dL/dS_n and adds
+// dL/dK_iso. The step's inputs T_n, S_n and outputs T_{n+1}, S_{n+1} are the
+// caller's checkpoints; the diffusion tensor is recomputed from them.
+//
+// Per-slope formulation: every slope of the tensor is attached to a T point
+// P, one of its horizontal faces h (east, west, north, south) and one of its
+// vertical faces v (below, above),
+//   s = -(drdT(P) dT/dh + drdS(P) dS/dh) / (min(0, drdT(P) dT/dz(v) + drdS(P) dS/dz(v)) - epsln),
+// and enters two terms of the forward with the same value: the term of face h
+// (Ai_ez / Ai_nz, K_11 / K_22; isoneutral.py:100-168) and the term of face v
+// (Ai_bx / Ai_by, K_33; :173-224). The adjoint visits each of the eight
+// slopes of a point once.
+//
+// Launches (one stream, in order):
+//   1. adj_tables_kernel     reciprocal grid factors
+//   2. pre_tile_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel)
+//   3. adj_implicit_kernel   per water column: the transposed tridiagonal
+//                            system A^T y = dL/dx (one Thomas factorisation
+//                            for temp and salt) and dL/dK_33 from
+//                            dL/ddelta_k = (x_{k+1} - x_k)(y_k/dzt_k - y_{k+1}/dzt_{k+1})
+//   4. adj_slope_kernel      per point: the eight slope adjoints, written as
+//                            per-point partial sums onto the point's faces
+//   5. adj_gather_kernel     per point: sums the partials of the faces around
+//                            it into dL/dT_n, dL/dS_n and dL/dK_iso
+//
+// Every partial is written exactly once by the point that owns it and read
+// by its neighbours in the next launch: no atomics, results are deterministic.
+#include "common.cuh"
+#include "pre_kernels.cuh"
+
+namespace vg {
+namespace adj {
+
+using detail::kEpsln;
+using detail::taper_of;
+
+// reciprocal grid tables (scratch tail)
+struct GridInv {
+  const double *inv_dxu, *inv_dxt, *qinv_dxt;                // X
+  const double *inv_dyu, *inv_dyt, *inv_cost, *qinv_dyt_cost;  // Y
+  const double *inv_dzw, *inv_dzt, *qinv_dzt;                 // Z
+};
+
+constexpr int kTensorFields = 19;  // K_11, K_22, K_33, 4 x 4 Ai components
+enum { F_GTP = kTensorFields, F_GSP, F_GK33, F_PART };
+// partial sums written by the slope pass, one field each
+enum { P_LRT = 0, P_NSUM = 1, P_LG = 5, P_LVD = 7, P_LHD = 11, P_LDL = 19, P_LKW = 23, P_N = 25 };
+constexpr int kFields = F_PART + P_N;
+
+inline size_t table_doubles(const Layout &L) { return 3 * (size_t)L.X + 4 * (size_t)L.Y + 3 * (size_t)L.Z; }
+
+inline size_t field_doubles(const Layout &L) { return (size_t)L.plane * L.Z; }
+
+inline size_t scratch_bytes(const Layout &L) {
+  size_t n = (size_t)kFields * field_doubles(L) + table_doubles(L);
+  return (n * sizeof(double) + 255) & ~(size_t)255;
+}
+
+GridInv tables_of(const Layout &L, const double *t) {
+  GridInv g;
+  g.inv_dxu = t;
+  g.inv_dxt = t + L.X;
+  g.qinv_dxt = t + 2 * L.X;
+  const double *ty = t + 3 * L.X;
+  g.inv_dyu = ty;
+  g.inv_dyt = ty + L.Y;
+  g.inv_cost = ty + 2 * L.Y;
+  g.qinv_dyt_cost = ty + 3 * L.Y;
+  const double *tz = ty + 4 * L.Y;
+  g.inv_dzw = tz;
+  g.inv_dzt = tz + L.Z;
+  g.qinv_dzt = tz + 2 * L.Z;
+  return g;
+}
+
+__global__ void adj_tables_kernel(Layout L, Grid g, double *t) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int X = L.X, Y = L.Y, Z = L.Z;
+  if (n < X) {
+    t[n] = 1.0 / g.dxu[n];
+    t[X + n] = 1.0 / g.dxt[n];
+    t[2 * X + n] = 1.0 / (4.0 * g.dxt[n]);
+  }
+  double *ty = t + 3 * X;
+  if (n < Y) {
+    ty[n] = 1.0 / g.dyu[n];
+    ty[Y + n] = 1.0 / g.dyt[n];
+    ty[2 * Y + n] = 1.0 / g.cost[n];
+    ty[3 * Y + n] = 1.0 / (4.0 * g.dyt[n] * g.cost[n]);
+  }
+  double *tz = ty + 4 * Y;
+  if (n < Z) {
+    tz[n] = 1.0 / g.dzw[n];
+    tz[Z + n] = 1.0 / g.dzt[n];
+    tz[2 * Z + n] = 1.0 / (4.0 * g.dzt[n]);
+  }
+}
+
+// d(drho/dT)/dT (veros/core/density/get_rho.py:93-111)
+__device__ __forceinline__ double drdT_dT(int eos) {
+  if (eos == 1) return 0.0;
+  if (eos == 3) return -Eos::betaTs3 * Eos::rho0;
+  return -2.0 * Eos::betaTs24 * Eos::rho0;
+}
+
+// ---------------------------------------------------------------------------
+// 3. implicit part (diffusion.py:142-169)
+// ---------------------------------------------------------------------------
+struct ImpArgs {
+  Layout L;
+  GridInv gi;
+  double dt;
+  const int32_t *__restrict__ kbot;
+  const double *__restrict__ K33;
+  const double *__restrict__ xT;  // T_{n+1}: the solution of the forward solve
+  const double *__restrict__ xS;
+  const double *__restrict__ gTn;  // dL/dT_{n+1}
+  const double *__restrict__ gSn;
+  double *gTp, *gSp, *gK33;  // dL/d(right-hand side), dL/dK_33
+};
+
+// Row k of the forward matrix: a_k = -delta_{k-1}/dzt_k, c_k = -delta_k/dzt_k,
+// b_k = 1 + (delta_k + delta_{k-1})/dzt_k (no delta_{k-1} on the bottom row
+// ks), delta_k = dt K_33/dzw_k (0 on the top level). The transposed system
+// has sub-diagonal c_{k-1} and super-diagonal a_{k+1}; A is row diagonally
+// dominant, so A^T is column diagonally dominant and needs no pivoting.
+__global__ void __launch_bounds__(64) adj_implicit_kernel(ImpArgs a) {
+  extern __shared__ double smem[];
+  const Layout &L = a.L;
+  const int Z = L.Z, nb = blockDim.x, t = threadIdx.x;
+  double *cps = smem;                   // [k][thread]
+  double *dps = smem + (size_t)Z * nb;  // [r][k][thread]
+  const int col = blockIdx.x * nb + t;
+  if (col >= L.X * L.Y) return;
+  const int i = col % L.X, j = col / L.X;
+  const long long base = L.at2(i, j);
+  const bool interior = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  const int ks = interior ? a.kbot[base] - 1 : -1;  // create_water_masks (utilities.py:38-48)
+  const int kw = (ks >= 0 && ks < Z) ? ks : Z;
+  // cells outside the solve pass their adjoint through
+  for (int k = 0; k < kw; ++k) {
+    const long long o = base + (long long)k * L.plane;
+    a.gTp[o] = a.gTn[o];
+    a.gSp[o] = a.gSn[o];
+    a.gK33[o] = 0.0;
+  }
+  if (kw == Z) return;
+
+  double cp = 0.0, dp0 = 0.0, dp1 = 0.0, delta_prev = 0.0;
+  for (int k = ks; k < Z; ++k) {
+    const long long o = base + (long long)k * L.plane;
+    const double delta = k < Z - 1 ? a.dt * a.gi.inv_dzw[k] * a.K33[o] : 0.0;
+    const double b = 1.0 + (delta + (k > ks ? delta_prev : 0.0)) * a.gi.inv_dzt[k];
+    const double sub = k > ks ? -delta_prev * a.gi.inv_dzt[k - 1] : 0.0;
+    const double sup = k < Z - 1 ? -delta * a.gi.inv_dzt[k + 1] : 0.0;
+    const double inv = 1.0 / (b - sub * cp);
+    cp = sup * inv;
+    dp0 = (a.gTn[o] - sub * dp0) * inv;
+    dp1 = (a.gSn[o] - sub * dp1) * inv;
+    cps[(size_t)k * nb + t] = cp;
+    dps[(size_t)k * nb + t] = dp0;
+    dps[((size_t)Z + k) * nb + t] = dp1;
+    delta_prev = delta;
+  }
+  double y0 = 0.0, y1 = 0.0, xu0 = 0.0, xu1 = 0.0;  // values one level up
+  for (int k = Z - 1; k >= ks; --k) {
+    const long long o = base + (long long)k * L.plane;
+    const double c = cps[(size_t)k * nb + t];
+    const double n0 = dps[(size_t)k * nb + t] - c * y0;
+    const double n1 = dps[((size_t)Z + k) * nb + t] - c * y1;
+    const double x0 = a.xT[o], x1 = a.xS[o];
+    double gk = 0.0;
+    if (k < Z - 1) {
+      const double r0 = a.gi.inv_dzt[k], r1 = a.gi.inv_dzt[k + 1];
+      const double ld = (xu0 - x0) * (n0 * r0 - y0 * r1) + (xu1 - x1) * (n1 * r0 - y1 * r1);
+      gk = ld * a.dt * a.gi.inv_dzw[k];
+    }
+    a.gTp[o] = n0;
+    a.gSp[o] = n1;
+    a.gK33[o] = gk;
+    y0 = n0;
+    y1 = n1;
+    xu0 = x0;
+    xu1 = x1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 4. slope adjoints
+// ---------------------------------------------------------------------------
+struct SlopeArgs {
+  Layout L;
+  Grid g;
+  GridInv gi;
+  int eos;
+  double slopec, inv_dslope, ksteep, dt;
+  const double *__restrict__ T;
+  const double *__restrict__ S;
+  const double *__restrict__ K;
+  const double *__restrict__ gTp;
+  const double *__restrict__ gSp;
+  const double *__restrict__ gK33;
+  const uint8_t *__restrict__ m;
+  double *part;
+  long long field;
+};
+
+// dt * dL/dT_p on interior wet points: the adjoint of the explicit tendency
+// (diffusion.py:116-139, 191-192)
+__device__ __forceinline__ double mu_at(const Layout &L, const uint8_t *m, const double *gp, double dt, long long o,
+                                        int i, int j) {
+  if (i < 2 || i >= L.X - 2 || j < 2 || j >= L.Y - 2) return 0.0;
+  if (!(__ldg(m + o) & VG_MASK_T)) return 0.0;
+  return dt * __ldg(gp + o);
+}
+
+__global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
+  const Layout &L = a.L;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= L.X || j >= L.Y) return;
+  const int X = L.X, Y = L.Y, Z = L.Z;
+  const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane;
+  const GridInv &gi = a.gi;
+  const uint8_t *m = a.m;
+  const unsigned mk = __ldg(m + o);
+  const bool hasE = i < X - 1, hasW = i > 0, hasN = j < Y - 1, hasS = j > 0, hasU = k < Z - 1, hasD = k > 0;
+  const bool inter = i >= 2 && i < X - 2 && j >= 2 && j < Y - 2;
+  const bool rowE = j >= 2 && j < Y - 2, colN = i >= 2 && i < X - 2;
+  const Eos eos{a.eos};
+
+  const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
+  const bool wet = mk & VG_MASK_T;
+  const double rT = wet ? eos.drdT(Tc, a.g.zt[k]) : 0.0;
+  const double rS = wet ? eos.drdS() : 0.0;
+
+  // tracer differences across the faces (unmasked) and the face masks
+  double hdT[4], hdS[4], vdT[2], vdS[2];
+  hdT[0] = hasE ? __ldg(a.T + o + 1) - Tc : 0.0;
+  hdS[0] = hasE ? __ldg(a.S + o + 1) - Sc : 0.0;
+  hdT[1] = hasW ? Tc - __ldg(a.T + o - 1) : 0.0;
+  hdS[1] = hasW ? Sc - __ldg(a.S + o - 1) : 0.0;
+  hdT[2] = hasN ? __ldg(a.T + o + PW) - Tc : 0.0;
+  hdS[2] = hasN ? __ldg(a.S + o + PW) - Sc : 0.0;
+  hdT[3] = hasS ? Tc - __ldg(a.T + o - PW) : 0.0;
+  hdS[3] = hasS ? Sc - __ldg(a.S + o - PW) : 0.0;
+  vdT[0] = hasD ? Tc - __ldg(a.T + o - PL) : 0.0;
+  vdS[0] = hasD ? Sc - __ldg(a.S + o - PL) : 0.0;
+  vdT[1] = hasU ? __ldg(a.T + o + PL) - Tc : 0.0;
+  vdS[1] = hasU ? __ldg(a.S + o + PL) - Sc : 0.0;
+  const bool mH[4] = {hasE && (mk & VG_MASK_U), hasW && (__ldg(m + o - 1) & VG_MASK_U),
+                      hasN && (mk & VG_MASK_V), hasS && (__ldg(m + o - PW) & VG_MASK_V)};
+  const bool mWv[2] = {hasD && (__ldg(m + o - PL) & VG_MASK_W), hasU && (mk & VG_MASK_W)};
+
+  // face gradients (isoneutral.py:46-95)
+  const double icx = gi.inv_cost[j];
+  double gxT[4], gxS[4], gzT[2], gzS[2];
+  {
+    const double f0 = mH[0] ? gi.inv_dxu[i] * icx : 0.0;
+    const double f1 = mH[1] ? gi.inv_dxu[i - 1] * icx : 0.0;
+    const double f2 = mH[2] ? gi.inv_dyu[j] : 0.0;
+    const double f3 = mH[3] ? gi.inv_dyu[j - 1] : 0.0;
+    gxT[0] = hdT[0] * f0;
+    gxS[0] = hdS[0] * f0;
+    gxT[1] = hdT[1] * f1;
+    gxS[1] = hdS[1] * f1;
+    gxT[2] = hdT[2] * f2;
+    gxS[2] = hdS[2] * f2;
+    gxT[3] = hdT[3] * f3;
+    gxS[3] = hdS[3] * f3;
+    const double z0 = mWv[0] ? gi.inv_dzw[k - 1] : 0.0;
+    const double z1 = mWv[1] ? gi.inv_dzw[k] : 0.0;
+    gzT[0] = vdT[0] * z0;
+    gzS[0] = vdS[0] * z0;
+    gzT[1] = vdT[1] * z1;
+    gzS[1] = vdS[1] * z1;
+  }
+  double G[2], R[2];
+#pragma unroll
+  for (int v = 0; v < 2; ++v) {
+    G[v] = rT * gzT[v] + rS * gzS[v];
+    R[v] = 1.0 / (fmin(0.0, G[v]) - kEpsln);
+  }
+
+  // which faces carry a term: face h (east/north terms) and face v (top terms)
+  const bool vE[4] = {rowE && i >= 1 && i < X - 2 && mH[0], rowE && i >= 2 && i < X - 1 && mH[1],
+                      colN && j >= 1 && j < Y - 2 && mH[2], colN && j >= 2 && j < Y - 1 && mH[3]};
+  const bool vT[2] = {inter && mWv[0], inter && mWv[1]};
+
+  // adjoints of the fluxes on the faces (diffusion.py:116-139)
+  double lfT[4] = {0, 0, 0, 0}, lfS[4] = {0, 0, 0, 0}, lftT[2] = {0, 0}, lftS[2] = {0, 0};
+  {
+    const double cT = mu_at(L, m, a.gTp, a.dt, o, i, j), cS = mu_at(L, m, a.gSp, a.dt, o, i, j);
+    if (vE[0]) {
+      const double eT = mu_at(L, m, a.gTp, a.dt, o + 1, i + 1, j), eS = mu_at(L, m, a.gSp, a.dt, o + 1, i + 1, j);
+      lfT[0] = (cT * gi.inv_dxt[i] - eT * gi.inv_dxt[i + 1]) * icx;
+      lfS[0] = (cS * gi.inv_dxt[i] - eS * gi.inv_dxt[i + 1]) * icx;
+    }
+    if (vE[1]) {
+      const double wT = mu_at(L, m, a.gTp, a.dt, o - 1, i - 1, j), wS = mu_at(L, m, a.gSp, a.dt, o - 1, i - 1, j);
+      lfT[1] = (wT * gi.inv_dxt[i - 1] - cT * gi.inv_dxt[i]) * icx;
+      lfS[1] = (wS * gi.inv_dxt[i - 1] - cS * gi.inv_dxt[i]) * icx;
+    }
+    const double cy = gi.inv_dyt[j] * icx;
+    if (vE[2]) {
+      const double nT = mu_at(L, m, a.gTp, a.dt, o + PW, i, j + 1), nS = mu_at(L, m, a.gSp, a.dt, o + PW, i, j + 1);
+      const double ny = gi.inv_dyt[j + 1] * gi.inv_cost[j + 1];
+      lfT[2] = a.g.cosu[j] * (cT * cy - nT * ny);
+      lfS[2] = a.g.cosu[j] * (cS * cy - nS * ny);
+    }
+    if (vE[3]) {
+      const double sT = mu_at(L, m, a.gTp, a.dt, o - PW, i, j - 1), sS = mu_at(L, m, a.gSp, a.dt, o - PW, i, j - 1);
+      const double sy = gi.inv_dyt[j - 1] * gi.inv_cost[j - 1];
+      lfT[3] = a.g.cosu[j - 1] * (sT * sy - cT * cy);
+      lfS[3] = a.g.cosu[j - 1] * (sS * sy - cS * cy);
+    }
+    if (vT[0]) {
+      const double dT = mu_at(L, m, a.gTp, a.dt, o - PL, i, j), dS = mu_at(L, m, a.gSp, a.dt, o - PL, i, j);
+      lftT[0] = dT * gi.inv_dzt[k - 1] - cT * gi.inv_dzt[k];
+      lftS[0] = dS * gi.inv_dzt[k - 1] - cS * gi.inv_dzt[k];
+    }
+    if (vT[1]) {
+      const double uT = mu_at(L, m, a.gTp, a.dt, o + PL, i, j), uS = mu_at(L, m, a.gSp, a.dt, o + PL, i, j);
+      lftT[1] = cT * gi.inv_dzt[k] - uT * gi.inv_dzt[k + 1];
+      lftS[1] = cS * gi.inv_dzt[k] - uS * gi.inv_dzt[k + 1];
+    }
+  }
+
+  // face-level factors of the two terms
+  double dl[4] = {0, 0, 0, 0}, gKh[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0}, cp[4] = {0, 0, 0, 0};
+  {
+    const double *K = a.K;
+    // diffloc of the face, isoneutral.py:101-104 and :138-141 (k = 0: :104)
+    auto dl_of = [&](long long ow, long long off) {
+      return hasD ? 0.25 * (__ldg(K + ow) + __ldg(K + ow - PL) + __ldg(K + ow + off) + __ldg(K + ow + off - PL))
+                  : 0.5 * (__ldg(K + ow) + __ldg(K + ow + off));
+    };
+    if (vE[0]) {
+      dl[0] = dl_of(o, 1);
+      gKh[0] = (lfT[0] * hdT[0] + lfS[0] * hdS[0]) * (gi.inv_dxu[i] * icx);
+    }
+    if (vE[1]) {
+      dl[1] = dl_of(o - 1, 1);
+      gKh[1] = (lfT[1] * hdT[1] + lfS[1] * hdS[1]) * (gi.inv_dxu[i - 1] * icx);
+    }
+    if (vE[2]) {
+      dl[2] = dl_of(o, PW);
+      gKh[2] = (lfT[2] * hdT[2] + lfS[2] * hdS[2]) * gi.inv_dyu[j];
+    }
+    if (vE[3]) {
+      dl[3] = dl_of(o - PW, PW);
+      gKh[3] = (lfT[3] * hdT[3] + lfS[3] * hdS[3]) * gi.inv_dyu[j - 1];
+    }
+    if (inter) {
+      c[0] = a.g.dxu[i] * gi.qinv_dxt[i];
+      c[1] = a.g.dxu[i - 1] * gi.qinv_dxt[i];
+      cp[0] = cp[1] = icx * gi.qinv_dxt[i];
+      c[2] = a.g.cosu[j] * a.g.dyu[j] * gi.qinv_dyt_cost[j];
+      c[3] = a.g.cosu[j - 1] * a.g.dyu[j - 1] * gi.qinv_dyt_cost[j];
+      cp[2] = a.g.cosu[j] * gi.qinv_dyt_cost[j];
+      cp[3] = a.g.cosu[j - 1] * gi.qinv_dyt_cost[j];
+    }
+  }
+  const double KW[2] = {vT[0] ? __ldg(a.K + o - PL) : 0.0, vT[1] ? __ldg(a.K + o) : 0.0};
+  const double gK33W[2] = {vT[0] ? __ldg(a.gK33 + o - PL) : 0.0, vT[1] ? __ldg(a.gK33 + o) : 0.0};
+  const double dzwv[2] = {hasD ? a.g.dzw[k - 1] : 0.0, a.g.dzw[k]};
+  const double q = gi.qinv_dzt[k];
+
+  double lrT = 0.0, nsum[4] = {0, 0, 0, 0}, lG[2] = {0, 0}, lvd[2][2] = {{0, 0}, {0, 0}};
+  double lhd[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}}, ldl[4] = {0, 0, 0, 0}, lKw[2] = {0, 0};
+#pragma unroll
+  for (int h = 0; h < 4; ++h) {
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const bool Ef = vE[h] && (v == 1 || hasD);
+      const bool Tf = vT[v];
+      if (!Ef && !Tf) continue;
+      const double s = -(rT * gxT[h] + rS * gxS[h]) * R[v];
+      const double t = taper_of(s, a.slopec, a.inv_dslope);
+      const double sg = (s > 0.0) ? 1.0 : (s < 0.0 ? -1.0 : 0.0);
+      const double tp = -2.0 * sg * t * (1.0 - t) * a.inv_dslope;  // d taper / ds
+      const double tst = t + s * tp;                              // d (taper s) / ds
+      const double ts = t * s;
+      double gs = 0.0;
+      if (Ef) {
+        // Ai = taper s, K_11 += dzw max(K_iso_steep, diffloc taper) / (4 dzt)
+        const double lfv = lfT[h] * vdT[v] + lfS[h] * vdS[v];
+        const double dlq = dl[h] * q;
+        const double kq = dl[h] * t > a.ksteep ? gKh[h] * dzwv[v] * q : 0.0;
+        gs += lfv * dlq * tst + kq * dl[h] * tp;
+        ldl[h] += kq * t + lfv * ts * q;
+        lvd[0][v] += lfT[h] * ts * dlq;
+        lvd[1][v] += lfS[h] * ts * dlq;
+      }
+      if (Tf) {
+        // Ai_b = taper s, K_33 += c K_iso taper s^2
+        const double lfh = lftT[v] * hdT[h] + lftS[v] * hdS[h];
+        const double kc = gK33W[v] * c[h];
+        gs += lfh * KW[v] * cp[h] * tst + kc * KW[v] * (tp * s * s + 2.0 * ts);
+        lKw[v] += kc * ts * s + lfh * ts * cp[h];
+        const double f = KW[v] * ts * cp[h];
+        lhd[0][h] += lftT[v] * f;
+        lhd[1][h] += lftS[v] * f;
+      }
+      const double lN = -gs * R[v];
+      if (G[v] < 0.0) lG[v] -= gs * s * R[v];
+      lrT += lN * gxT[h];
+      nsum[h] += lN;
+    }
+  }
+  lrT += lG[0] * gzT[0] + lG[1] * gzT[1];
+
+  double *p = a.part + o;
+  const long long F = a.field;
+  p[P_LRT * F] = lrT;
+#pragma unroll
+  for (int h = 0; h < 4; ++h) {
+    p[(P_NSUM + h) * F] = nsum[h];
+    p[(P_LHD + h) * F] = lhd[0][h];
+    p[(P_LHD + 4 + h) * F] = lhd[1][h];
+    p[(P_LDL + h) * F] = ldl[h];
+  }
+#pragma unroll
+  for (int v = 0; v < 2; ++v) {
+    p[(P_LG + v) * F] = lG[v];
+    p[(P_LVD + v) * F] = lvd[0][v];
+    p[(P_LVD + 2 + v) * F] = lvd[1][v];
+    p[(P_LKW + v) * F] = lKw[v];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. gather onto points
+// ---------------------------------------------------------------------------
+struct GatherArgs {
+  Layout L;
+  Grid g;
+  GridInv gi;
+  int eos;
+  double dt;
+  const double *__restrict__ T;
+  const double *__restrict__ gTp;
+  const double *__restrict__ gSp;
+  const double *__restrict__ K11;
+  const double *__restrict__ K22;
+  const uint8_t *__restrict__ m;
+  const double *__restrict__ part;
+  long long field;
+  double *gT, *gS, *gK;
+};
+
+__global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
+  const Layout &L = a.L;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (i >= L.X || j >= L.Y) return;
+  const int X = L.X, Y = L.Y, Z = L.Z;
+  const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane, F = a.field;
+  const GridInv &gi = a.gi;
+  const uint8_t *m = a.m;
+  const Eos eos{a.eos};
+  auto part = [&](int comp, long long at) { return __ldg(a.part + comp * F + at); };
+  auto rT_at = [&](long long at, int kk) {
+    return (__ldg(m + at) & VG_MASK_T) ? eos.drdT(__ldg(a.T + at), a.g.zt[kk]) : 0.0;
+  };
+  auto rS_at = [&](long long at) { return (__ldg(m + at) & VG_MASK_T) ? eos.drdS() : 0.0; };
+
+  const bool wet = __ldg(m + o) & VG_MASK_T;
+  double lamT = wet ? __ldg(a.gTp + o) + drdT_dT(a.eos) * part(P_LRT, o) : 0.0;
+  double lamS = wet ? __ldg(a.gSp + o) : 0.0;
+  double gk = part(P_LKW + 1, o) + (k < Z - 1 ? part(P_LKW + 0, o + PL) : 0.0);
+  const double wk = k >= 1 ? 0.25 : 0.5;
+
+  // x-faces f = i-1 (this point is east of it) and f = i (west of it)
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int f = i - 1 + side;
+    if (f < 0 || f > X - 2) continue;
+    const long long ow = o - 1 + side, oe = ow + 1;
+    const double nW = part(P_NSUM + 0, ow), nE = part(P_NSUM + 1, oe);
+    const double lgT = nW * rT_at(ow, k) + nE * rT_at(oe, k);
+    const double lgS = nW * rS_at(ow) + nE * rS_at(oe);
+    const double fac = (__ldg(m + ow) & VG_MASK_U) ? gi.inv_dxu[f] * gi.inv_cost[j] : 0.0;
+    double lhT = part(P_LHD + 0, ow) + part(P_LHD + 1, oe);
+    double lhS = part(P_LHD + 4, ow) + part(P_LHD + 5, oe);
+    if (f >= 1 && f < X - 2 && j >= 2 && j < Y - 2) {
+      // flux_east's K_11 term (diffusion.py:31-33)
+      const double k11 = __ldg(a.K11 + ow) * (gi.inv_dxu[f] * gi.inv_cost[j]);
+      const double muwT = mu_at(L, m, a.gTp, a.dt, ow, f, j), mueT = mu_at(L, m, a.gTp, a.dt, oe, f + 1, j);
+      const double muwS = mu_at(L, m, a.gSp, a.dt, ow, f, j), mueS = mu_at(L, m, a.gSp, a.dt, oe, f + 1, j);
+      lhT += (muwT * gi.inv_dxt[f] - mueT * gi.inv_dxt[f + 1]) * gi.inv_cost[j] * k11;
+      lhS += (muwS * gi.inv_dxt[f] - mueS * gi.inv_dxt[f + 1]) * gi.inv_cost[j] * k11;
+    }
+    const double wT = lgT * fac + lhT, wS = lgS * fac + lhS;
+    lamT += side == 0 ? wT : -wT;
+    lamS += side == 0 ? wS : -wS;
+    gk += wk * (part(P_LDL + 0, ow) + part(P_LDL + 1, oe));
+    if (k < Z - 1) gk += 0.25 * (part(P_LDL + 0, ow + PL) + part(P_LDL + 1, oe + PL));
+  }
+  // y-faces f = j-1, j
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int f = j - 1 + side;
+    if (f < 0 || f > Y - 2) continue;
+    const long long os = o + (side - 1) * PW, on = os + PW;
+    const double nS_ = part(P_NSUM + 2, os), nN_ = part(P_NSUM + 3, on);
+    const double lgT = nS_ * rT_at(os, k) + nN_ * rT_at(on, k);
+    const double lgS = nS_ * rS_at(os) + nN_ * rS_at(on);
+    const double fac = (__ldg(m + os) & VG_MASK_V) ? gi.inv_dyu[f] : 0.0;
+    double lhT = part(P_LHD + 2, os) + part(P_LHD + 3, on);
+    double lhS = part(P_LHD + 6, os) + part(P_LHD + 7, on);
+    if (f >= 1 && f < Y - 2 && i >= 2 && i < X - 2) {
+      // flux_north's K_22 term (diffusion.py:57-60)
+      const double k22 = __ldg(a.K22 + os) * gi.inv_dyu[f];
+      const double cs = gi.inv_dyt[f] * gi.inv_cost[f], cn = gi.inv_dyt[f + 1] * gi.inv_cost[f + 1];
+      const double musT = mu_at(L, m, a.gTp, a.dt, os, i, f), munT = mu_at(L, m, a.gTp, a.dt, on, i, f + 1);
+      const double musS = mu_at(L, m, a.gSp, a.dt, os, i, f), munS = mu_at(L, m, a.gSp, a.dt, on, i, f + 1);
+      lhT += a.g.cosu[f] * (musT * cs - munT * cn) * k22;
+      lhS += a.g.cosu[f] * (musS * cs - munS * cn) * k22;
+    }
+    const double wT = lgT * fac + lhT, wS = lgS * fac + lhS;
+    lamT += side == 0 ? wT : -wT;
+    lamS += side == 0 ? wS : -wS;
+    gk += wk * (part(P_LDL + 2, os) + part(P_LDL + 3, on));
+    if (k < Z - 1) gk += 0.25 * (part(P_LDL + 2, os + PL) + part(P_LDL + 3, on + PL));
+  }
+  // z-faces f = k-1, k
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    const int f = k - 1 + side;
+    if (f < 0 || f > Z - 2) continue;
+    const long long od = o + (side - 1) * PL, ou = od + PL;
+    const double gU = part(P_LG + 1, od), gD = part(P_LG + 0, ou);
+    const double lgT = gU * rT_at(od, f) + gD * rT_at(ou, f + 1);
+    const double lgS = gU * rS_at(od) + gD * rS_at(ou);
+    const double fac = (__ldg(m + od) & VG_MASK_W) ? gi.inv_dzw[f] : 0.0;
+    lamT += side == 0 ? lgT * fac : -lgT * fac;
+    lamS += side == 0 ? lgS * fac : -lgS * fac;
+  }
+  // vertical tracer differences of the isoneutral fluxes (edge-padded in z)
+  if (k >= 1) {
+    lamT += part(P_LVD + 0, o) + part(P_LVD + 1, o - PL);
+    lamS += part(P_LVD + 2, o) + part(P_LVD + 3, o - PL);
+  }
+  if (k < Z - 1) {
+    lamT -= part(P_LVD + 1, o) + part(P_LVD + 0, o + PL);
+    lamS -= part(P_LVD + 3, o) + part(P_LVD + 2, o + PL);
+  }
+  a.gT[o] = lamT;
+  a.gS[o] = lamS;
+  a.gK[o] += gk;
+}
+
+}  // namespace adj
+}  // namespace vg
+
+using namespace vg;
+
+extern "C" size_t vg_isoneutral_step_adjoint_scratch_bytes(const VgDomain *dom) {
+  if (validate_domain(dom)) return 0;
+  return adj::scratch_bytes(layout_of(dom));
+}
+
+extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                              const VgAdjointFields *f, void *scratch, size_t scratch_bytes,
+                                              void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  if (!grid_complete(grid) || !set || !f || !f->temp || !f->salt || !f->temp_new || !f->salt_new || !f->K_iso ||
+      !f->mask_bits || !f->kbot || !f->gtemp_new || !f->gsalt_new || !f->gtemp || !f->gsalt || !f->gK_iso)
+    return fail(VG_ERR_ARG, "vg_isoneutral_step_adjoint_f64: NULL pointer argument");
+  if (!(set->iso_dslope > 0.0)) return fail(VG_ERR_ARG, "iso_dslope must be positive");
+  if (set->eq_of_state_type < 1 || set->eq_of_state_type > 4)
+    return fail(VG_ERR_ARG, "eq_of_state_type %d not supported", set->eq_of_state_type);
+  const Layout L = layout_of(dom);
+  const size_t need = adj::scratch_bytes(L);
+  if (!scratch || scratch_bytes < need)
+    return fail(VG_ERR_SCRATCH, "adjoint scratch of %zu bytes given, %zu needed", scratch_bytes, need);
+  if (L.Z > 200) return fail(VG_ERR_SHAPE, "Z=%d above the 200 levels supported", L.Z);
+  cudaStream_t s = as_stream(stream);
+  double *base = static_cast<double *>(scratch);
+  const long long F = (long long)adj::field_doubles(L);
+  double *tables = base + adj::kFields * F;
+  const adj::GridInv gi = adj::tables_of(L, tables);
+  const Grid g = grid_of(grid);
+
+  // 1. reciprocal grid tables
+  {
+    const int n = L.X > L.Y ? (L.X > L.Z ? L.X : L.Z) : (L.Y > L.Z ? L.Y : L.Z);
+    adj::adj_tables_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, g, tables);
+    if ((st = check_launch("adj_tables_kernel"))) return st;
+  }
+  // 2. the step's tensor
+  VgTensorFields ten;
+  ten.K_11 = base;
+  ten.K_22 = base + F;
+  ten.K_33 = base + 2 * F;
+  ten.Ai_ez = base + 3 * F;
+  ten.Ai_nz = base + 7 * F;
+  ten.Ai_bx = base + 11 * F;
+  ten.Ai_by = base + 15 * F;
+  ten.ai_stride_p = 2 * F;
+  ten.ai_stride_r = F;
+  if ((st = vg_isoneutral_pre_f64(dom, grid, set, f->temp, f->salt, f->K_iso, f->mask_bits, &ten, stream))) return st;
+  double *gTp = base + adj::F_GTP * F, *gSp = base + adj::F_GSP * F, *gK33 = base + adj::F_GK33 * F;
+  double *part = base + adj::F_PART * F;
+
+  // 3. implicit part
+  {
+    adj::ImpArgs a{L, gi, set->dt_tracer, f->kbot, ten.K_33, f->temp_new, f->salt_new, f->gtemp_new, f->gsalt_new,
+                   gTp, gSp, gK33};
+    int nb = 64;
+    size_t smem = 3 * (size_t)L.Z * nb * sizeof(double);
+    if (smem > 160 * 1024) {
+      nb = 32;
+      smem /= 2;
+    }
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(adj::adj_implicit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "adj_implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
+    }
+    const int ncols = L.X * L.Y;
+    adj::adj_implicit_kernel<<<(ncols + nb - 1) / nb, nb, smem, s>>>(a);
+    if ((st = check_launch("adj_implicit_kernel"))) return st;
+  }
+  const dim3 block(32, 4), grd((L.X + 31) / 32, (L.Y + 3) / 4, L.Z);
+  // 4. slope adjoints
+  {
+    adj::SlopeArgs a{L,          g,          gi,      set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
+                     set->K_iso_steep, set->dt_tracer, f->temp, f->salt, f->K_iso, gTp, gSp, gK33, f->mask_bits,
+                     part,       F};
+    adj::adj_slope_kernel<<<grd, block, 0, s>>>(a);
+    if ((st = check_launch("adj_slope_kernel"))) return st;
+  }
+  // 5. gather
+  {
+    adj::GatherArgs a{L,        g,        gi,           set->eq_of_state_type, set->dt_tracer, f->temp, gTp, gSp,
+                      ten.K_11, ten.K_22, f->mask_bits, part,                  F,              f->gtemp, f->gsalt,
+                      f->gK_iso};
+    adj::adj_gather_kernel<<<grd, block, 0, s>>>(a);
+    if ((st = check_launch("adj_gather_kernel"))) return st;
+  }
+  return VG_OK;
+}
