@@ -233,7 +233,7 @@ struct Ensemble : EnsembleBase {
     tun = t;
     int st = build_lists();
     if (st) return st;
-    smem_pre = t.pre_rows == 4 ? pre_smem_bytes<4>(maxZ) : pre_smem_bytes<8>(maxZ);
+    smem_pre = t.pre_rows == 4 ? pre_smem_bytes<F, 4>(maxZ) : pre_smem_bytes<F, 8>(maxZ);
     smem_flux = 2 * (size_t)maxZ * sizeof(double);
     smem_solve = ((size_t)maxZ + 3 * (size_t)maxZ * t.solve_threads) * sizeof(double);
     if (t.pre_rows == 4)

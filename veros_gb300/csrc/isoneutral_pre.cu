@@ -49,7 +49,7 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   while ((long long)nbx * nby * nchunks < 2 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
   a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
   const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
-  const size_t smem = pre_smem_bytes<TY>(a.L.Z);
+  const size_t smem = pre_smem_bytes<F, TY>(a.L.Z);
   cudaError_t e =
       cudaFuncSetAttribute(pre_tile_kernel<F, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_tile_kernel smem %zu: %s", smem, cudaGetErrorString(e));

@@ -12,6 +12,18 @@
 //   gradients min(0, drho/dz) - epsln that every slope divides by (:121, :158,
 //   :188, :207): one for the face below the point (kr = 0) and one above
 //   (kr = 1). Two planes (k and k+1) live in shared memory.
+// * Each slope is evaluated once. A slope belongs to a T point P, one of its
+//   horizontal faces h (east, west, north, south) and one of its vertical
+//   faces v (below, above): s = -(drdT(P) dT/dh + drdS(P) dS/dh) / R(P, v).
+//   The reference evaluates it twice, in the term of face h (Ai_ez/Ai_nz,
+//   K_11/K_22, :100-168) and in the term of face v (Ai_bx/Ai_by, K_33,
+//   :173-224), with the same operands. Here each thread computes the eight
+//   slopes and tapers of its own point per level and keeps them in
+//   registers for its own faces; the taper and taper*slope of its west and
+//   south slopes go to shared memory for the east/north faces of the
+//   neighbouring point. A ring column and row of the tile add 2 slopes per
+//   ring point. Slopes no face of the point uses (all their faces masked)
+//   are skipped.
 // * Grid divisions become multiplications by reciprocals computed once per
 //   CTA; slope divisions become multiplications by the shared reciprocals.
 // * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
@@ -66,19 +78,33 @@ struct PreArgs {
   int kchunk;
 };
 
-template <int TY>
+// slope index h * 2 + v: h = east, west, north, south face; v = face below, above
+enum { S_XE0, S_XE1, S_XW0, S_XW1, S_YN0, S_YN1, S_YS0, S_YS1, NS };
+// published per point: taper and taper*slope of the west and south slopes
+enum { PB_T_XW0, PB_T_XW1, PB_T_YS0, PB_T_YS1, PB_TS_XW0, PB_TS_XW1, PB_TS_YS0, PB_TS_YS1, NPB };
+constexpr unsigned kMaskWBelow = 0x10;  // in the plane mask byte: W mask of the level below
+
+template <typename F, int TY>
 struct Smem {
   static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
   double q[2][NQ][NP];
+  F pub[2][NPB][NP];
   double inv_dxu[PX], inv_dyu[PY], inv_cost[PY], facty[PY];
   double qinv_dxt[PX], qinv_dyt_cost[PY], dxu[PX];
+  uint8_t qm[2][NP];
   // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant
 };
 
-template <int TY>
+template <typename F, int TY>
 constexpr size_t pre_smem_bytes(int Z) {
-  return sizeof(Smem<TY>) + 4 * (size_t)Z * sizeof(double);
+  return sizeof(Smem<F, TY>) + 4 * (size_t)Z * sizeof(double);
 }
+
+template <typename F>
+struct Slope {
+  F t;       // taper
+  double s;  // slope
+};
 
 static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
   const double x = (slopec - fabs(s)) * inv_dslope;
@@ -132,7 +158,7 @@ __device__ __forceinline__ float sq_term<float>(float tp, float ai, double s) {
 // One tile (bx, by) and k-chunk bz of one domain; the whole CTA takes part.
 template <typename F, int TY>
 __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char *smem_raw, int bx, int by, int bz) {
-  using Sm = Smem<TY>;
+  using Sm = Smem<F, TY>;
   constexpr int TX = Tile<TY>::TX, NT = Tile<TY>::NT, PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
   constexpr int kPtSlots = Tile<TY>::kPtSlots;
   Sm &sm = *reinterpret_cast<Sm *>(smem_raw);
@@ -183,8 +209,12 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 
   // ---- per-point plane quantities ------------------------------------------
   double carryT[kPtSlots], carryS[kPtSlots];  // dT/dz, dS/dz of the previous level per point slot
+  unsigned carryW[kPtSlots];                  // W mask of the previous level per point slot
 #pragma unroll
-  for (int s = 0; s < kPtSlots; ++s) carryT[s] = carryS[s] = 0.0;
+  for (int s = 0; s < kPtSlots; ++s) {
+    carryT[s] = carryS[s] = 0.0;
+    carryW[s] = 0;
+  }
 
   auto compute_plane = [&](int lev, int buf, bool store) {
 #pragma unroll
@@ -195,9 +225,10 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       const int i = i0 - 1 + pi, j = j0 - 1 + pj;
       F rT = 0, rS = 0;
       double dTx = 0, dSx = 0, dTy = 0, dSy = 0, dTz = 0, dSz = 0;
+      unsigned mk = 0;
       if (i < L.X && j < L.Y) {
         const long long o = L.at(i, j, lev);
-        const unsigned mk = __ldg(a.m + o);
+        mk = __ldg(a.m + o);
         const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
         if (mk & VG_MASK_T) {
           const F Tf = F(Tc);
@@ -222,6 +253,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           dTz = (__ldg(a.T + o + L.plane) - Tc) * zinv_dzw[lev];
           dSz = (__ldg(a.S + o + L.plane) - Sc) * zinv_dzw[lev];
         }
+        if (lev >= Z - 1) mk &= ~(unsigned)VG_MASK_W;  // no face above the top level
       }
       if (store) {
         // vertical density gradients in FP64 (exact products of the split form's FP32 values)
@@ -236,31 +268,90 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         q[Q_SY][p] = dSy;
         q[Q_R0][p] = 1.0 / (fmin(0.0, G0) - kEpsln);
         q[Q_R1][p] = 1.0 / (fmin(0.0, G1) - kEpsln);
+        sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
       carryS[s] = dSz;
+      carryW[s] = mk & VG_MASK_W;
     }
   };
 
-  if (kb > 0) compute_plane(kb - 1, 0, false);  // only the carries
+  // slope (h, v) of plane point p: isoneutral.py:118-122, :155-159, :187-189, :205-207
+  auto slope_of = [&](const double(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
+    if (!need) return Slope<F>{F(0), 0.0};
+    const int pg = (h == 0 || h == 2) ? p : (h == 1 ? p - 1 : p - PX);
+    const int qT = h < 2 ? Q_TX : Q_TY, qS = h < 2 ? Q_SX : Q_SY;
+    const double s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
+    return Slope<F>{taper_t<F>(s, a.slopec, a.inv_dslope), s};
+  };
+
+  const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
+  // ring point whose west (east ring column) or south (north ring row) slopes this thread publishes
+  int pring = -1, hring = 0;
+  if (tid < TX) {
+    pring = (TY + 1) * PX + tid + 1;
+    hring = 3;
+  } else if (tid < TX + TY) {
+    pring = (tid - TX + 1) * PX + TX + 1;
+    hring = 1;
+  }
+
+  // the eight slopes of the own point at level lev; publishes its west/south slopes and the ring's
+  auto slopes_level = [&](int lev, int b, Slope<F> *out) {
+    const double(*q)[NP] = sm.q[b];
+    const uint8_t *qm = sm.qm[b];
+    F(*pb)[NP] = sm.pub[b];
+    const unsigned m = qm[pc];
+    const bool mH[4] = {(m & VG_MASK_U) != 0, (qm[pc - 1] & VG_MASK_U) != 0, (m & VG_MASK_V) != 0,
+                        (qm[pc - PX] & VG_MASK_V) != 0};
+    const bool mWv[2] = {(m & kMaskWBelow) != 0, (m & VG_MASK_W) != 0};
+#pragma unroll
+    for (int h = 0; h < 4; ++h)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) out[h * 2 + v] = slope_of(q, pc, h, v, (v == 1 || lev > 0) && (mH[h] || mWv[v]));
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      pb[PB_T_XW0 + v][pc] = out[S_XW0 + v].t;
+      pb[PB_TS_XW0 + v][pc] = out[S_XW0 + v].t * F(out[S_XW0 + v].s);
+      pb[PB_T_YS0 + v][pc] = out[S_YS0 + v].t;
+      pb[PB_TS_YS0 + v][pc] = out[S_YS0 + v].t * F(out[S_YS0 + v].s);
+    }
+    if (pring >= 0) {
+      const bool mHr = hring == 1 ? (qm[pring - 1] & VG_MASK_U) != 0 : (qm[pring - PX] & VG_MASK_V) != 0;
+      const int base_t = hring == 1 ? PB_T_XW0 : PB_T_YS0, base_ts = hring == 1 ? PB_TS_XW0 : PB_TS_YS0;
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const Slope<F> sl = slope_of(q, pring, hring, v, mHr && (v == 1 || lev > 0));
+        pb[base_t + v][pring] = sl.t;
+        pb[base_ts + v][pring] = sl.t * F(sl.s);
+      }
+    }
+  };
+
+  if (kb > 0) compute_plane(kb - 1, (kb - 1) & 1, false);  // only the carries
   compute_plane(kb, kb & 1, true);
+  __syncthreads();
+  Slope<F> cur[NS], nxt[NS];
+#pragma unroll
+  for (int n = 0; n < NS; ++n) nxt[n] = Slope<F>{F(0), 0.0};
+  slopes_level(kb, kb & 1, cur);
 
   const int i = i0 + tx, j = j0 + ty;
-  const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
   const bool east = i < L.X - 2 && j >= 2 && j < L.Y - 2;
   const bool north = i >= 2 && i < L.X - 2 && j < L.Y - 2;
   const bool top = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
 
   for (int k = kb; k < ke; ++k) {
     if (k + 1 < Z) compute_plane(k + 1, (k + 1) & 1, true);
+    // plane k+1 complete; the slopes of level k published; nobody still reads the buffers rewritten next
     __syncthreads();
-    const double(*q)[NP] = sm.q[k & 1];
-    const double(*qn)[NP] = sm.q[(k + 1) & 1];
+    if (k + 1 < Z) slopes_level(k + 1, (k + 1) & 1, nxt);
+    const F(*pb)[NP] = sm.pub[k & 1];
     const long long o = L.at(i, j, k);
     unsigned mk = 0;
-    if (east || north) mk = __ldg(a.m + o);
+    if (east || north || top) mk = __ldg(a.m + o);
 
-    // east face: Ai_ez, K_11 (isoneutral.py:100-132)
+    // east face: Ai_ez, K_11 (isoneutral.py:100-132); ip = 0 is this point, ip = 1 the east neighbour
     if (east) {
       F sumz = 0.0;
       if (mk & VG_MASK_U) {
@@ -270,18 +361,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                                __ldg(a.K + o + 1 - L.plane));
         else
           diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + 1));
-        const double dTx = q[Q_TX][pc], dSx = q[Q_SX][pc];
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
-#pragma unroll
-          for (int ip = 0; ip < 2; ++ip) {
-            const int pp = pc + ip;
-            const double s = -(q[Q_RT][pp] * dTx + q[Q_RS][pp] * dSx) * q[kr ? Q_R1 : Q_R0][pp];
-            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
-            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
-            a.Aez[o + ip * a.sp + kr * a.sr] = tp * F(s);
-          }
+          const F t0 = cur[S_XE0 + kr].t, t1 = pb[PB_T_XW0 + kr][pc + 1];
+          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t0);
+          a.Aez[o + kr * a.sr] = t0 * F(cur[S_XE0 + kr].s);
+          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t1);
+          a.Aez[o + a.sp + kr * a.sr] = pb[PB_TS_XW0 + kr][pc + 1];
         }
       } else {
 #pragma unroll
@@ -294,7 +381,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       a.K11[o] = sumz * F(zq_dzt[k]);
     }
 
-    // north face: Ai_nz, K_22 (isoneutral.py:137-168)
+    // north face: Ai_nz, K_22 (isoneutral.py:137-168); jp = 0 is this point, jp = 1 the north neighbour
     if (north) {
       F sumz = 0.0;
       if (mk & VG_MASK_V) {
@@ -304,18 +391,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                                __ldg(a.K + o + L.pitch - L.plane));
         else
           diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
-        const double dTy = q[Q_TY][pc], dSy = q[Q_SY][pc];
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
-#pragma unroll
-          for (int jp = 0; jp < 2; ++jp) {
-            const int pp = pc + jp * PX;
-            const double s = -(q[Q_RT][pp] * dTy + q[Q_RS][pp] * dSy) * q[kr ? Q_R1 : Q_R0][pp];
-            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
-            sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * tp);
-            a.Anz[o + jp * a.sp + kr * a.sr] = tp * F(s);
-          }
+          const F t0 = cur[S_YN0 + kr].t, t1 = pb[PB_T_YS0 + kr][pc + PX];
+          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t0);
+          a.Anz[o + kr * a.sr] = t0 * F(cur[S_YN0 + kr].s);
+          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t1);
+          a.Anz[o + a.sp + kr * a.sr] = pb[PB_TS_YS0 + kr][pc + PX];
         }
       } else {
 #pragma unroll
@@ -328,34 +411,28 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       a.K22[o] = sumz * F(zq_dzt[k]);
     }
 
-    // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224)
+    // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224); kr = 0 is this point's upper slopes,
+    // kr = 1 the lower slopes of the point above
     if (top && k < Z - 1) {
       F sumx = 0.0, sumy = 0.0;
       if (mk & VG_MASK_W) {
         const F Kc = __ldg(a.K + o);
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
-          const double(*qq)[NP] = kr ? qn : q;
-          const double rT = qq[Q_RT][pc], rS = qq[Q_RS][pc];
-          const double Rz = kr ? qn[Q_R0][pc] : q[Q_R1][pc];
 #pragma unroll
           for (int ip = 0; ip < 2; ++ip) {
-            const int pp = pc - 1 + ip;
-            const double s = -(rT * qq[Q_TX][pp] + rS * qq[Q_SX][pp]) * Rz;
-            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
-            const F ai = tp * F(s);
+            const Slope<F> sl = kr == 0 ? cur[ip ? S_XE1 : S_XW1] : nxt[ip ? S_XE0 : S_XW0];
+            const F ai = sl.t * F(sl.s);
             // FP64: dxu*K*taper*s^2 in the reference's order; split: (taper*s)*s, which stays
             // finite where an FP32 s^2 would overflow under a vanishing taper
-            sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(tp, ai, s);
+            sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(sl.t, ai, sl.s);
             a.Abx[o + ip * a.sp + kr * a.sr] = ai;
           }
 #pragma unroll
           for (int jp = 0; jp < 2; ++jp) {
-            const int pp = pc - PX + jp * PX;
-            const double s = -(rT * qq[Q_TY][pp] + rS * qq[Q_SY][pp]) * Rz;
-            const F tp = taper_t<F>(s, a.slopec, a.inv_dslope);
-            const F ai = tp * F(s);
-            sumy += F(sm.facty[ty + jp]) * Kc * sq_term<F>(tp, ai, s);
+            const Slope<F> sl = kr == 0 ? cur[jp ? S_YN1 : S_YS1] : nxt[jp ? S_YN0 : S_YS0];
+            const F ai = sl.t * F(sl.s);
+            sumy += F(sm.facty[ty + jp]) * Kc * sq_term<F>(sl.t, ai, sl.s);
             a.Aby[o + jp * a.sp + kr * a.sr] = ai;
           }
         }
@@ -369,7 +446,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       }
       a.K33[o] = sumx * F(sm.qinv_dxt[tx + 1]) + sumy * F(sm.qinv_dyt_cost[ty + 1]);
     }
-    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < NS; ++n) cur[n] = nxt[n];
   }
 }
 
