@@ -130,7 +130,7 @@ class IsoneutralAdjoint:
         return T, S
 
     # launches per forward and backward step (for launch accounting)
-    forward_launches = 1 + 1 + 2
+    forward_launches = 1 + 1 + 1 + 1  # prepare, pre, flux (temp and salt), implicit
     backward_launches = 5
 
 

@@ -68,87 +68,125 @@ static __device__ __forceinline__ double mul_(double x, double y) { return rmul(
 static __device__ __forceinline__ float add_(float x, float y) { return x + y; }
 static __device__ __forceinline__ float mul_(float x, float y) { return x * y; }
 
-// east-face flux at cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
+// Multiplies and fused multiply-adds with their rounding fixed in the source,
+// so that every instantiation of a flux (one tracer, two tracers, batched)
+// performs the same operations whatever the compiler would contract.
+static __device__ __forceinline__ double pm(double x, double y) { return __dmul_rn(x, y); }
+static __device__ __forceinline__ float pm(float x, float y) { return __fmul_rn(x, y); }
+static __device__ __forceinline__ double pfma(double x, double y, double z) { return __fma_rn(x, y, z); }
+static __device__ __forceinline__ float pfma(float x, float y, float z) { return __fmaf_rn(x, y, z); }
+
+// Face fluxes, split into the coefficients a face's tracers share (diffloc
+// times the slope components, the K_11/K_22 factor) and the per-tracer
+// differences, so that temp and salt diffused together load and multiply the
+// tensor once. Operand order per tracer is the reference's.
+
+// east face of cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
 template <typename F>
-__device__ __forceinline__ F flux_east(const DiffArgs<F> &a, int i, int j, int k, F inv_cost_dxu, F q_dzt) {
+__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int k, F c[5]) {
   const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
-  const int Z = L.Z;
+  const F s1 = F(a.s1);  // +-1: s1 * (sum) equals the sum of s1 * K
+  F diffloc;
+  if (k >= 1)
+    diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + 1) + ld(a.K, o + 1 - L.plane)));
+  else
+    diffloc = F(0.5) * (s1 * (ld(a.K, o) + ld(a.K, o + 1)));
+  c[0] = pm(diffloc, ld(a.Aez, o));
+  c[1] = pm(diffloc, ld(a.Aez, o + a.sp));
+  c[2] = pm(diffloc, ld(a.Aez, o + a.sr));
+  c[3] = pm(diffloc, ld(a.Aez, o + a.sp + a.sr));
+  c[4] = ld(a.K11, o);
+}
+
+template <typename F>
+__device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long long o, int k, const F c[5],
+                                       F inv_cost_dxu, F q_dzt) {
   const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
-  const long long dp = k < Z - 1 ? L.plane : 0;
-  const F s1 = F(a.s1);
-  F diffloc;
-  if (k >= 1)
-    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + 1) +
-                         s1 * ld(a.K, o + 1 - L.plane));
-  else
-    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + 1));
-  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + 1);
-  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + 1 - dm);
-  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + 1 + dp);
-  F sumz = 0.0;
-  sumz += diffloc * ld(a.Aez, o) * F(t0 - t0m);
-  sumz += diffloc * ld(a.Aez, o + a.sp) * F(t1 - t1m);
-  sumz += diffloc * ld(a.Aez, o + a.sr) * F(t0p - t0);
-  sumz += diffloc * ld(a.Aez, o + a.sp + a.sr) * F(t1p - t1);
-  return sumz * q_dzt + F(t1 - t0) * inv_cost_dxu * ld(a.K11, o);
+  const long long dp = k < L.Z - 1 ? L.plane : 0;
+  const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + 1);
+  const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + 1 - dm);
+  const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + 1 + dp);
+  F sumz = pm(c[0], F(t0 - t0m));
+  sumz = pfma(c[1], F(t1 - t1m), sumz);
+  sumz = pfma(c[2], F(t0p - t0), sumz);
+  sumz = pfma(c[3], F(t1p - t1), sumz);
+  return pfma(sumz, q_dzt, pm(pm(F(t1 - t0), inv_cost_dxu), c[4]));
 }
 
-// north-face flux at cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
+// north face of cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
 template <typename F>
-__device__ __forceinline__ F flux_north(const DiffArgs<F> &a, int i, int j, int k, F cosu, F inv_dyu, F q_dzt) {
+__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, int k, F c[5]) {
   const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
   const long long P = L.pitch;
-  const int Z = L.Z;
-  const long long dm = k > 0 ? L.plane : 0;
-  const long long dp = k < Z - 1 ? L.plane : 0;
   const F s1 = F(a.s1);
   F diffloc;
   if (k >= 1)
-    diffloc = F(0.25) * (s1 * ld(a.K, o) + s1 * ld(a.K, o - L.plane) + s1 * ld(a.K, o + P) +
-                         s1 * ld(a.K, o + P - L.plane));
+    diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + P) + ld(a.K, o + P - L.plane)));
   else
-    diffloc = F(0.5) * (s1 * ld(a.K, o) + s1 * ld(a.K, o + P));
-  const double t0 = ld(a.tr, o), t1 = ld(a.tr, o + P);
-  const double t0m = ld(a.tr, o - dm), t1m = ld(a.tr, o + P - dm);
-  const double t0p = ld(a.tr, o + dp), t1p = ld(a.tr, o + P + dp);
-  F sumz = 0.0;
-  sumz += diffloc * ld(a.Anz, o) * F(t0 - t0m);
-  sumz += diffloc * ld(a.Anz, o + a.sp) * F(t1 - t1m);
-  sumz += diffloc * ld(a.Anz, o + a.sr) * F(t0p - t0);
-  sumz += diffloc * ld(a.Anz, o + a.sp + a.sr) * F(t1p - t1);
-  return cosu * (sumz * q_dzt + F(t1 - t0) * inv_dyu * ld(a.K22, o));
+    diffloc = F(0.5) * (s1 * (ld(a.K, o) + ld(a.K, o + P)));
+  c[0] = pm(diffloc, ld(a.Anz, o));
+  c[1] = pm(diffloc, ld(a.Anz, o + a.sp));
+  c[2] = pm(diffloc, ld(a.Anz, o + a.sr));
+  c[3] = pm(diffloc, ld(a.Anz, o + a.sp + a.sr));
+  c[4] = ld(a.K22, o);
 }
 
-// top-face flux at interior cell (i, j, k < Z-1) (diffusion.py:85-111)
 template <typename F>
-__device__ __forceinline__ F flux_top(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F q_dxt,
-                                      F q_dyt_cost) {
-  const Layout &L = a.L;
-  const long long P = L.pitch, Q = L.plane;
-  const F diffloc = F(a.s2) * ld(a.K, o);
-  const double tc = ld(a.tr, o), tcu = ld(a.tr, o + Q);
-  F sumx = 0.0;
-  sumx += diffloc * ld(a.Abx, o) * inv_cost * F(tc - ld(a.tr, o - 1));
-  sumx += diffloc * ld(a.Abx, o + a.sr) * inv_cost * F(tcu - ld(a.tr, o - 1 + Q));
-  sumx += diffloc * ld(a.Abx, o + a.sp) * inv_cost * F(ld(a.tr, o + 1) - tc);
-  sumx += diffloc * ld(a.Abx, o + a.sp + a.sr) * inv_cost * F(ld(a.tr, o + 1 + Q) - tcu);
-  F sumy = 0.0;
-  sumy += diffloc * ld(a.Aby, o) * cosu_s * F(tc - ld(a.tr, o - P));
-  sumy += diffloc * ld(a.Aby, o + a.sr) * cosu_s * F(tcu - ld(a.tr, o - P + Q));
-  sumy += diffloc * ld(a.Aby, o + a.sp) * cosu_c * F(ld(a.tr, o + P) - tc);
-  sumy += diffloc * ld(a.Aby, o + a.sp + a.sr) * cosu_c * F(ld(a.tr, o + P + Q) - tcu);
-  return sumx * q_dxt + sumy * q_dyt_cost;
+__device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long long o, int k, const F c[5], F cosu,
+                                        F inv_dyu, F q_dzt) {
+  const long long P = L.pitch;
+  const long long dm = k > 0 ? L.plane : 0;
+  const long long dp = k < L.Z - 1 ? L.plane : 0;
+  const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + P);
+  const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + P - dm);
+  const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + P + dp);
+  F sumz = pm(c[0], F(t0 - t0m));
+  sumz = pfma(c[1], F(t1 - t1m), sumz);
+  sumz = pfma(c[2], F(t0p - t0), sumz);
+  sumz = pfma(c[3], F(t1p - t1), sumz);
+  return pm(cosu, pfma(sumz, q_dzt, pm(pm(F(t1 - t0), inv_dyu), c[4])));
 }
 
-// One tile (bx, by) and k-chunk bz of one tracer of one domain; the whole CTA
-// (32 x TY threads) takes part. zq_dzt: dynamic shared memory of 2 Z doubles.
-template <typename F, int TY>
-__device__ __forceinline__ void flux_div_body(const DiffArgs<F> &a, double *zq_dzt, int bx, int by, int bz) {
+// top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111)
+template <typename F>
+__device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F c[8]) {
+  const F diffloc = F(a.s2) * ld(a.K, o);
+  c[0] = pm(pm(diffloc, ld(a.Abx, o)), inv_cost);
+  c[1] = pm(pm(diffloc, ld(a.Abx, o + a.sr)), inv_cost);
+  c[2] = pm(pm(diffloc, ld(a.Abx, o + a.sp)), inv_cost);
+  c[3] = pm(pm(diffloc, ld(a.Abx, o + a.sp + a.sr)), inv_cost);
+  c[4] = pm(pm(diffloc, ld(a.Aby, o)), cosu_s);
+  c[5] = pm(pm(diffloc, ld(a.Aby, o + a.sr)), cosu_s);
+  c[6] = pm(pm(diffloc, ld(a.Aby, o + a.sp)), cosu_c);
+  c[7] = pm(pm(diffloc, ld(a.Aby, o + a.sp + a.sr)), cosu_c);
+}
+
+template <typename F>
+__device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long long o, const F c[8], F q_dxt,
+                                      F q_dyt_cost) {
+  const long long P = L.pitch, Q = L.plane;
+  const double tc = __ldg(tr + o), tcu = __ldg(tr + o + Q);
+  F sumx = pm(c[0], F(tc - __ldg(tr + o - 1)));
+  sumx = pfma(c[1], F(tcu - __ldg(tr + o - 1 + Q)), sumx);
+  sumx = pfma(c[2], F(__ldg(tr + o + 1) - tc), sumx);
+  sumx = pfma(c[3], F(__ldg(tr + o + 1 + Q) - tcu), sumx);
+  F sumy = pm(c[4], F(tc - __ldg(tr + o - P)));
+  sumy = pfma(c[5], F(tcu - __ldg(tr + o - P + Q)), sumy);
+  sumy = pfma(c[6], F(__ldg(tr + o + P) - tc), sumy);
+  sumy = pfma(c[7], F(__ldg(tr + o + P + Q) - tcu), sumy);
+  return pfma(sumx, q_dxt, pm(sumy, q_dyt_cost));
+}
+
+// One tile (bx, by) and k-chunk bz of NTR tracers of one domain; the whole CTA
+// (32 x TY threads) takes part. A[0..NTR-1] differ only in their tracer
+// fields; geometry, tensor and masks come from A[0]. zq_dzt: dynamic shared
+// memory of 2 Z doubles.
+template <typename F, int TY, int NTR>
+__device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_dzt, int bx, int by, int bz) {
   constexpr int NT = TX * TY;
-  __shared__ F fe_s[2][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
-  __shared__ F fn_s[2][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
+  __shared__ F fe_s[2][NTR][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
+  __shared__ F fn_s[2][NTR][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
+  const DiffArgs<F> &a = A[0];
   const Layout &L = a.L;
   const int Z = L.Z;
   double *zinv_dzt = zq_dzt + Z;  // 1/(4 dzt[k]) then 1/dzt[k]
@@ -185,51 +223,96 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> &a, double *zq_d
   }
   if (halo_e) h_inv_cost_dxu = F(1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]));
 
-  F ft_prev = 0.0;
-  if (own && kb > 0) ft_prev = flux_top(a, L.at(i, j, kb - 1), inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
+  F ft_prev[NTR];
+#pragma unroll
+  for (int r = 0; r < NTR; ++r) ft_prev[r] = 0.0;
+  if (own && kb > 0) {
+    const long long ob = L.at(i, j, kb - 1);
+    F ct[8];
+    top_coef(a, ob, inv_cost, cosu_s, cosu_c, ct);
+#pragma unroll
+    for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, ob, ct, q_dxt, q_dyt_cost);
+  }
 
   for (int k = kb; k < ke; ++k) {
     // double-buffered exchange: the barrier of level k+1 orders level k's
     // reads before level k+2's writes to the same buffer
     const int b = k & 1;
     const long long o = L.at(i, j, k);
-    F fe = 0, fn = 0, ft = 0;
+    const F qz = F(zq_dzt[k]);
+    F fe[NTR], fn[NTR], ft[NTR];
+#pragma unroll
+    for (int r = 0; r < NTR; ++r) fe[r] = fn[r] = ft[r] = 0.0;
     if (own) {
-      fe = flux_east(a, i, j, k, inv_cost_dxu, F(zq_dzt[k]));
-      fn = flux_north(a, i, j, k, cosu_c, inv_dyu, F(zq_dzt[k]));
-      if (k < Z - 1) ft = flux_top(a, o, inv_cost, cosu_s, cosu_c, q_dxt, q_dyt_cost);
-      fe_s[b][ty][tx + 1] = fe;
-      fn_s[b][ty + 1][tx] = fn;
+      F ce[5], cn[5];
+      east_coef(a, o, k, ce);
+      north_coef(a, o, k, cn);
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        fe[r] = east_flux(L, A[r].tr, o, k, ce, inv_cost_dxu, qz);
+        fn[r] = north_flux(L, A[r].tr, o, k, cn, cosu_c, inv_dyu, qz);
+      }
+      if (k < Z - 1) {
+        F ct[8];
+        top_coef(a, o, inv_cost, cosu_s, cosu_c, ct);
+#pragma unroll
+        for (int r = 0; r < NTR; ++r) ft[r] = top_flux(L, A[r].tr, o, ct, q_dxt, q_dyt_cost);
+      }
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        fe_s[b][r][ty][tx + 1] = fe[r];
+        fn_s[b][r][ty + 1][tx] = fn[r];
+      }
     }
-    if (halo_n) fn_s[b][0][lane] = flux_north(a, hi_n, j0 - 1, k, h_cosu, h_inv_dyu, F(zq_dzt[k]));
-    if (halo_e) fe_s[b][lane][0] = flux_east(a, i0 - 1, hj_e, k, h_inv_cost_dxu, F(zq_dzt[k]));
+    if (halo_n) {
+      const long long oh = L.at(hi_n, j0 - 1, k);
+      F cn[5];
+      north_coef(a, oh, k, cn);
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu, h_inv_dyu, qz);
+    }
+    if (halo_e) {
+      const long long oh = L.at(i0 - 1, hj_e, k);
+      F ce[5];
+      east_coef(a, oh, k, ce);
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce, h_inv_cost_dxu, qz);
+    }
     __syncthreads();
     if (own) {
       const F mT = (__ldg(a.m + o) & VG_MASK_T) ? F(1.0) : F(0.0);
-      F e = mT * ((fe - fe_s[b][ty][tx]) * inv_fx + (fn - fn_s[b][ty][tx]) * inv_fy);
-      e = e + mT * (ft - ft_prev) * F(zinv_dzt[k]);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
-      ft_prev = ft;
-      a.dtr_iso[o] = add_(a.dtr_iso[o], e);
-      a.trp[o] = radd(a.trp[o], rmul(a.dt, (double)e));
-      if (a.save_fluxes) {
-        a.fe[o] = fe;
-        a.fn[o] = fn;
-        a.ft[o] = ft;
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        const DiffArgs<F> &t = A[r];
+        F e = pm(mT, pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy)));
+        e = pfma(pm(mT, ft[r] - ft_prev[r]), F(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
+        ft_prev[r] = ft[r];
+        t.dtr_iso[o] = add_(t.dtr_iso[o], e);
+        t.trp[o] = radd(t.trp[o], rmul(t.dt, (double)e));
+        if (t.save_fluxes) {
+          t.fe[o] = fe[r];
+          t.fn[o] = fn[r];
+          t.ft[o] = ft[r];
+        }
       }
     }
-    if (a.save_fluxes) {
-      if (halo_n) a.fn[L.at(hi_n, j0 - 1, k)] = fn_s[b][0][lane];
-      if (halo_e) a.fe[L.at(i0 - 1, hj_e, k)] = fe_s[b][lane][0];
+#pragma unroll
+    for (int r = 0; r < NTR; ++r) {
+      if (A[r].save_fluxes) {
+        if (halo_n) A[r].fn[L.at(hi_n, j0 - 1, k)] = fn_s[b][r][0][lane];
+        if (halo_e) A[r].fe[L.at(i0 - 1, hj_e, k)] = fe_s[b][r][lane][0];
+      }
     }
   }
   // the tile's exchange buffers are reused by the next tile a persistent CTA takes
   __syncthreads();
 }
 
-template <typename F, int TY>
-__global__ void __launch_bounds__(TX * TY, 2) flux_div_kernel(DiffArgs<F> a) {
+template <typename F, int TY, int NTR>
+__global__ void __launch_bounds__(TX * TY, 2) flux_div_kernel(DiffArgs<F> a, DiffArgs<F> b) {
   extern __shared__ double zq_dzt[];
-  flux_div_body<F, TY>(a, zq_dzt, blockIdx.x, blockIdx.y, blockIdx.z);
+  const DiffArgs<F> A[2] = {a, b};
+  flux_div_body<F, TY, NTR>(A, zq_dzt, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Implicit solve of NRHS tracers sharing one matrix, one thread per column.
@@ -243,7 +326,8 @@ __global__ void __launch_bounds__(TX * TY, 2) flux_div_kernel(DiffArgs<F> a) {
 // The solve of one column (i, j) whose water starts at level ks.
 template <typename F, int NRHS>
 __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const DiffArgs<F> &b2, const double *dtdzw,
-                                                double *cps, double *dps, int t, int nb, int i, int j, int ks) {
+                                                const double *inv_dzt, double *cps, double *dps, int t, int nb,
+                                                int i, int j, int ks) {
   const Layout &L = a.L;
   const int Z = L.Z;
   const long long base = L.at2(i, j);
@@ -263,6 +347,8 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
 #pragma unroll
     for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? (double)trp[r][o] : 0.0;
   }
+  // Thomas elimination of the system of diffusion.py:152-164 with one
+  // reciprocal per level: the matrix entries use the per-level 1/dzt table
   double delta_prev = 0.0, cp = 0.0, dp[NRHS];
 #pragma unroll
   for (int r = 0; r < NRHS; ++r) dp[r] = 0.0;
@@ -271,8 +357,8 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
     for (int u = 0; u < PF; ++u) {
       const int k = k0 + u;
       if (k < Z) {
-        const double dzt = a.g.dzt[k];
-        const double delta = k < Z - 1 ? rmul(dtdzw[k], qK[u]) : 0.0;
+        const double idzt = inv_dzt[k];
+        const double delta = k < Z - 1 ? pm(dtdzw[k], qK[u]) : 0.0;
         double tr1[NRHS];
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) tr1[r] = qT[u][r];
@@ -284,15 +370,15 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
 #pragma unroll
           for (int r = 0; r < NRHS; ++r) qT[u][r] = (double)trp[r][on];
         }
-        const double ak = k == ks ? 0.0 : rdiv(-delta_prev, dzt);  // a_tri, zero at the edge (operators.py:72)
-        const double bk = k == ks ? radd(1.0, rdiv(delta, dzt)) : radd(1.0, rdiv(radd(delta, delta_prev), dzt));
-        const double ck = k < Z - 1 ? rdiv(-delta, dzt) : 0.0;
-        const double den = 1.0 / (bk - ak * cp);
-        cp = ck * den;
+        const double ak = k == ks ? 0.0 : pm(-delta_prev, idzt);  // a_tri, zero at the edge (operators.py:72)
+        const double bk = pfma(k == ks ? delta : delta + delta_prev, idzt, 1.0);  // b_tri, b_tri_edge at ks
+        const double ck = pm(-delta, idzt);                                      // c_tri (0 on the top level)
+        const double den = 1.0 / pfma(-ak, cp, bk);
+        cp = pm(ck, den);
         cps[(size_t)k * nb + t] = cp;
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
-          dp[r] = (tr1[r] - ak * dp[r]) * den;
+          dp[r] = pm(pfma(-ak, dp[r], tr1[r]), den);
           dps[((size_t)r * Z + k) * nb + t] = dp[r];
         }
         delta_prev = delta;
@@ -326,9 +412,9 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         const double c = cps[(size_t)k * nb + t];
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
-          x[r] = dps[((size_t)r * Z + k) * nb + t] - c * x[r];
+          x[r] = pfma(-c, x[r], dps[((size_t)r * Z + k) * nb + t]);
           trp[r][o] = x[r];
-          dtr[r][o] = F(d1[u][r] + (x[r] - t1[u][r]) * inv_dt);  // diffusion.py:204
+          dtr[r][o] = F(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
         }
       }
     }
@@ -344,15 +430,19 @@ __device__ __forceinline__ void implicit_body(const DiffArgs<F> &a, const DiffAr
   const int ncols_x = L.X - 4, ncols = ncols_x * (L.Y - 4);
   const int t = threadIdx.x, nb = blockDim.x;
   double *dtdzw = smem;
-  double *cps = smem + Z;
+  double *inv_dzt = smem + Z;
+  double *cps = smem + 2 * Z;
   double *dps = cps + (size_t)Z * nb;  // [r][k][thread]
-  for (int k = t; k < Z; k += nb) dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
+  for (int k = t; k < Z; k += nb) {
+    dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
+    inv_dzt[k] = 1.0 / a.g.dzt[k];
+  }
   __syncthreads();
   const int col = cb * nb + t;
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
   const int ks = col < ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
-  if (ks >= 0 && ks < Z) implicit_column<F, NRHS>(a, b2, dtdzw, cps, dps, t, nb, i, j, ks);
+  if (ks >= 0 && ks < Z) implicit_column<F, NRHS>(a, b2, dtdzw, inv_dzt, cps, dps, t, nb, i, j, ks);
   __syncthreads();  // dtdzw is refilled by the next block of columns a persistent CTA takes
 }
 

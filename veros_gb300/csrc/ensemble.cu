@@ -103,14 +103,14 @@ __global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *
                                                            const WorkItem *__restrict__ items, int nitems,
                                                            int *counter, int kchunk) {
   extern __shared__ double zq_dzt[];
-  __shared__ DiffArgs<F> a;
+  __shared__ DiffArgs<F> a[2];  // temp, salt
   WorkItem w;
   while (next_item(counter, nitems, items, w)) {
-    // item.member = 2 * member + tracer
-    stage(&a, (w.member & 1) ? &members[w.member >> 1].dS : &members[w.member >> 1].dT);
-    if (threadIdx.x == 0) a.kchunk = kchunk > 0 ? min(kchunk, a.L.Z) : a.L.Z;
+    stage(&a[0], &members[w.member].dT);
+    stage(&a[1], &members[w.member].dS);
+    if (threadIdx.x == 0) a[0].kchunk = a[1].kchunk = kchunk > 0 ? min(kchunk, a[0].L.Z) : a[0].L.Z;
     __syncthreads();
-    flux_div_body<F, TY>(a, zq_dzt, w.a, w.b, w.c);
+    flux_div_body<F, TY, 2>(a, zq_dzt, w.a, w.b, w.c);
   }
 }
 
@@ -192,10 +192,9 @@ struct Ensemble : EnsembleBase {
           for (int bx = 0; bx < pbx; ++bx) pre.push_back({m, bx, by, bz});
       const int fbx = (L.X - 4 + 31) / 32, fby = (L.Y - 4 + tun.flux_rows - 1) / tun.flux_rows;
       const int fbz = (L.Z + kc_flux - 1) / kc_flux;
-      for (int tr = 0; tr < 2; ++tr)
-        for (int bz = 0; bz < fbz; ++bz)
-          for (int by = 0; by < fby; ++by)
-            for (int bx = 0; bx < fbx; ++bx) flux.push_back({2 * m + tr, bx, by, bz});
+      for (int bz = 0; bz < fbz; ++bz)  // temp and salt of a tile in one item
+        for (int by = 0; by < fby; ++by)
+          for (int bx = 0; bx < fbx; ++bx) flux.push_back({m, bx, by, bz});
       const int ncols = (L.X - 4) * (L.Y - 4);
       for (int cb = 0; cb < (ncols + tun.solve_threads - 1) / tun.solve_threads; ++cb) solve.push_back({m, cb, 0, 0});
       for (int k = 0; k < L.Z; ++k) prep.push_back({m, 0, 0, k});
@@ -235,7 +234,7 @@ struct Ensemble : EnsembleBase {
     if (st) return st;
     smem_pre = t.pre_rows == 4 ? pre_smem_bytes<F, 4>(maxZ) : pre_smem_bytes<F, 8>(maxZ);
     smem_flux = 2 * (size_t)maxZ * sizeof(double);
-    smem_solve = ((size_t)maxZ + 3 * (size_t)maxZ * t.solve_threads) * sizeof(double);
+    smem_solve = (2 * (size_t)maxZ + 3 * (size_t)maxZ * t.solve_threads) * sizeof(double);
     if (t.pre_rows == 4)
       st = occupancy_grid(pre_batched<F, 4>, 128, smem_pre, grid_pre);
     else

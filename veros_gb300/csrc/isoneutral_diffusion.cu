@@ -12,16 +12,17 @@ extern "C" size_t vg_isoneutral_diffusion_scratch_bytes(const VgDomain *dom) {
 namespace vg {
 namespace {
 
-template <typename F>
-int launch_flux_div(DiffArgs<F> &a, cudaStream_t s) {
+// NTR = 2: temp and salt in one pass over the tensor (b: salt); NTR = 1: a alone
+template <typename F, int NTR>
+int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
   constexpr int TY = 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
   int nchunks = 1;
   while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
-  a.kchunk = (a.L.Z + nchunks - 1) / nchunks;
+  a.kchunk = b.kchunk = (a.L.Z + nchunks - 1) / nchunks;
   const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
   const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-  flux_div_kernel<F, TY><<<dim3(nbx, nby, nbz), TX * TY, smem, s>>>(a);
+  flux_div_kernel<F, TY, NTR><<<dim3(nbx, nby, nbz), TX * TY, smem, s>>>(a, b);
   return check_launch("flux_div_kernel");
 }
 
@@ -29,7 +30,7 @@ template <typename F, int NRHS>
 int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) {
   const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
   const int nb = 64;
-  const size_t smem = ((size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
+  const size_t smem = (2 * (size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e =
         cudaFuncSetAttribute(implicit_kernel<F, NRHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -61,7 +62,7 @@ int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *
   if ((st = make_diff_args(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, static_cast<F *>(scratch), a)))
     return st;
   cudaStream_t s = as_stream(stream);
-  if ((st = launch_flux_div(a, s))) return st;
+  if ((st = launch_flux_div<F, 1>(a, a, s))) return st;
   if (a.iso && (st = launch_implicit<F, 1>(a, a, s))) return st;
   if (a.save_fluxes && (st = launch_energy(a, s))) return st;
   return VG_OK;
@@ -83,8 +84,7 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
   if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
     return st;
   cudaStream_t s = as_stream(stream);
-  if ((st = launch_flux_div(aT, s))) return st;
-  if ((st = launch_flux_div(aS, s))) return st;
+  if ((st = launch_flux_div<F, 2>(aT, aS, s))) return st;
   if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
   if (aT.save_fluxes) {
     if ((st = launch_energy(aT, s))) return st;

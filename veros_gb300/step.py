@@ -114,7 +114,7 @@ class IsoneutralStepper:
         torch.cuda.current_stream(self.dev.device).synchronize()
 
     def launches_per_step(self):
-        """Kernels of this library one step enqueues: prepare, pre, two flux
-        kernels, one shared implicit solve and, with the energy branch, two
-        energy kernels."""
-        return 1 + 1 + 2 + 1 + (2 if self.dev.settings.enable_conserve_energy else 0)
+        """Kernels of this library one step enqueues: prepare, pre, one flux
+        kernel for temp and salt, one shared implicit solve and, with the
+        energy branch, two energy kernels."""
+        return 1 + 1 + 1 + 1 + (2 if self.dev.settings.enable_conserve_energy else 0)
