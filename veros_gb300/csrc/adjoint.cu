@@ -18,13 +18,15 @@
 //
 // Launches (one stream, in order):
 //   1. adj_tables_kernel     reciprocal grid factors
-//   2. pre_tile_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel)
+//   2. pre_tile_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel), and
+//                            per point its 8 tapers, 8 slopes and 2 clamped reciprocals
 //   3. adj_implicit_kernel   per water column: the transposed tridiagonal
 //                            system A^T y = dL/dx (one Thomas factorisation
 //                            for temp and salt) and dL/dK_33 from
 //                            dL/ddelta_k = (x_{k+1} - x_k)(y_k/dzt_k - y_{k+1}/dzt_{k+1})
-//   4. adj_slope_kernel      per point: the eight slope adjoints, written as
-//                            per-point partial sums onto the point's faces
+//   4. adj_slope_kernel      per point: the eight slope adjoints (from the stored
+//                            tapers and slopes), written as per-point partial
+//                            sums onto the point's faces
 //   5. adj_gather_kernel     per point: sums the partials of the faces around
 //                            it into dL/dT_n, dL/dS_n and dL/dK_iso
 //
@@ -37,7 +39,6 @@ namespace vg {
 namespace adj {
 
 using detail::kEpsln;
-using detail::taper_of;
 
 // reciprocal grid tables (scratch tail)
 struct GridInv {
@@ -50,7 +51,9 @@ constexpr int kTensorFields = 19;  // K_11, K_22, K_33, 4 x 4 Ai components
 enum { F_GTP = kTensorFields, F_GSP, F_GK33, F_PART };
 // partial sums written by the slope pass, one field each
 enum { P_LRT = 0, P_NSUM = 1, P_LG = 5, P_LVD = 7, P_LHD = 11, P_LDL = 19, P_LKW = 23, P_N = 25 };
-constexpr int kFields = F_PART + P_N;
+// the forward's per-point tapers, slopes and reciprocals (detail::SLOPE_*)
+constexpr int F_SLOPES = F_PART + P_N;
+constexpr int kFields = F_SLOPES + detail::SLOPE_FIELDS;
 
 inline size_t table_doubles(const Layout &L) { return 3 * (size_t)L.X + 4 * (size_t)L.Y + 3 * (size_t)L.Z; }
 
@@ -206,6 +209,7 @@ struct SlopeArgs {
   const double *__restrict__ gSp;
   const double *__restrict__ gK33;
   const uint8_t *__restrict__ m;
+  const double *__restrict__ slopes;  // the forward's tapers, slopes and reciprocals
   double *part;
   long long field;
 };
@@ -233,13 +237,8 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const bool hasE = i < X - 1, hasW = i > 0, hasN = j < Y - 1, hasS = j > 0, hasU = k < Z - 1, hasD = k > 0;
   const bool inter = i >= 2 && i < X - 2 && j >= 2 && j < Y - 2;
   const bool rowE = j >= 2 && j < Y - 2, colN = i >= 2 && i < X - 2;
-  const Eos eos{a.eos};
-
   const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
-  const bool wet = mk & VG_MASK_T;
-  const double rT = wet ? eos.drdT(Tc, a.g.zt[k]) : 0.0;
-  const double rS = wet ? eos.drdS() : 0.0;
-
+  const long long F = a.field;
   // tracer differences across the faces (unmasked) and the face masks
   double hdT[4], hdS[4], vdT[2], vdS[2];
   hdT[0] = hasE ? __ldg(a.T + o + 1) - Tc : 0.0;
@@ -258,35 +257,18 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
                       hasN && (mk & VG_MASK_V), hasS && (__ldg(m + o - PW) & VG_MASK_V)};
   const bool mWv[2] = {hasD && (__ldg(m + o - PL) & VG_MASK_W), hasU && (mk & VG_MASK_W)};
 
-  // face gradients (isoneutral.py:46-95)
+  // temperature gradients on the faces (isoneutral.py:46-95)
   const double icx = gi.inv_cost[j];
-  double gxT[4], gxS[4], gzT[2], gzS[2];
-  {
-    const double f0 = mH[0] ? gi.inv_dxu[i] * icx : 0.0;
-    const double f1 = mH[1] ? gi.inv_dxu[i - 1] * icx : 0.0;
-    const double f2 = mH[2] ? gi.inv_dyu[j] : 0.0;
-    const double f3 = mH[3] ? gi.inv_dyu[j - 1] : 0.0;
-    gxT[0] = hdT[0] * f0;
-    gxS[0] = hdS[0] * f0;
-    gxT[1] = hdT[1] * f1;
-    gxS[1] = hdS[1] * f1;
-    gxT[2] = hdT[2] * f2;
-    gxS[2] = hdS[2] * f2;
-    gxT[3] = hdT[3] * f3;
-    gxS[3] = hdS[3] * f3;
-    const double z0 = mWv[0] ? gi.inv_dzw[k - 1] : 0.0;
-    const double z1 = mWv[1] ? gi.inv_dzw[k] : 0.0;
-    gzT[0] = vdT[0] * z0;
-    gzS[0] = vdS[0] * z0;
-    gzT[1] = vdT[1] * z1;
-    gzS[1] = vdS[1] * z1;
-  }
-  double G[2], R[2];
-#pragma unroll
-  for (int v = 0; v < 2; ++v) {
-    G[v] = rT * gzT[v] + rS * gzS[v];
-    R[v] = 1.0 / (fmin(0.0, G[v]) - kEpsln);
-  }
+  double gxT[4], gzT[2];
+  gxT[0] = mH[0] ? hdT[0] * (gi.inv_dxu[i] * icx) : 0.0;
+  gxT[1] = mH[1] ? hdT[1] * (gi.inv_dxu[i - 1] * icx) : 0.0;
+  gxT[2] = mH[2] ? hdT[2] * gi.inv_dyu[j] : 0.0;
+  gxT[3] = mH[3] ? hdT[3] * gi.inv_dyu[j - 1] : 0.0;
+  gzT[0] = mWv[0] ? vdT[0] * gi.inv_dzw[k - 1] : 0.0;
+  gzT[1] = mWv[1] ? vdT[1] * gi.inv_dzw[k] : 0.0;
+  // the clamped reciprocals 1/(min(0, G) - epsln) of the forward; G >= 0 gives exactly R_flat
+  const double R_flat = 1.0 / (fmin(0.0, 0.0) - kEpsln);
+  const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
 
   // which faces carry a term: face h (east/north terms) and face v (top terms)
   const bool vE[4] = {rowE && i >= 1 && i < X - 2 && mH[0], rowE && i >= 2 && i < X - 1 && mH[1],
@@ -381,8 +363,8 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
       const bool Ef = vE[h] && (v == 1 || hasD);
       const bool Tf = vT[v];
       if (!Ef && !Tf) continue;
-      const double s = -(rT * gxT[h] + rS * gxS[h]) * R[v];
-      const double t = taper_of(s, a.slopec, a.inv_dslope);
+      const double s = __ldg(a.slopes + o + (detail::SLOPE_S + h * 2 + v) * F);
+      const double t = __ldg(a.slopes + o + (detail::SLOPE_T + h * 2 + v) * F);
       const double sg = (s > 0.0) ? 1.0 : (s < 0.0 ? -1.0 : 0.0);
       const double tp = -2.0 * sg * t * (1.0 - t) * a.inv_dslope;  // d taper / ds
       const double tst = t + s * tp;                              // d (taper s) / ds
@@ -409,7 +391,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
         lhd[1][h] += lftS[v] * f;
       }
       const double lN = -gs * R[v];
-      if (G[v] < 0.0) lG[v] -= gs * s * R[v];
+      if (R[v] != R_flat) lG[v] -= gs * s * R[v];  // d min(0, G)/dG = 1 where G < 0
       lrT += lN * gxT[h];
       nsum[h] += lN;
     }
@@ -417,7 +399,6 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   lrT += lG[0] * gzT[0] + lG[1] * gzT[1];
 
   double *p = a.part + o;
-  const long long F = a.field;
   p[P_LRT * F] = lrT;
 #pragma unroll
   for (int h = 0; h < 4; ++h) {
@@ -609,7 +590,9 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   ten.Ai_by = base + 15 * F;
   ten.ai_stride_p = 2 * F;
   ten.ai_stride_r = F;
-  if ((st = vg_isoneutral_pre_f64(dom, grid, set, f->temp, f->salt, f->K_iso, f->mask_bits, &ten, stream))) return st;
+  double *slopes = base + adj::F_SLOPES * F;
+  if ((st = pre_f64_with_slopes(dom, grid, set, f->temp, f->salt, f->K_iso, f->mask_bits, &ten, slopes, stream)))
+    return st;
   double *gTp = base + adj::F_GTP * F, *gSp = base + adj::F_GSP * F, *gK33 = base + adj::F_GK33 * F;
   double *part = base + adj::F_PART * F;
 
@@ -637,7 +620,7 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   {
     adj::SlopeArgs a{L,          g,          gi,      set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
                      set->K_iso_steep, set->dt_tracer, f->temp, f->salt, f->K_iso, gTp, gSp, gK33, f->mask_bits,
-                     part,       F};
+                     slopes,     part,       F};
     adj::adj_slope_kernel<<<grd, block, 0, s>>>(a);
     if ((st = check_launch("adj_slope_kernel"))) return st;
   }

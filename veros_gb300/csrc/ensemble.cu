@@ -315,6 +315,8 @@ int member_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *se
     a.sp = f.ten.ai_stride_p;
     a.sr = f.ten.ai_stride_r;
     a.kchunk = dom->Z;
+    a.slopes = nullptr;
+    a.slope_field = 0;
     Tr trT{f.temp_tau, f.temp_taup1, f.dtemp_iso, nullptr, nullptr};
     Tr trS{f.salt_tau, f.salt_taup1, f.dsalt_iso, nullptr, nullptr};
     // the diffusion argument builder of diffusion_kernels.cuh; no scratch without the energy branch

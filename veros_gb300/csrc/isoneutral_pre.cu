@@ -11,7 +11,7 @@ using namespace detail;
 template <typename F, typename Out>
 int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
                const double *salt_tau, const F *K_iso, const uint8_t *mask_bits, const Out *out, void *stream,
-               const char *name) {
+               const char *name, double *slopes = nullptr) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -42,6 +42,8 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   a.Aby = out->Ai_by;
   a.sp = out->ai_stride_p;
   a.sr = out->ai_stride_r;
+  a.slopes = slopes;
+  a.slope_field = (long long)a.L.plane * a.L.Z;
   // k-chunking: enough CTAs for two per SM on the 152 SMs of a GB300
   constexpr int TY = 8, TX = 32;
   const int nbx = (a.L.X - 3 + TX - 1) / TX, nby = (a.L.Y - 3 + TY - 1) / TY;
@@ -58,6 +60,14 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
 }
 
 }  // namespace
+
+int pre_f64_with_slopes(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                        const double *salt_tau, const double *K_iso, const uint8_t *mask_bits,
+                        const VgTensorFields *out, double *slopes, void *stream) {
+  return launch_pre<double>(dom, grid, set, temp_tau, salt_tau, K_iso, mask_bits, out, stream, "pre (adjoint)",
+                            slopes);
+}
+
 }  // namespace vg
 
 extern "C" int vg_isoneutral_pre_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,

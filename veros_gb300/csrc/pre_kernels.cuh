@@ -76,7 +76,13 @@ struct PreArgs {
   F *K11, *K22, *K33, *Aez, *Anz, *Abx, *Aby;
   long long sp, sr;
   int kchunk;
+  // optional (FP64, single domain): per point the 8 tapers, 8 slopes and the
+  // 2 clamped reciprocals, fields SLOPE_T + n, SLOPE_S + n, SLOPE_R + v
+  // slope_field doubles apart, for the adjoint
+  double *slopes;
+  long long slope_field;
 };
+enum { SLOPE_T = 0, SLOPE_S = 8, SLOPE_R = 16, SLOPE_FIELDS = 18 };
 
 // slope index h * 2 + v: h = east, west, north, south face; v = face below, above
 enum { S_XE0, S_XE1, S_XW0, S_XW1, S_YN0, S_YN1, S_YS0, S_YS1, NS };
@@ -296,6 +302,12 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     hring = 1;
   }
 
+  // the slopes of the ring points no tile owns (the last tile column / row of the domain)
+  const bool ring_store = pring >= 0 && (hring == 1 ? bx == (L.X - 3 + TX - 1) / TX - 1
+                                                    : by == (L.Y - 3 + TY - 1) / TY - 1);
+  const int ring_i = i0 - 1 + (pring >= 0 ? pring % PX : 0), ring_j = j0 - 1 + (pring >= 0 ? pring / PX : 0);
+  const bool own_in = i0 + tx < L.X && j0 + ty < L.Y;
+
   // the eight slopes of the own point at level lev; publishes its west/south slopes and the ring's
   auto slopes_level = [&](int lev, int b, Slope<F> *out) {
     const double(*q)[NP] = sm.q[b];
@@ -309,6 +321,17 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     for (int h = 0; h < 4; ++h)
 #pragma unroll
       for (int v = 0; v < 2; ++v) out[h * 2 + v] = slope_of(q, pc, h, v, (v == 1 || lev > 0) && (mH[h] || mWv[v]));
+    if (a.slopes && lev < ke && own_in) {
+      double *sl = a.slopes + L.at(i0 + tx, j0 + ty, lev);
+      const long long F_ = a.slope_field;
+#pragma unroll
+      for (int n = 0; n < NS; ++n) {
+        sl[(SLOPE_T + n) * F_] = (double)out[n].t;
+        sl[(SLOPE_S + n) * F_] = out[n].s;
+      }
+      sl[SLOPE_R * F_] = q[Q_R0][pc];
+      sl[(SLOPE_R + 1) * F_] = q[Q_R1][pc];
+    }
 #pragma unroll
     for (int v = 0; v < 2; ++v) {
       pb[PB_T_XW0 + v][pc] = out[S_XW0 + v].t;
@@ -324,6 +347,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         const Slope<F> sl = slope_of(q, pring, hring, v, mHr && (v == 1 || lev > 0));
         pb[base_t + v][pring] = sl.t;
         pb[base_ts + v][pring] = sl.t * F(sl.s);
+        if (a.slopes && lev < ke && ring_store && ring_i < L.X && ring_j < L.Y) {
+          double *st = a.slopes + L.at(ring_i, ring_j, lev);
+          const int n = hring * 2 + v;
+          st[(SLOPE_T + n) * a.slope_field] = (double)sl.t;
+          st[(SLOPE_S + n) * a.slope_field] = sl.s;
+          st[(SLOPE_R + v) * a.slope_field] = q[v ? Q_R1 : Q_R0][pring];
+        }
       }
     }
   };
@@ -458,4 +488,10 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_tile_kernel(PreArgs<F> a) {
 }
 
 }  // namespace detail
+
+// The FP64 tensor of one domain plus the per-point slope fields of
+// PreArgs::slopes (SLOPE_FIELDS fields of plane * Z doubles), for the adjoint.
+int pre_f64_with_slopes(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                        const double *salt_tau, const double *K_iso, const uint8_t *mask_bits,
+                        const VgTensorFields *out, double *slopes, void *stream);
 }  // namespace vg
