@@ -318,6 +318,58 @@ def run_adjoint(device, reps=5):
             "timing": "CUDA events, median of 5 after 2 warm-up rollouts"}
 
 
+def run_quarter_degree(device, steps=100):
+    """The FP32/FP64-split form at 0.25 degree (1440 x 720 x 60, nonlinear
+    EOS): ``steps`` steps of the FP64 drop-in and of the split form from the
+    same state, cells/s of each, and per-field max and RMS errors of the split
+    form against the FP64 run (the FP64 drop-in equals the FP64 oracle to
+    1e-12) over the interior wet cells."""
+    import torch
+
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    host = synthetic.global_quarter_deg_state(seed=0, lean=True)
+    cells = host.nx * host.ny * host.nz
+    out = {"workload": f"{host.nx}x{host.ny}x{host.nz} at 0.25 degree, eq 3, {steps} steps", "steps": steps}
+    states = {}
+    for precision in ("f64", "f32split"):
+        dev = DeviceState.from_host(host, device=device, precision=precision)
+        stepper = IsoneutralStepper(dev)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        stepper.step(steps)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out[precision] = {"cells_per_s": cells * steps / (ms / 1e3), "ms_per_step": ms / steps}
+        states[precision] = dev
+    out["split_speedup"] = out["f32split"]["cells_per_s"] / out["f64"]["cells_per_s"]
+    ref, got = states["f64"], states["f32split"]
+    wet = ref.variables.maskT[2:-2, 2:-2].to(torch.float64)
+    errs = {}
+    for name in ("temp", "salt", "dtemp_iso", "dsalt_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx",
+                 "Ai_by"):
+        r = getattr(ref.variables, name)
+        g = getattr(got.variables, name)
+        if name in ("temp", "salt"):
+            r, g = r[..., ref.variables.tau], g[..., got.variables.tau]
+        r = r[2:-2, 2:-2].to(torch.float64)
+        g = g[2:-2, 2:-2].to(torch.float64)
+        w = wet.reshape(wet.shape + (1,) * (r.dim() - 3))
+        d = (g - r) * w
+        rr = r * w
+        n = float(w.expand_as(d).sum())
+        errs[name] = {"max_rel": float(d.abs().max() / rr.abs().max()),
+                      "rms_rel": float((d.pow(2).sum() / n).sqrt() / (rr.pow(2).sum() / n).sqrt())}
+    out["split_error_vs_f64"] = errs
+    del states, ref, got
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -405,13 +457,14 @@ def run_gb300(args):
 
     launches = args.steps * stepper.launches_per_step()
     ensemble = adjoint = None
-    if not (args.no_ensemble and args.no_adjoint):
+    if not (args.no_ensemble and args.no_adjoint and not args.quarter_degree):
         del dev, stepper
         torch.cuda.empty_cache()
     if not args.no_ensemble:
         ensemble = run_ensemble(device)
     if not args.no_adjoint:
         adjoint = run_adjoint(device)
+    quarter = run_quarter_degree(device) if args.quarter_degree else None
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -448,6 +501,7 @@ def run_gb300(args):
         "gpu_launches": launches,
         "ensemble": ensemble,
         "adjoint": adjoint,
+        "quarter_degree": quarter,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))
@@ -464,6 +518,8 @@ def main():
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 48-member batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 8-step rollout adjoint measurement")
+    ap.add_argument("--quarter-degree", action="store_true",
+                    help="add the 0.25-degree split-versus-FP64 measurement (100 steps, ~25 GB of device memory)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

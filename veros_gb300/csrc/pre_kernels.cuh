@@ -93,7 +93,7 @@ constexpr unsigned kMaskWBelow = 0x10;  // in the plane mask byte: W mask of the
 template <typename F, int TY>
 struct Smem {
   static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
-  double q[2][NQ][NP];
+  F q[2][NQ][NP];  // per-point quantities; the split form keeps them FP32 (R computed in FP64)
   F pub[2][NPB][NP];
   double inv_dxu[PX], inv_dyu[PY], inv_cost[PY], facty[PY];
   double qinv_dxt[PX], qinv_dyt_cost[PY], dxu[PX];
@@ -108,8 +108,8 @@ constexpr size_t pre_smem_bytes(int Z) {
 
 template <typename F>
 struct Slope {
-  F t;       // taper
-  double s;  // slope
+  F t;  // taper
+  F s;  // slope
 };
 
 static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
@@ -131,34 +131,34 @@ static __device__ __forceinline__ double taper_of(double s, double slopec, doubl
   return 0.5 * (1.0 + tanh(x));
 }
 
-// Split form: the slope and the taper argument are FP64; the taper itself, a
-// bounded smooth function, is evaluated in FP32.
-static __device__ __forceinline__ float taper_of_split(double s, double slopec, double inv_dslope) {
-  const float x = (float)((slopec - fabs(s)) * inv_dslope);
+// Split form: slope, taper argument and taper in FP32 (the slope's clamped
+// denominator was formed in FP64).
+static __device__ __forceinline__ float taper_of_split(float s, double slopec, double inv_dslope) {
+  const float x = ((float)slopec - fabsf(s)) * (float)inv_dslope;
   return 0.5f * (1.0f + tanhf(x));
 }
 
 template <typename F>
-__device__ __forceinline__ F taper_t(double s, double slopec, double inv_dslope);
+__device__ __forceinline__ F taper_t(F s, double slopec, double inv_dslope);
 template <>
 __device__ __forceinline__ double taper_t<double>(double s, double slopec, double inv_dslope) {
   return taper_of(s, slopec, inv_dslope);
 }
 template <>
-__device__ __forceinline__ float taper_t<float>(double s, double slopec, double inv_dslope) {
+__device__ __forceinline__ float taper_t<float>(float s, double slopec, double inv_dslope) {
   return taper_of_split(s, slopec, inv_dslope);
 }
 
 // taper * s^2 for the K_33 sums
 template <typename F>
-__device__ __forceinline__ F sq_term(F tp, F ai, double s);
+__device__ __forceinline__ F sq_term(F tp, F ai, F s);
 template <>
 __device__ __forceinline__ double sq_term<double>(double tp, double ai, double s) {
   return tp * (s * s);
 }
 template <>
-__device__ __forceinline__ float sq_term<float>(float tp, float ai, double s) {
-  return ai * (float)s;
+__device__ __forceinline__ float sq_term<float>(float tp, float ai, float s) {
+  return ai * s;
 }
 
 // One tile (bx, by) and k-chunk bz of one domain; the whole CTA takes part.
@@ -265,15 +265,15 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         // vertical density gradients in FP64 (exact products of the split form's FP32 values)
         const double G0 = (double)rT * carryT[s] + (double)rS * carryS[s];  // face below (kr = 0)
         const double G1 = (double)rT * dTz + (double)rS * dSz;                   // face above (kr = 1)
-        double(*q)[NP] = sm.q[buf];
+        F(*q)[NP] = sm.q[buf];
         q[Q_RT][p] = rT;
         q[Q_RS][p] = rS;
-        q[Q_TX][p] = dTx;
-        q[Q_SX][p] = dSx;
-        q[Q_TY][p] = dTy;
-        q[Q_SY][p] = dSy;
-        q[Q_R0][p] = 1.0 / (fmin(0.0, G0) - kEpsln);
-        q[Q_R1][p] = 1.0 / (fmin(0.0, G1) - kEpsln);
+        q[Q_TX][p] = F(dTx);
+        q[Q_SX][p] = F(dSx);
+        q[Q_TY][p] = F(dTy);
+        q[Q_SY][p] = F(dSy);
+        q[Q_R0][p] = F(1.0 / (fmin(0.0, G0) - kEpsln));
+        q[Q_R1][p] = F(1.0 / (fmin(0.0, G1) - kEpsln));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
@@ -283,11 +283,11 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   };
 
   // slope (h, v) of plane point p: isoneutral.py:118-122, :155-159, :187-189, :205-207
-  auto slope_of = [&](const double(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
-    if (!need) return Slope<F>{F(0), 0.0};
+  auto slope_of = [&](const F(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
+    if (!need) return Slope<F>{F(0), F(0)};
     const int pg = (h == 0 || h == 2) ? p : (h == 1 ? p - 1 : p - PX);
     const int qT = h < 2 ? Q_TX : Q_TY, qS = h < 2 ? Q_SX : Q_SY;
-    const double s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
+    const F s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
     return Slope<F>{taper_t<F>(s, a.slopec, a.inv_dslope), s};
   };
 
@@ -310,7 +310,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 
   // the eight slopes of the own point at level lev; publishes its west/south slopes and the ring's
   auto slopes_level = [&](int lev, int b, Slope<F> *out) {
-    const double(*q)[NP] = sm.q[b];
+    const F(*q)[NP] = sm.q[b];
     const uint8_t *qm = sm.qm[b];
     F(*pb)[NP] = sm.pub[b];
     const unsigned m = qm[pc];
@@ -327,10 +327,10 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 #pragma unroll
       for (int n = 0; n < NS; ++n) {
         sl[(SLOPE_T + n) * F_] = (double)out[n].t;
-        sl[(SLOPE_S + n) * F_] = out[n].s;
+        sl[(SLOPE_S + n) * F_] = (double)out[n].s;
       }
-      sl[SLOPE_R * F_] = q[Q_R0][pc];
-      sl[(SLOPE_R + 1) * F_] = q[Q_R1][pc];
+      sl[SLOPE_R * F_] = (double)q[Q_R0][pc];
+      sl[(SLOPE_R + 1) * F_] = (double)q[Q_R1][pc];
     }
 #pragma unroll
     for (int v = 0; v < 2; ++v) {
@@ -351,8 +351,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           double *st = a.slopes + L.at(ring_i, ring_j, lev);
           const int n = hring * 2 + v;
           st[(SLOPE_T + n) * a.slope_field] = (double)sl.t;
-          st[(SLOPE_S + n) * a.slope_field] = sl.s;
-          st[(SLOPE_R + v) * a.slope_field] = q[v ? Q_R1 : Q_R0][pring];
+          st[(SLOPE_S + n) * a.slope_field] = (double)sl.s;
+          st[(SLOPE_R + v) * a.slope_field] = (double)q[v ? Q_R1 : Q_R0][pring];
         }
       }
     }
@@ -363,7 +363,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   __syncthreads();
   Slope<F> cur[NS], nxt[NS];
 #pragma unroll
-  for (int n = 0; n < NS; ++n) nxt[n] = Slope<F>{F(0), 0.0};
+  for (int n = 0; n < NS; ++n) nxt[n] = Slope<F>{F(0), F(0)};
   slopes_level(kb, kb & 1, cur);
 
   const int i = i0 + tx, j = j0 + ty;

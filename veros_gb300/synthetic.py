@@ -296,10 +296,10 @@ def global_1deg_state(seed=0, nz=60, k_iso_lognormal_sigma=None):
                       k_iso_lognormal_sigma=k_iso_lognormal_sigma, stable_caps=True)
 
 
-def global_quarter_deg_state(seed=0):
+def global_quarter_deg_state(seed=0, lean=False):
     """1440 x 720 x 60 at 0.25 degree, -90..90, dz 10-250 m, ~30% land plus polar caps beyond 62 deg, nonlinear EOS."""
     return make_state(1440, 720, 60, seed=seed, dx_deg=0.25, dy_deg=0.25, y_origin=-90.0, dz_top=10.0,
-                      dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3, stable_caps=True)
+                      dz_bottom=250.0, land_fraction=0.30, eq_of_state_type=3, stable_caps=True, lean=lean)
 
 
 def ensemble_states(n=48, seed0=0, lean=True):
