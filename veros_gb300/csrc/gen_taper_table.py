@@ -1,11 +1,13 @@
 """Generate taper_table.inc: piecewise Taylor coefficients of the slope taper.
 
 The taper of veros/core/isoneutral/isoneutral.py:10-15 is
-f(x) = 0.5 * (1 + tanh(x)) with x = (iso_slopec - |s|) / iso_dslope. On
-[X0, X1) the table holds, for intervals of width 1/64, the Taylor
-coefficients f^(n)(c)/n!, n = 0..6, about each interval centre c, computed
-with mpmath at 40 significant digits and rounded to double. With |x - c| <=
-1/128 the truncation error is below 5e-17 (max |f^(7)| = 136 on the range).
+f(x) = 0.5 * (1 + tanh(x)) with x = (iso_slopec - |s|) / iso_dslope. For
+the centres c_n = X0 + n/64, n = 0..(X1-X0)*64, the table holds the Taylor
+coefficients f^(k)(c_n)/k!, k = 0..6, computed with mpmath at 40 significant
+digits and rounded to double; entry n serves |x - c_n| <= 1/128, so the table
+covers [X0 - 1/128, X1 + 1/128). The truncation error is below 5e-17
+(max |f^(7)| = 136 on the range). Centres on the 1/64 grid let the kernel
+find n by rounding x*64 to the nearest integer.
 
 Run from the repository root: python veros_gb300/csrc/gen_taper_table.py
 """
@@ -19,17 +21,17 @@ X0, X1, PER_UNIT, DEG = -4, 2, 64, 6
 
 def main():
     mp.mp.dps = 40
-    n = (X1 - X0) * PER_UNIT
+    n = (X1 - X0) * PER_UNIT + 1
     f = lambda x: mp.mpf("0.5") * (1 + mp.tanh(x))  # noqa: E731
     rows = []
     for i in range(n):
-        c = mp.mpf(X0) + (mp.mpf(i) + mp.mpf("0.5")) / PER_UNIT
+        c = mp.mpf(X0) + mp.mpf(i) / PER_UNIT
         coef = mp.taylor(f, c, DEG)
         rows.append("  {" + ", ".join(repr(float(v)) for v in coef) + "},")
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "taper_table.inc")
     with open(out, "w") as fh:
         fh.write("// Generated by gen_taper_table.py: Taylor coefficients (degree %d) of\n" % DEG)
-        fh.write("// 0.5*(1+tanh(x)) about the centres of 1/%d-wide intervals on [%d, %d).\n" % (PER_UNIT, X0, X1))
+        fh.write("// 0.5*(1+tanh(x)) about the centres %d + n/%d, n = 0..%d.\n" % (X0, PER_UNIT, n - 1))
         fh.write("constexpr double kTaperX0 = %d.0;\n" % X0)
         fh.write("constexpr double kTaperX1 = %d.0;\n" % X1)
         fh.write("constexpr double kTaperPerUnit = %d.0;\n" % PER_UNIT)

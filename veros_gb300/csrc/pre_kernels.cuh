@@ -27,9 +27,10 @@
 // * Grid divisions become multiplications by reciprocals computed once per
 //   CTA; slope divisions become multiplications by the shared reciprocals.
 // * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
-//   Taylor polynomial on [-4, 2) (taper_table.inc, truncation error < 5e-17),
-//   the library tanh elsewhere, and an FP32 exp below x = -10 where the taper
-//   is below 2e-9 and the reference itself carries ~1e-16 absolute error.
+//   Taylor polynomial about the points -4 + n/64 (taper_table.inc, truncation
+//   error < 5e-17), the library tanh elsewhere, and an FP32 exp below x = -10
+//   where the taper is below 2e-9 and the reference itself carries ~1e-16
+//   absolute error.
 // * Faces whose mask is zero skip the slope work and store the zeros the
 //   reference's mask multiplication produces.
 //
@@ -112,13 +113,18 @@ struct Slope {
   F s;  // slope
 };
 
+// The table entry nearest to x is n = round(64 (x - X0)): x*64 + (1.5*2^52 -
+// 64*X0) rounds to an integer (the ulp at 1.5*2^52 is 1), whose low word is n
+// and whose high word is that of 1.5*2^52 for every n in the table (so
+// infinities and NaN fail the test and take the tail path).
 static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
+  constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
   const double x = (slopec - fabs(s)) * inv_dslope;
-  if (x >= kTaperX0 && x < kTaperX1) {
-    int idx = (int)((x - kTaperX0) * kTaperPerUnit);
-    idx = idx < kTaperN - 1 ? idx : kTaperN - 1;
-    const double b = x - (kTaperX0 + ((double)idx + 0.5) * (1.0 / kTaperPerUnit));
-    const double *c = kTaperCoef[idx];
+  const double y = fma(x, kTaperPerUnit, kMagic - kTaperX0 * kTaperPerUnit);
+  const int n = __double2loint(y);
+  if (__double2hiint(y) == 0x43380000 && (unsigned)n < (unsigned)kTaperN) {
+    const double b = fma(y - kMagic, -1.0 / kTaperPerUnit, x - kTaperX0);  // x - (X0 + n/64)
+    const double *c = kTaperCoef[n];
     double r = __ldg(c + 6);
     r = fma(r, b, __ldg(c + 5));
     r = fma(r, b, __ldg(c + 4));
@@ -154,7 +160,7 @@ template <typename F>
 __device__ __forceinline__ F sq_term(F tp, F ai, F s);
 template <>
 __device__ __forceinline__ double sq_term<double>(double tp, double ai, double s) {
-  return tp * (s * s);
+  return ai * s;
 }
 template <>
 __device__ __forceinline__ float sq_term<float>(float tp, float ai, float s) {
@@ -453,8 +459,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           for (int ip = 0; ip < 2; ++ip) {
             const Slope<F> sl = kr == 0 ? cur[ip ? S_XE1 : S_XW1] : nxt[ip ? S_XE0 : S_XW0];
             const F ai = sl.t * F(sl.s);
-            // FP64: dxu*K*taper*s^2 in the reference's order; split: (taper*s)*s, which stays
-            // finite where an FP32 s^2 would overflow under a vanishing taper
+            // taper*s^2 as (taper*s)*s: reuses Ai and stays finite where an FP32 s^2
+            // would overflow under a vanishing taper
             sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(sl.t, ai, sl.s);
             a.Abx[o + ip * a.sp + kr * a.sr] = ai;
           }
