@@ -83,7 +83,7 @@ static __device__ __forceinline__ float pfma(float x, float y, float z) { return
 
 // east face of cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
 template <typename F>
-__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int k, F c[5]) {
+__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int k, F inv_cost_dxu, F c[5]) {
   const Layout &L = a.L;
   const F s1 = F(a.s1);  // +-1: s1 * (sum) equals the sum of s1 * K
   F diffloc;
@@ -95,12 +95,11 @@ __device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int
   c[1] = pm(diffloc, ld(a.Aez, o + a.sp));
   c[2] = pm(diffloc, ld(a.Aez, o + a.sr));
   c[3] = pm(diffloc, ld(a.Aez, o + a.sp + a.sr));
-  c[4] = ld(a.K11, o);
+  c[4] = pm(inv_cost_dxu, ld(a.K11, o));
 }
 
 template <typename F>
-__device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long long o, int k, const F c[5],
-                                       F inv_cost_dxu, F q_dzt) {
+__device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long long o, int k, const F c[5], F q_dzt) {
   const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
   const long long dp = k < L.Z - 1 ? L.plane : 0;
   const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + 1);
@@ -110,12 +109,12 @@ __device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long l
   sumz = pfma(c[1], F(t1 - t1m), sumz);
   sumz = pfma(c[2], F(t0p - t0), sumz);
   sumz = pfma(c[3], F(t1p - t1), sumz);
-  return pfma(sumz, q_dzt, pm(pm(F(t1 - t0), inv_cost_dxu), c[4]));
+  return pfma(sumz, q_dzt, pm(F(t1 - t0), c[4]));
 }
 
 // north face of cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
 template <typename F>
-__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, int k, F c[5]) {
+__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, int k, F inv_dyu, F c[5]) {
   const Layout &L = a.L;
   const long long P = L.pitch;
   const F s1 = F(a.s1);
@@ -128,12 +127,12 @@ __device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, in
   c[1] = pm(diffloc, ld(a.Anz, o + a.sp));
   c[2] = pm(diffloc, ld(a.Anz, o + a.sr));
   c[3] = pm(diffloc, ld(a.Anz, o + a.sp + a.sr));
-  c[4] = ld(a.K22, o);
+  c[4] = pm(inv_dyu, ld(a.K22, o));
 }
 
 template <typename F>
 __device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long long o, int k, const F c[5], F cosu,
-                                        F inv_dyu, F q_dzt) {
+                                        F q_dzt) {
   const long long P = L.pitch;
   const long long dm = k > 0 ? L.plane : 0;
   const long long dp = k < L.Z - 1 ? L.plane : 0;
@@ -144,21 +143,22 @@ __device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long 
   sumz = pfma(c[1], F(t1 - t1m), sumz);
   sumz = pfma(c[2], F(t0p - t0), sumz);
   sumz = pfma(c[3], F(t1p - t1), sumz);
-  return pm(cosu, pfma(sumz, q_dzt, pm(pm(F(t1 - t0), inv_dyu), c[4])));
+  return pm(cosu, pfma(sumz, q_dzt, pm(F(t1 - t0), c[4])));
 }
 
 // top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111)
 template <typename F>
 __device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F c[8]) {
   const F diffloc = F(a.s2) * ld(a.K, o);
-  c[0] = pm(pm(diffloc, ld(a.Abx, o)), inv_cost);
-  c[1] = pm(pm(diffloc, ld(a.Abx, o + a.sr)), inv_cost);
-  c[2] = pm(pm(diffloc, ld(a.Abx, o + a.sp)), inv_cost);
-  c[3] = pm(pm(diffloc, ld(a.Abx, o + a.sp + a.sr)), inv_cost);
-  c[4] = pm(pm(diffloc, ld(a.Aby, o)), cosu_s);
-  c[5] = pm(pm(diffloc, ld(a.Aby, o + a.sr)), cosu_s);
-  c[6] = pm(pm(diffloc, ld(a.Aby, o + a.sp)), cosu_c);
-  c[7] = pm(pm(diffloc, ld(a.Aby, o + a.sp + a.sr)), cosu_c);
+  const F dx = pm(diffloc, inv_cost), ds = pm(diffloc, cosu_s), dc = pm(diffloc, cosu_c);
+  c[0] = pm(dx, ld(a.Abx, o));
+  c[1] = pm(dx, ld(a.Abx, o + a.sr));
+  c[2] = pm(dx, ld(a.Abx, o + a.sp));
+  c[3] = pm(dx, ld(a.Abx, o + a.sp + a.sr));
+  c[4] = pm(ds, ld(a.Aby, o));
+  c[5] = pm(ds, ld(a.Aby, o + a.sr));
+  c[6] = pm(dc, ld(a.Aby, o + a.sp));
+  c[7] = pm(dc, ld(a.Aby, o + a.sp + a.sr));
 }
 
 template <typename F>
@@ -223,15 +223,44 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   }
   if (halo_e) h_inv_cost_dxu = F(1.0 / (a.g.cost[hj_e] * a.g.dxu[i0 - 1]));
 
+  // Tracer values and differences of the own faces carried up the column:
+  // per tracer the values at the own, east and north columns, their vertical
+  // differences t(k) - t(k-1) (0 at k = 0, edge padding), and the west and
+  // south differences around the own point; each level loads the level above
+  // once and forms its differences once.
+  const long long P = L.pitch, Q = L.plane;
+  double vc[NTR], ve[NTR], vn[NTR];     // values at level k
+  double dzc[NTR], dze[NTR], dzn[NTR];  // t(k) - t(k-1)
+  double hw[NTR], hs[NTR];              // west and south differences at level k
   F ft_prev[NTR];
 #pragma unroll
-  for (int r = 0; r < NTR; ++r) ft_prev[r] = 0.0;
-  if (own && kb > 0) {
-    const long long ob = L.at(i, j, kb - 1);
-    F ct[8];
-    top_coef(a, ob, inv_cost, cosu_s, cosu_c, ct);
+  for (int r = 0; r < NTR; ++r) {
+    ft_prev[r] = 0.0;
+    vc[r] = ve[r] = vn[r] = dzc[r] = dze[r] = dzn[r] = hw[r] = hs[r] = 0.0;
+  }
+  if (own) {
+    const long long ob = L.at(i, j, kb);
 #pragma unroll
-    for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, ob, ct, q_dxt, q_dyt_cost);
+    for (int r = 0; r < NTR; ++r) {
+      const double *tr = A[r].tr;
+      vc[r] = __ldg(tr + ob);
+      ve[r] = __ldg(tr + ob + 1);
+      vn[r] = __ldg(tr + ob + P);
+      hw[r] = vc[r] - __ldg(tr + ob - 1);
+      hs[r] = vc[r] - __ldg(tr + ob - P);
+      if (kb > 0) {
+        dzc[r] = vc[r] - __ldg(tr + ob - Q);
+        dze[r] = ve[r] - __ldg(tr + ob + 1 - Q);
+        dzn[r] = vn[r] - __ldg(tr + ob + P - Q);
+      }
+    }
+    if (kb > 0) {
+      const long long op = L.at(i, j, kb - 1);
+      F ct[8];
+      top_coef(a, op, inv_cost, cosu_s, cosu_c, ct);
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, op, ct, q_dxt, q_dyt_cost);
+    }
   }
 
   for (int k = kb; k < ke; ++k) {
@@ -244,22 +273,67 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
 #pragma unroll
     for (int r = 0; r < NTR; ++r) fe[r] = fn[r] = ft[r] = 0.0;
     if (own) {
+      const bool up = k < Z - 1;
+      double uc[NTR], ue[NTR], un[NTR], uw[NTR], us[NTR];  // level k+1
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        const double *tr = A[r].tr;
+        if (up) {
+          uc[r] = __ldg(tr + o + Q);
+          ue[r] = __ldg(tr + o + 1 + Q);
+          un[r] = __ldg(tr + o + P + Q);
+          uw[r] = __ldg(tr + o - 1 + Q);
+          us[r] = __ldg(tr + o - P + Q);
+        } else {
+          uc[r] = vc[r];
+          ue[r] = ve[r];
+          un[r] = vn[r];
+          uw[r] = us[r] = 0.0;
+        }
+      }
       F ce[5], cn[5];
-      east_coef(a, o, k, ce);
-      north_coef(a, o, k, cn);
+      east_coef(a, o, k, inv_cost_dxu, ce);
+      north_coef(a, o, k, inv_dyu, cn);
+      F ct[8];
+      if (up) top_coef(a, o, inv_cost, cosu_s, cosu_c, ct);
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
-        fe[r] = east_flux(L, A[r].tr, o, k, ce, inv_cost_dxu, qz);
-        fn[r] = north_flux(L, A[r].tr, o, k, cn, cosu_c, inv_dyu, qz);
-      }
-      if (k < Z - 1) {
-        F ct[8];
-        top_coef(a, o, inv_cost, cosu_s, cosu_c, ct);
-#pragma unroll
-        for (int r = 0; r < NTR; ++r) ft[r] = top_flux(L, A[r].tr, o, ct, q_dxt, q_dyt_cost);
-      }
-#pragma unroll
-      for (int r = 0; r < NTR; ++r) {
+        // z differences above the own, east and north columns (0 on the top level)
+        const double zc = uc[r] - vc[r], ze = ue[r] - ve[r], zn = un[r] - vn[r];
+        const double he = ve[r] - vc[r], hn = vn[r] - vc[r];  // east and north differences at level k
+        // east face (diffusion.py:25-47)
+        F sz = pm(ce[0], F(dzc[r]));
+        sz = pfma(ce[1], F(dze[r]), sz);
+        sz = pfma(ce[2], F(zc), sz);
+        sz = pfma(ce[3], F(ze), sz);
+        fe[r] = pfma(sz, qz, pm(F(he), ce[4]));
+        // north face (diffusion.py:52-77)
+        F sn = pm(cn[0], F(dzc[r]));
+        sn = pfma(cn[1], F(dzn[r]), sn);
+        sn = pfma(cn[2], F(zc), sn);
+        sn = pfma(cn[3], F(zn), sn);
+        fn[r] = pm(cosu_c, pfma(sn, qz, pm(F(hn), cn[4])));
+        // horizontal differences on level k+1
+        const double hw1 = uc[r] - uw[r], he1 = ue[r] - uc[r], hs1 = uc[r] - us[r], hn1 = un[r] - uc[r];
+        if (up) {  // top face (diffusion.py:85-111)
+          F sx = pm(ct[0], F(hw[r]));
+          sx = pfma(ct[1], F(hw1), sx);
+          sx = pfma(ct[2], F(he), sx);
+          sx = pfma(ct[3], F(he1), sx);
+          F sy = pm(ct[4], F(hs[r]));
+          sy = pfma(ct[5], F(hs1), sy);
+          sy = pfma(ct[6], F(hn), sy);
+          sy = pfma(ct[7], F(hn1), sy);
+          ft[r] = pfma(sx, q_dxt, pm(sy, q_dyt_cost));
+        }
+        vc[r] = uc[r];
+        ve[r] = ue[r];
+        vn[r] = un[r];
+        dzc[r] = zc;
+        dze[r] = ze;
+        dzn[r] = zn;
+        hw[r] = hw1;
+        hs[r] = hs1;
         fe_s[b][r][ty][tx + 1] = fe[r];
         fn_s[b][r][ty + 1][tx] = fn[r];
       }
@@ -267,28 +341,33 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     if (halo_n) {
       const long long oh = L.at(hi_n, j0 - 1, k);
       F cn[5];
-      north_coef(a, oh, k, cn);
+      north_coef(a, oh, k, h_inv_dyu, cn);
 #pragma unroll
-      for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu, h_inv_dyu, qz);
+      for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu, qz);
     }
     if (halo_e) {
       const long long oh = L.at(i0 - 1, hj_e, k);
       F ce[5];
-      east_coef(a, oh, k, ce);
+      east_coef(a, oh, k, h_inv_cost_dxu, ce);
 #pragma unroll
-      for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce, h_inv_cost_dxu, qz);
+      for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce, qz);
     }
     __syncthreads();
-    if (own) {
-      const F mT = (__ldg(a.m + o) & VG_MASK_T) ? F(1.0) : F(0.0);
+    if (own && (__ldg(a.m + o) & VG_MASK_T)) {  // maskT multiplies the divergence (diffusion.py:123-137)
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
         const DiffArgs<F> &t = A[r];
-        F e = pm(mT, pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy)));
-        e = pfma(pm(mT, ft[r] - ft_prev[r]), F(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
-        ft_prev[r] = ft[r];
+        F e = pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy));
+        e = pfma(ft[r] - ft_prev[r], F(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
         t.dtr_iso[o] = add_(t.dtr_iso[o], e);
         t.trp[o] = radd(t.trp[o], rmul(t.dt, (double)e));
+      }
+    }
+    if (own) {
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        const DiffArgs<F> &t = A[r];
+        ft_prev[r] = ft[r];
         if (t.save_fluxes) {
           t.fe[o] = fe[r];
           t.fn[o] = fn[r];
