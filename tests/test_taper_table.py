@@ -1,0 +1,71 @@
+"""The taper table of the slope kernel (csrc/taper_table.inc) against the
+taper 0.5 * (1 + tanh(x)) of veros/core/isoneutral/isoneutral.py:10-15.
+
+The kernel picks entry n = round(64 (x + 4)) from the low word of
+x*64 + (1.5*2^52 + 256) and evaluates the entry's degree-6 Taylor polynomial
+at b = x - (-4 + n/64). This restates that arithmetic in NumPy (the product
+x*64 is exact, so a plain add rounds like the kernel's fused multiply-add)
+and checks the result against mpmath on random arguments and on both edges
+of every interval.
+"""
+
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+INC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "veros_gb300", "csrc",
+                   "taper_table.inc")
+MAGIC = 6755399441055744.0  # 1.5 * 2^52
+
+
+def _table():
+    txt = open(INC).read()
+    x0 = float(re.search(r"kTaperX0 = (-?[\d.]+)", txt).group(1))
+    per = float(re.search(r"kTaperPerUnit = ([\d.]+)", txt).group(1))
+    n = int(re.search(r"kTaperN = (\d+)", txt).group(1))
+    rows = re.findall(r"\{([^{}]+)\},", txt.split("kTaperCoef")[1])
+    coef = np.array([[float(v) for v in r.split(",")] for r in rows])
+    assert coef.shape == (n, 7)
+    return x0, per, coef
+
+
+def _taper_table(x, x0, per, coef):
+    y = np.float64(x) * per + (MAGIC - x0 * per)
+    bits = struct.unpack("<Q", struct.pack("<d", y))[0]
+    lo, hi = np.int64(np.uint32(bits & 0xFFFFFFFF)).astype(np.int32), bits >> 32
+    if hi != 0x43380000 or not 0 <= lo < coef.shape[0]:
+        return None
+    b = (y - MAGIC) * (-1.0 / per) + (x - x0)
+    r = coef[lo, 6]
+    for k in range(5, -1, -1):
+        r = r * b + coef[lo, k]
+    return r
+
+
+def test_table_matches_the_taper_to_rounding():
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 30
+    x0, per, coef = _table()
+    n = coef.shape[0]
+    centres = x0 + np.arange(n) / per
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(x0, x0 + (n - 1) / per, 4000), centres + 0.5 / per - 1e-14,
+                         centres - 0.5 / per + 1e-14])
+    worst = 0.0
+    for x in xs:
+        t = _taper_table(float(x), x0, per, coef)
+        assert t is not None, x
+        ref = float(mp.mpf("0.5") * (1 + mp.tanh(mp.mpf(float(x)))))
+        worst = max(worst, abs(t - ref))
+    assert worst <= 3e-16, worst
+
+
+def test_out_of_table_arguments_take_the_tail_path():
+    x0, per, coef = _table()
+    n = coef.shape[0]
+    for x in (x0 - 0.6 / per, x0 + (n - 1) / per + 0.6 / per, -50.0, 50.0, float("inf"), float("-inf"),
+              float("nan")):
+        assert _taper_table(x, x0, per, coef) is None, x
