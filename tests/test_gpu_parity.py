@@ -272,6 +272,27 @@ def test_global_1deg_step_vs_oracle():
     assert np.all(dev.download("temp")[land] == 0.0)
 
 
+def test_quarter_degree_step_vs_oracle():
+    """The 0.25-degree workload (1440 x 720 x 60, 62 M cells, nonlinear EOS):
+    one FP64 step against one oracle step from the same state. The oracle
+    step takes about a minute of one host core at this size; it reads the
+    host state without a copy (the step copies what it writes)."""
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    host = synthetic.global_quarter_deg_state(seed=0)
+    dev = DeviceState.from_host(host)
+    IsoneutralStepper(dev).step(1)
+    torch.cuda.synchronize()
+    vs = orc.OracleState(host.arrays, tau=host.tau, taup1=host.taup1, taum1=host.taum1)
+    tau_in = vs.tau
+    orc.isoneutral_step(vs, host.settings)
+    assert dev.variables.tau == vs.tau
+    _check_state(dev, vs, STEP_FIELDS, host.settings, tau_in)
+
+
 def test_drop_in_signatures_on_device_state():
     import veros_gb300 as vg
     from veros_gb300 import synthetic
