@@ -166,6 +166,24 @@ int vg_isoneutral_diffusion_pair_f32split(const VgDomain *dom, const VgGrid *gri
                                           const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
                                           void *scratch, size_t scratch_bytes, void *stream);
 
+/* The pair calls with the implicit solve's interior columns taken in the
+ * order column_order (indices (i-2) + (j-2)*(X-4), a permutation of all
+ * (X-4)*(Y-4) interior columns; deepest first keeps the lanes of a warp on
+ * columns of similar length; NULL: natural order). Results are identical to
+ * the unordered calls. */
+int vg_isoneutral_diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                             const VgTensorFields *ten, const double *K_iso,
+                                             const uint8_t *mask_bits, const int32_t *kbot,
+                                             const VgTracerArgs *temp, const VgTracerArgs *salt,
+                                             const int32_t *column_order, void *scratch, size_t scratch_bytes,
+                                             void *stream);
+int vg_isoneutral_diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                                  const VgTensorFieldsF32 *ten, const float *K_iso,
+                                                  const uint8_t *mask_bits, const int32_t *kbot,
+                                                  const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
+                                                  const int32_t *column_order, void *scratch,
+                                                  size_t scratch_bytes, void *stream);
+
 /* Scratch-free variant of vg_isoneutral_diffusion_f64 for callers that cannot
  * allocate device memory (an XLA custom-call or FFI handler working only with
  * the buffers it is handed, or a host model that fixes its device memory at
@@ -195,6 +213,11 @@ typedef struct VgStepFields {
   double *dtemp_iso, *dsalt_iso;
   const double *int_drhodT_tau, *int_drhodS_tau; /* energy branch only */
   double *P_diss_iso;                            /* may be NULL without the energy branch */
+  /* optional (NULL: natural order): the interior columns, as indices
+   * (i-2) + (j-2)*(X-4), in the order the implicit solve takes them; deepest
+   * first keeps the lanes of a warp on columns of similar length. A
+   * permutation of all (X-4)*(Y-4) interior columns. */
+  const int32_t *column_order;
 } VgStepFields;
 
 /* One isoneutral step as the reference's caller runs it
@@ -219,6 +242,7 @@ typedef struct VgStepFieldsF32 {
   float *dtemp_iso, *dsalt_iso;
   const float *int_drhodT_tau, *int_drhodS_tau;
   float *P_diss_iso;
+  const int32_t *column_order; /* as in VgStepFields */
 } VgStepFieldsF32;
 
 /* One isoneutral step of the FP32/FP64-split form (see vg_isoneutral_step_f64). */

@@ -61,13 +61,15 @@ class VgTracerArgs(ctypes.Structure):
 class VgStepFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
                                                 "mask_bits", "kbot")] + [("ten", VgTensorFields)] + [
-        (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso")]
+        (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso",
+                                       "column_order")]
 
 
 class VgStepFieldsF32(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
                                                 "mask_bits", "kbot")] + [("ten", VgTensorFieldsF32)] + [
-        (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso")]
+        (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso",
+                                       "column_order")]
 
 
 class VgEnsembleTuning(ctypes.Structure):
@@ -137,6 +139,23 @@ SIGNATURES = {
                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                         ctypes.POINTER(VgTracerArgs), ctypes.POINTER(VgTracerArgs),
                                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "vg_isoneutral_diffusion_pair_ordered_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                                ctypes.POINTER(VgIsoSettings),
+                                                                ctypes.POINTER(VgTensorFields), ctypes.c_void_p,
+                                                                ctypes.c_void_p, ctypes.c_void_p,
+                                                                ctypes.POINTER(VgTracerArgs),
+                                                                ctypes.POINTER(VgTracerArgs), ctypes.c_void_p,
+                                                                ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "vg_isoneutral_diffusion_pair_ordered_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain),
+                                                                     ctypes.POINTER(VgGrid),
+                                                                     ctypes.POINTER(VgIsoSettings),
+                                                                     ctypes.POINTER(VgTensorFieldsF32),
+                                                                     ctypes.c_void_p, ctypes.c_void_p,
+                                                                     ctypes.c_void_p,
+                                                                     ctypes.POINTER(VgTracerArgsF32),
+                                                                     ctypes.POINTER(VgTracerArgsF32),
+                                                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                                     ctypes.c_void_p]),
     "vg_isoneutral_step_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                               ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgStepFields),
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),

@@ -98,7 +98,8 @@ class IsoneutralAdjoint:
         T_new, S_new = self.empty(), self.empty()
         f = _capi.VgStepFields(T.data_ptr(), T_new.data_ptr(), S.data_ptr(), S_new.data_ptr(), K.data_ptr(),
                                dev.mask_bits().data_ptr(), dev.variables.kbot.data_ptr(), self._ten,
-                               self._diag[0].data_ptr(), self._diag[1].data_ptr(), None, None, None)
+                               self._diag[0].data_ptr(), self._diag[1].data_ptr(), None, None, None,
+                               dev.column_order().data_ptr())
         _capi.check(self.lib.vg_isoneutral_step_f64(self._dom, self._grid, self._set, f, self._pair.data_ptr(),
                                                     self._pair.numel() * 8, self._stream()), "isoneutral step")
         return T_new, S_new

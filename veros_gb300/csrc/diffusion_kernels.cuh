@@ -49,6 +49,7 @@ struct DiffArgs {
   long long sp, sr;
   const uint8_t *__restrict__ m;
   const int32_t *__restrict__ kbot;
+  const int32_t *__restrict__ col_order;  // implicit solve: interior columns in this order (NULL: natural)
   const double *__restrict__ tr;  // tau
   double *trp;                    // taup1
   F *dtr_iso;
@@ -517,10 +518,13 @@ __device__ __forceinline__ void implicit_body(const DiffArgs<F> &a, const DiffAr
     inv_dzt[k] = 1.0 / a.g.dzt[k];
   }
   __syncthreads();
-  const int col = cb * nb + t;
+  // with col_order, the deepest columns first: the lanes of a warp then walk
+  // columns of similar length
+  const int slot = cb * nb + t;
+  const int col = a.col_order ? (slot < ncols ? __ldg(a.col_order + slot) : ncols) : slot;
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
-  const int ks = col < ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
+  const int ks = (unsigned)col < (unsigned)ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
   if (ks >= 0 && ks < Z) implicit_column<F, NRHS>(a, b2, dtdzw, inv_dzt, cps, dps, t, nb, i, j, ks);
   __syncthreads();  // dtdzw is refilled by the next block of columns a persistent CTA takes
 }
@@ -640,6 +644,7 @@ inline int make_diff_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSe
   a.ft = scratch3 ? scratch3 + 2 * fsz : nullptr;
   a.iso = skew ? 0 : 1;
   a.kchunk = 0;
+  a.col_order = nullptr;
   return VG_OK;
 }
 

@@ -324,6 +324,7 @@ int member_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *se
         (st = make_diff_args<F>(dom, grid, set, &f.ten, f.K_iso, f.mask_bits, f.kbot, &trS, 0, nullptr, out[p].dS)))
       return st;
     out[p].dT.kchunk = out[p].dS.kchunk = dom->Z;
+    out[p].dT.col_order = out[p].dS.col_order = f.column_order;  // optional per member
     tau[2 * p] = f.temp_tau;
     tau[2 * p + 1] = f.salt_tau;
   }

@@ -71,7 +71,7 @@ int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *
 template <typename F, typename Ten, typename Tr>
 int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten,
                    const F *K_iso, const uint8_t *mask_bits, const int32_t *kbot, const Tr *temp, const Tr *salt,
-                   void *scratch, size_t scratch_bytes, void *stream) {
+                   void *scratch, size_t scratch_bytes, void *stream, const int32_t *col_order = nullptr) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -83,6 +83,7 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
   if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, 0, sc, aT))) return st;
   if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
     return st;
+  aT.col_order = aS.col_order = col_order;
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div<F, 2>(aT, aS, s))) return st;
   if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
@@ -94,6 +95,24 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
 }
 
 }  // namespace
+
+int diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                               const VgTensorFields *ten, const double *K_iso, const uint8_t *mask_bits,
+                               const int32_t *kbot, const VgTracerArgs *temp, const VgTracerArgs *salt,
+                               const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream) {
+  return diffusion_pair<double>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                                stream, column_order);
+}
+
+int diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                    const VgTensorFieldsF32 *ten, const float *K_iso, const uint8_t *mask_bits,
+                                    const int32_t *kbot, const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
+                                    const int32_t *column_order, void *scratch, size_t scratch_bytes,
+                                    void *stream) {
+  return diffusion_pair<float>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                               stream, column_order);
+}
+
 }  // namespace vg
 
 extern "C" int vg_isoneutral_diffusion_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
@@ -208,4 +227,25 @@ extern "C" int vg_isoneutral_diffusion_noalloc_f64(const VgDomain *dom, const Vg
   }
   return vg_isoneutral_diffusion_f64(dom, grid, set, ten, K_field, mask_bits, kbot, tr, skew, ptr,
                                      kNoAllocScratchBytes, stream);
+}
+
+extern "C" int vg_isoneutral_diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid,
+                                                        const VgIsoSettings *set, const VgTensorFields *ten,
+                                                        const double *K_iso, const uint8_t *mask_bits,
+                                                        const int32_t *kbot, const VgTracerArgs *temp,
+                                                        const VgTracerArgs *salt, const int32_t *column_order,
+                                                        void *scratch, size_t scratch_bytes, void *stream) {
+  return diffusion_pair<double>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                                stream, column_order);
+}
+
+extern "C" int vg_isoneutral_diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid,
+                                                             const VgIsoSettings *set, const VgTensorFieldsF32 *ten,
+                                                             const float *K_iso, const uint8_t *mask_bits,
+                                                             const int32_t *kbot, const VgTracerArgsF32 *temp,
+                                                             const VgTracerArgsF32 *salt,
+                                                             const int32_t *column_order, void *scratch,
+                                                             size_t scratch_bytes, void *stream) {
+  return diffusion_pair<float>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
+                               stream, column_order);
 }

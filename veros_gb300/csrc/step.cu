@@ -61,8 +61,8 @@ extern "C" int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, c
     return st;
   VgTracerArgs trT{f->temp_tau, f->temp_taup1, f->dtemp_iso, f->int_drhodT_tau, f->P_diss_iso};
   VgTracerArgs trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
-  return vg_isoneutral_diffusion_pair_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS, scratch,
-                                          scratch_bytes, stream);
+  return diffusion_pair_ordered_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
+                                    f->column_order, scratch, scratch_bytes, stream);
 }
 
 extern "C" int vg_isoneutral_step_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
@@ -77,6 +77,6 @@ extern "C" int vg_isoneutral_step_f32split(const VgDomain *dom, const VgGrid *gr
     return st;
   VgTracerArgsF32 trT{f->temp_tau, f->temp_taup1, f->dtemp_iso, f->int_drhodT_tau, f->P_diss_iso};
   VgTracerArgsF32 trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
-  return vg_isoneutral_diffusion_pair_f32split(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
-                                               scratch, scratch_bytes, stream);
+  return diffusion_pair_ordered_f32split(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
+                                         f->column_order, scratch, scratch_bytes, stream);
 }

@@ -77,7 +77,8 @@ class Ensemble:
         lvl = lambda t, n: t[..., n].data_ptr()  # noqa: E731
         return self._fields_t(lvl(v.temp, tau), lvl(v.temp, taup1), lvl(v.salt, tau), lvl(v.salt, taup1),
                               v.K_iso.data_ptr(), dev.mask_bits().data_ptr(), v.kbot.data_ptr(), dev.tensor_fields(),
-                              v.dtemp_iso.data_ptr(), v.dsalt_iso.data_ptr(), None, None, v.P_diss_iso.data_ptr())
+                              v.dtemp_iso.data_ptr(), v.dsalt_iso.data_ptr(), None, None, v.P_diss_iso.data_ptr(),
+                              dev.column_order().data_ptr())
 
     @property
     def cells(self):

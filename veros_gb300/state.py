@@ -263,6 +263,20 @@ class DeviceState:
             self._mask_version = version
         return self._mask_bits
 
+    def column_order(self):
+        """Interior columns, as indices (i-2) + (j-2)*(X-4), deepest first
+        (land last): the order in which the implicit solve takes them, so that
+        the lanes of a warp walk columns of similar length. Cached per kbot."""
+        kb = self.variables.kbot
+        key = (kb.data_ptr(), kb._version)
+        if getattr(self, "_order_key", None) != key:
+            inner = kb[2:-2, 2:-2].to(torch.int64)
+            depth = torch.where(inner > 0, self.Z - (inner - 1), torch.zeros_like(inner))
+            flat = depth.t().reshape(-1)  # index (i-2) + (j-2)*(X-4)
+            self._column_order = torch.argsort(-flat, stable=True).to(torch.int32).contiguous()
+            self._order_key = key
+        return self._column_order
+
     def tensor_fields(self):
         v = self.variables
         ai = v.Ai_ez

@@ -33,7 +33,7 @@ class IsoneutralStepper:
             lvl(v.temp, v.tau), lvl(v.temp, v.taup1), lvl(v.salt, v.tau), lvl(v.salt, v.taup1), v.K_iso.data_ptr(),
             dev.mask_bits().data_ptr(), v.kbot.data_ptr(), dev.tensor_fields(), v.dtemp_iso.data_ptr(),
             v.dsalt_iso.data_ptr(), lvl(v.int_drhodT, v.tau) if energy else None,
-            lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr())
+            lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr(), dev.column_order().data_ptr())
 
     def _fn(self, name):
         suffix = "_f64" if self.dev.precision == "f64" else "_f32split"
@@ -78,8 +78,9 @@ class IsoneutralStepper:
         targs = _capi.VgTracerArgs if dev.precision == "f64" else _capi.VgTracerArgsF32
         trT = targs(f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau, f.P_diss_iso)
         trS = targs(f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau, f.P_diss_iso)
-        _capi.check(self._fn("vg_isoneutral_diffusion_pair")(dom, grid, sett, f.ten, f.K_iso, f.mask_bits, f.kbot,
-                                                             trT, trS, self.scratch.data_ptr(), nbytes, stream),
+        _capi.check(self._fn("vg_isoneutral_diffusion_pair_ordered")(dom, grid, sett, f.ten, f.K_iso, f.mask_bits,
+                                                                     f.kbot, trT, trS, f.column_order,
+                                                                     self.scratch.data_ptr(), nbytes, stream),
                     "diffusion")
         rec(3)
         self._rotate()
