@@ -1,12 +1,13 @@
 """The taper table of the slope kernel (csrc/taper_table.inc) against the
 taper 0.5 * (1 + tanh(x)) of veros/core/isoneutral/isoneutral.py:10-15.
 
-The kernel picks entry n = round(64 (x + 4)) from the low word of
-x*64 + (1.5*2^52 + 256) and evaluates the entry's degree-6 Taylor polynomial
-at b = x - (-4 + n/64). This restates that arithmetic in NumPy (the product
-x*64 is exact, so a plain add rounds like the kernel's fused multiply-add)
-and checks the result against mpmath on random arguments and on both edges
-of every interval.
+The kernel picks entry n = round(P (x - X0)) (P entries per unit) from the
+low word of x*P + (1.5*2^52 - P*X0) and evaluates the entry's Taylor
+polynomial at b = x - (X0 + n/P). This restates that arithmetic in NumPy
+(the product x*P is exact for a power-of-two P, so a plain add rounds like
+the kernel's fused multiply-add) and checks the result against mpmath on
+random arguments and on both edges of every interval, within the table's
+truncation bound.
 """
 
 import os
@@ -26,9 +27,10 @@ def _table():
     x0 = float(re.search(r"kTaperX0 = (-?[\d.]+)", txt).group(1))
     per = float(re.search(r"kTaperPerUnit = ([\d.]+)", txt).group(1))
     n = int(re.search(r"kTaperN = (\d+)", txt).group(1))
+    deg = int(re.search(r"kTaperDeg = (\d+)", txt).group(1))
     rows = re.findall(r"\{([^{}]+)\},", txt.split("kTaperCoef")[1])
     coef = np.array([[float(v) for v in r.split(",")] for r in rows])
-    assert coef.shape == (n, 7)
+    assert coef.shape == (n, deg + 1)
     return x0, per, coef
 
 
@@ -39,8 +41,9 @@ def _taper_table(x, x0, per, coef):
     if hi != 0x43380000 or not 0 <= lo < coef.shape[0]:
         return None
     b = (y - MAGIC) * (-1.0 / per) + (x - x0)
-    r = coef[lo, 6]
-    for k in range(5, -1, -1):
+    deg = coef.shape[1] - 1
+    r = coef[lo, deg]
+    for k in range(deg - 1, -1, -1):
         r = r * b + coef[lo, k]
     return r
 
@@ -52,15 +55,17 @@ def test_table_matches_the_taper_to_rounding():
     n = coef.shape[0]
     centres = x0 + np.arange(n) / per
     rng = np.random.default_rng(0)
-    xs = np.concatenate([rng.uniform(x0, x0 + (n - 1) / per, 4000), centres + 0.5 / per - 1e-14,
-                         centres - 0.5 / per + 1e-14])
+    xs = np.concatenate([rng.uniform(x0, x0 + (n - 1) / per, 4000), centres[::4] + 0.5 / per - 1e-14,
+                         centres[::4] - 0.5 / per + 1e-14])
     worst = 0.0
     for x in xs:
         t = _taper_table(float(x), x0, per, coef)
         assert t is not None, x
         ref = float(mp.mpf("0.5") * (1 + mp.tanh(mp.mpf(float(x)))))
         worst = max(worst, abs(t - ref))
-    assert worst <= 3e-16, worst
+    # truncation bound of the table: max |f^(deg+1)| (1/(2P))^(deg+1) / (deg+1)! (2e-15 for degree 4 at
+    # P = 256) plus the polynomial's own rounding
+    assert worst <= 2.5e-15, worst
 
 
 def test_out_of_table_arguments_take_the_tail_path():

@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   gzT[0] = mWv[0] ? vdT[0] * gi.inv_dzw[k - 1] : 0.0;
   gzT[1] = mWv[1] ? vdT[1] * gi.inv_dzw[k] : 0.0;
   // the clamped reciprocals 1/(min(0, G) - epsln) of the forward; G >= 0 gives exactly R_flat
-  const double R_flat = 1.0 / (fmin(0.0, 0.0) - kEpsln);
+  const double R_flat = detail::recip_neg(fmin(0.0, 0.0) - kEpsln);
   const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
 
   // which faces carry a term: face h (east/north terms) and face v (top terms)

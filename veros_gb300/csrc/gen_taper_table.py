@@ -2,12 +2,13 @@
 
 The taper of veros/core/isoneutral/isoneutral.py:10-15 is
 f(x) = 0.5 * (1 + tanh(x)) with x = (iso_slopec - |s|) / iso_dslope. For
-the centres c_n = X0 + n/64, n = 0..(X1-X0)*64, the table holds the Taylor
-coefficients f^(k)(c_n)/k!, k = 0..6, computed with mpmath at 40 significant
-digits and rounded to double; entry n serves |x - c_n| <= 1/128, so the table
-covers [X0 - 1/128, X1 + 1/128). The truncation error is below 5e-17
-(max |f^(7)| = 136 on the range). Centres on the 1/64 grid let the kernel
-find n by rounding x*64 to the nearest integer.
+the centres c_n = X0 + n/256, n = 0..(X1-X0)*256, the table holds the Taylor
+coefficients f^(k)(c_n)/k!, k = 0..4, computed with mpmath at 40 significant
+digits and rounded to double; entry n serves |x - c_n| <= 1/512, so the table
+covers [X0 - 1/512, X1 + 1/512). The truncation error is below 2e-15
+(max |f^(5)| < 8 on the range, (1/512)^5 / 5!), 1e-15 of the taper's range
+and far below the 1e-12 bar of the outputs. Centres on the 1/256 grid let
+the kernel find n by rounding x*256 to the nearest integer.
 
 Run from the repository root: python veros_gb300/csrc/gen_taper_table.py
 """
@@ -16,7 +17,7 @@ import os
 
 import mpmath as mp
 
-X0, X1, PER_UNIT, DEG = -4, 2, 64, 6
+X0, X1, PER_UNIT, DEG = -4, 2, 256, 4
 
 
 def main():

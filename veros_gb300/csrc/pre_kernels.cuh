@@ -27,10 +27,11 @@
 // * Grid divisions become multiplications by reciprocals computed once per
 //   CTA; slope divisions become multiplications by the shared reciprocals.
 // * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
-//   Taylor polynomial about the points -4 + n/64 (taper_table.inc, truncation
-//   error < 5e-17), the library tanh elsewhere, and an FP32 exp below x = -10
-//   where the taper is below 2e-9 and the reference itself carries ~1e-16
-//   absolute error.
+//   Taylor polynomial of degree 4 about the points -4 + n/256 (taper_table.inc,
+//   truncation error < 2e-15), the library tanh elsewhere, and an FP32 exp
+//   below x = -10 where the taper is below 2e-9.
+// * The two clamped reciprocals 1/(min(0, G) - epsln) per point use
+//   recip_neg: an FP32 reciprocal refined by two Newton-Raphson steps.
 // * Faces whose mask is zero skip the slope work and store the zeros the
 //   reference's mask multiplication produces.
 //
@@ -113,8 +114,8 @@ struct Slope {
   F s;  // slope
 };
 
-// The table entry nearest to x is n = round(64 (x - X0)): x*64 + (1.5*2^52 -
-// 64*X0) rounds to an integer (the ulp at 1.5*2^52 is 1), whose low word is n
+// The table entry nearest to x is n = round(256 (x - X0)): x*256 + (1.5*2^52 -
+// 256*X0) rounds to an integer (the ulp at 1.5*2^52 is 1), whose low word is n
 // and whose high word is that of 1.5*2^52 for every n in the table (so
 // infinities and NaN fail the test and take the tail path).
 static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
@@ -123,11 +124,9 @@ static __device__ __forceinline__ double taper_of(double s, double slopec, doubl
   const double y = fma(x, kTaperPerUnit, kMagic - kTaperX0 * kTaperPerUnit);
   const int n = __double2loint(y);
   if (__double2hiint(y) == 0x43380000 && (unsigned)n < (unsigned)kTaperN) {
-    const double b = fma(y - kMagic, -1.0 / kTaperPerUnit, x - kTaperX0);  // x - (X0 + n/64)
+    const double b = fma(y - kMagic, -1.0 / kTaperPerUnit, x - kTaperX0);  // x - (X0 + n/256)
     const double *c = kTaperCoef[n];
-    double r = __ldg(c + 6);
-    r = fma(r, b, __ldg(c + 5));
-    r = fma(r, b, __ldg(c + 4));
+    double r = __ldg(c + 4);
     r = fma(r, b, __ldg(c + 3));
     r = fma(r, b, __ldg(c + 2));
     r = fma(r, b, __ldg(c + 1));
@@ -135,6 +134,18 @@ static __device__ __forceinline__ double taper_of(double s, double slopec, doubl
   }
   if (x < -10.0) return (double)expf(2.0f * (float)x);
   return 0.5 * (1.0 + tanh(x));
+}
+
+// 1/d for d = min(0, G) - epsln, i.e. d in (-inf, -1e-20]: an FP32 reciprocal
+// (d and 1/d are within FP32 range) refined by two Newton-Raphson steps
+// r <- r + r (1 - d r), each of which squares the relative error (2^-23 ->
+// 2^-46 -> below the final rounding): within one ulp of the quotient.
+static __device__ __forceinline__ double recip_neg(double d) {
+  double r = (double)__frcp_rn((float)d);
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
 }
 
 // Split form: slope, taper argument and taper in FP32 (the slope's clamped
@@ -278,8 +289,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         q[Q_SX][p] = F(dSx);
         q[Q_TY][p] = F(dTy);
         q[Q_SY][p] = F(dSy);
-        q[Q_R0][p] = F(1.0 / (fmin(0.0, G0) - kEpsln));
-        q[Q_R1][p] = F(1.0 / (fmin(0.0, G1) - kEpsln));
+        q[Q_R0][p] = F(recip_neg(fmin(0.0, G0) - kEpsln));
+        q[Q_R1][p] = F(recip_neg(fmin(0.0, G1) - kEpsln));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
