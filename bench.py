@@ -66,24 +66,36 @@ def aggregate_over_ranks(units, seconds, dist=None, device=None):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling while the timed region runs."""
+    """nvidia-smi clock/throttle sampling (every 50 ms) while the timed region
+    runs: the sampler starts half a second before the region, and only the
+    samples whose timestamps fall inside the region (``mark_start`` to
+    ``mark_stop``) are summarised."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.t0 = self.t1 = None
+        self.lines = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)
         except OSError:
             self.proc = None
         return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_stop(self):
+        self.t1 = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -94,26 +106,37 @@ class ClockSampler:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
             self.lines = [ln for ln in out.splitlines() if ln.strip()]
-        else:
-            self.lines = []
+
+    def _in_window(self, ln):
+        if self.t0 is None or self.t1 is None:
+            return True
+        import datetime
+
+        try:
+            stamp = datetime.datetime.strptime(ln.split(",")[0].strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return False
+        return self.t0 - 0.05 <= stamp <= self.t1 + 0.05
 
     def summary(self):
         sm, smax, reasons = [], None, set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for ln in self.lines:
+        window = [ln for ln in self.lines if self._in_window(ln)]
+        for ln in window or self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax = float(parts[2])
+                sm.append(float(parts[2]))
+                smax = float(parts[3])
             except ValueError:
                 continue
-            for n, val in zip(names, parts[5:9]):
+            for n, val in zip(names, parts[6:10]):
                 if val.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "in_timed_region": bool(window),
+                "interval_ms": 50}
 
 
 def _peaks():
@@ -401,11 +424,13 @@ def run_gb300(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        clocks.mark_start()
         start.record()
         for s in range(args.steps):
             stepper.step_stages(ev[s])
         stop.record()
         torch.cuda.synchronize()
+        clocks.mark_stop()
     if dist:
         dist.barrier()
     ms = start.elapsed_time(stop)
@@ -513,7 +538,7 @@ def run_gb300(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 48-member batched-ensemble measurement")

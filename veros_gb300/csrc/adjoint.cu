@@ -50,7 +50,13 @@ struct GridInv {
 constexpr int kTensorFields = 19;  // K_11, K_22, K_33, 4 x 4 Ai components
 enum { F_GTP = kTensorFields, F_GSP, F_GK33, F_PART };
 // partial sums written by the slope pass, one field each
-enum { P_LRT = 0, P_NSUM = 1, P_LG = 5, P_LVD = 7, P_LHD = 11, P_LDL = 19, P_LKW = 23, P_N = 25 };
+// per point: LRT the adjoint of drho/dT; WT/WS (per horizontal face h) the
+// face's tracer-difference adjoint from this point's slopes and fluxes, scaled
+// by the face's masked metric factor where it multiplies a gradient; GZT/GZS
+// (per vertical face v) likewise for the vertical gradients; LVD (tracer, v)
+// the vertical differences of the fluxes; LDL (h) diffloc; LKW (v) K_iso at
+// the vertical faces
+enum { P_LRT = 0, P_WT = 1, P_WS = 5, P_GZT = 9, P_GZS = 11, P_LVD = 13, P_LDL = 17, P_LKW = 21, P_N = 23 };
 // the forward's per-point tapers, slopes and reciprocals (detail::SLOPE_*)
 constexpr int F_SLOPES = F_PART + P_N;
 constexpr int kFields = F_SLOPES + detail::SLOPE_FIELDS;
@@ -210,6 +216,8 @@ struct SlopeArgs {
   const double *__restrict__ gK33;
   const uint8_t *__restrict__ m;
   const double *__restrict__ slopes;  // the forward's tapers, slopes and reciprocals
+  const double *__restrict__ K11;     // the forward's tensor
+  const double *__restrict__ K22;
   double *part;
   long long field;
 };
@@ -257,15 +265,19 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
                       hasN && (mk & VG_MASK_V), hasS && (__ldg(m + o - PW) & VG_MASK_V)};
   const bool mWv[2] = {hasD && (__ldg(m + o - PL) & VG_MASK_W), hasU && (mk & VG_MASK_W)};
 
-  // temperature gradients on the faces (isoneutral.py:46-95)
+  // masked metric factors of the face gradients and the temperature gradients (isoneutral.py:46-95)
   const double icx = gi.inv_cost[j];
+  const double fx[4] = {mH[0] ? gi.inv_dxu[i] * icx : 0.0, mH[1] ? gi.inv_dxu[i - 1] * icx : 0.0,
+                        mH[2] ? gi.inv_dyu[j] : 0.0, mH[3] ? gi.inv_dyu[j - 1] : 0.0};
+  const double fz[2] = {mWv[0] ? gi.inv_dzw[k - 1] : 0.0, mWv[1] ? gi.inv_dzw[k] : 0.0};
   double gxT[4], gzT[2];
-  gxT[0] = mH[0] ? hdT[0] * (gi.inv_dxu[i] * icx) : 0.0;
-  gxT[1] = mH[1] ? hdT[1] * (gi.inv_dxu[i - 1] * icx) : 0.0;
-  gxT[2] = mH[2] ? hdT[2] * gi.inv_dyu[j] : 0.0;
-  gxT[3] = mH[3] ? hdT[3] * gi.inv_dyu[j - 1] : 0.0;
-  gzT[0] = mWv[0] ? vdT[0] * gi.inv_dzw[k - 1] : 0.0;
-  gzT[1] = mWv[1] ? vdT[1] * gi.inv_dzw[k] : 0.0;
+#pragma unroll
+  for (int h = 0; h < 4; ++h) gxT[h] = hdT[h] * fx[h];
+  gzT[0] = vdT[0] * fz[0];
+  gzT[1] = vdT[1] * fz[1];
+  const bool wetP = mk & VG_MASK_T;
+  const Eos eos{a.eos};
+  const double rT = wetP ? eos.drdT(Tc, a.g.zt[k]) : 0.0, rS = wetP ? eos.drdS() : 0.0;
   // the clamped reciprocals 1/(min(0, G) - epsln) of the forward; G >= 0 gives exactly R_flat
   const double R_flat = detail::recip_neg(fmin(0.0, 0.0) - kEpsln);
   const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
@@ -397,19 +409,31 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
     }
   }
   lrT += lG[0] * gzT[0] + lG[1] * gzT[1];
+  // the K_11 / K_22 terms of the east and north fluxes (diffusion.py:31-33, :57-60), added
+  // once per face by the point west / south of it
+  if (vE[0]) {
+    const double k11 = __ldg(a.K11 + o) * (gi.inv_dxu[i] * icx);
+    lhd[0][0] += lfT[0] * k11;
+    lhd[1][0] += lfS[0] * k11;
+  }
+  if (vE[2]) {
+    const double k22 = __ldg(a.K22 + o) * gi.inv_dyu[j];
+    lhd[0][2] += lfT[2] * k22;
+    lhd[1][2] += lfS[2] * k22;
+  }
 
   double *p = a.part + o;
   p[P_LRT * F] = lrT;
 #pragma unroll
   for (int h = 0; h < 4; ++h) {
-    p[(P_NSUM + h) * F] = nsum[h];
-    p[(P_LHD + h) * F] = lhd[0][h];
-    p[(P_LHD + 4 + h) * F] = lhd[1][h];
+    p[(P_WT + h) * F] = nsum[h] * rT * fx[h] + lhd[0][h];
+    p[(P_WS + h) * F] = nsum[h] * rS * fx[h] + lhd[1][h];
     p[(P_LDL + h) * F] = ldl[h];
   }
 #pragma unroll
   for (int v = 0; v < 2; ++v) {
-    p[(P_LG + v) * F] = lG[v];
+    p[(P_GZT + v) * F] = lG[v] * rT * fz[v];
+    p[(P_GZS + v) * F] = lG[v] * rS * fz[v];
     p[(P_LVD + v) * F] = lvd[0][v];
     p[(P_LVD + 2 + v) * F] = lvd[1][v];
     p[(P_LKW + v) * F] = lKw[v];
@@ -424,12 +448,8 @@ struct GatherArgs {
   Grid g;
   GridInv gi;
   int eos;
-  double dt;
-  const double *__restrict__ T;
   const double *__restrict__ gTp;
   const double *__restrict__ gSp;
-  const double *__restrict__ K11;
-  const double *__restrict__ K22;
   const uint8_t *__restrict__ m;
   const double *__restrict__ part;
   long long field;
@@ -444,14 +464,8 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
   if (i >= L.X || j >= L.Y) return;
   const int X = L.X, Y = L.Y, Z = L.Z;
   const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane, F = a.field;
-  const GridInv &gi = a.gi;
   const uint8_t *m = a.m;
-  const Eos eos{a.eos};
   auto part = [&](int comp, long long at) { return __ldg(a.part + comp * F + at); };
-  auto rT_at = [&](long long at, int kk) {
-    return (__ldg(m + at) & VG_MASK_T) ? eos.drdT(__ldg(a.T + at), a.g.zt[kk]) : 0.0;
-  };
-  auto rS_at = [&](long long at) { return (__ldg(m + at) & VG_MASK_T) ? eos.drdS() : 0.0; };
 
   const bool wet = __ldg(m + o) & VG_MASK_T;
   double lamT = wet ? __ldg(a.gTp + o) + drdT_dT(a.eos) * part(P_LRT, o) : 0.0;
@@ -459,27 +473,14 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
   double gk = part(P_LKW + 1, o) + (k < Z - 1 ? part(P_LKW + 0, o + PL) : 0.0);
   const double wk = k >= 1 ? 0.25 : 0.5;
 
-  // x-faces f = i-1 (this point is east of it) and f = i (west of it)
+  // x-faces f = i-1 (this point is east of it) and f = i (west of it): the
+  // face's difference T(f+1) - T(f) takes the partials of both its points
 #pragma unroll
   for (int side = 0; side < 2; ++side) {
     const int f = i - 1 + side;
     if (f < 0 || f > X - 2) continue;
     const long long ow = o - 1 + side, oe = ow + 1;
-    const double nW = part(P_NSUM + 0, ow), nE = part(P_NSUM + 1, oe);
-    const double lgT = nW * rT_at(ow, k) + nE * rT_at(oe, k);
-    const double lgS = nW * rS_at(ow) + nE * rS_at(oe);
-    const double fac = (__ldg(m + ow) & VG_MASK_U) ? gi.inv_dxu[f] * gi.inv_cost[j] : 0.0;
-    double lhT = part(P_LHD + 0, ow) + part(P_LHD + 1, oe);
-    double lhS = part(P_LHD + 4, ow) + part(P_LHD + 5, oe);
-    if (f >= 1 && f < X - 2 && j >= 2 && j < Y - 2) {
-      // flux_east's K_11 term (diffusion.py:31-33)
-      const double k11 = __ldg(a.K11 + ow) * (gi.inv_dxu[f] * gi.inv_cost[j]);
-      const double muwT = mu_at(L, m, a.gTp, a.dt, ow, f, j), mueT = mu_at(L, m, a.gTp, a.dt, oe, f + 1, j);
-      const double muwS = mu_at(L, m, a.gSp, a.dt, ow, f, j), mueS = mu_at(L, m, a.gSp, a.dt, oe, f + 1, j);
-      lhT += (muwT * gi.inv_dxt[f] - mueT * gi.inv_dxt[f + 1]) * gi.inv_cost[j] * k11;
-      lhS += (muwS * gi.inv_dxt[f] - mueS * gi.inv_dxt[f + 1]) * gi.inv_cost[j] * k11;
-    }
-    const double wT = lgT * fac + lhT, wS = lgS * fac + lhS;
+    const double wT = part(P_WT + 0, ow) + part(P_WT + 1, oe), wS = part(P_WS + 0, ow) + part(P_WS + 1, oe);
     lamT += side == 0 ? wT : -wT;
     lamS += side == 0 ? wS : -wS;
     gk += wk * (part(P_LDL + 0, ow) + part(P_LDL + 1, oe));
@@ -491,22 +492,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
     const int f = j - 1 + side;
     if (f < 0 || f > Y - 2) continue;
     const long long os = o + (side - 1) * PW, on = os + PW;
-    const double nS_ = part(P_NSUM + 2, os), nN_ = part(P_NSUM + 3, on);
-    const double lgT = nS_ * rT_at(os, k) + nN_ * rT_at(on, k);
-    const double lgS = nS_ * rS_at(os) + nN_ * rS_at(on);
-    const double fac = (__ldg(m + os) & VG_MASK_V) ? gi.inv_dyu[f] : 0.0;
-    double lhT = part(P_LHD + 2, os) + part(P_LHD + 3, on);
-    double lhS = part(P_LHD + 6, os) + part(P_LHD + 7, on);
-    if (f >= 1 && f < Y - 2 && i >= 2 && i < X - 2) {
-      // flux_north's K_22 term (diffusion.py:57-60)
-      const double k22 = __ldg(a.K22 + os) * gi.inv_dyu[f];
-      const double cs = gi.inv_dyt[f] * gi.inv_cost[f], cn = gi.inv_dyt[f + 1] * gi.inv_cost[f + 1];
-      const double musT = mu_at(L, m, a.gTp, a.dt, os, i, f), munT = mu_at(L, m, a.gTp, a.dt, on, i, f + 1);
-      const double musS = mu_at(L, m, a.gSp, a.dt, os, i, f), munS = mu_at(L, m, a.gSp, a.dt, on, i, f + 1);
-      lhT += a.g.cosu[f] * (musT * cs - munT * cn) * k22;
-      lhS += a.g.cosu[f] * (musS * cs - munS * cn) * k22;
-    }
-    const double wT = lgT * fac + lhT, wS = lgS * fac + lhS;
+    const double wT = part(P_WT + 2, os) + part(P_WT + 3, on), wS = part(P_WS + 2, os) + part(P_WS + 3, on);
     lamT += side == 0 ? wT : -wT;
     lamS += side == 0 ? wS : -wS;
     gk += wk * (part(P_LDL + 2, os) + part(P_LDL + 3, on));
@@ -518,12 +504,9 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
     const int f = k - 1 + side;
     if (f < 0 || f > Z - 2) continue;
     const long long od = o + (side - 1) * PL, ou = od + PL;
-    const double gU = part(P_LG + 1, od), gD = part(P_LG + 0, ou);
-    const double lgT = gU * rT_at(od, f) + gD * rT_at(ou, f + 1);
-    const double lgS = gU * rS_at(od) + gD * rS_at(ou);
-    const double fac = (__ldg(m + od) & VG_MASK_W) ? gi.inv_dzw[f] : 0.0;
-    lamT += side == 0 ? lgT * fac : -lgT * fac;
-    lamS += side == 0 ? lgS * fac : -lgS * fac;
+    const double gT = part(P_GZT + 1, od) + part(P_GZT + 0, ou), gS = part(P_GZS + 1, od) + part(P_GZS + 0, ou);
+    lamT += side == 0 ? gT : -gT;
+    lamS += side == 0 ? gS : -gS;
   }
   // vertical tracer differences of the isoneutral fluxes (edge-padded in z)
   if (k >= 1) {
@@ -620,14 +603,13 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   {
     adj::SlopeArgs a{L,          g,          gi,      set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
                      set->K_iso_steep, set->dt_tracer, f->temp, f->salt, f->K_iso, gTp, gSp, gK33, f->mask_bits,
-                     slopes,     part,       F};
+                     slopes,     ten.K_11,   ten.K_22, part, F};
     adj::adj_slope_kernel<<<grd, block, 0, s>>>(a);
     if ((st = check_launch("adj_slope_kernel"))) return st;
   }
   // 5. gather
   {
-    adj::GatherArgs a{L,        g,        gi,           set->eq_of_state_type, set->dt_tracer, f->temp, gTp, gSp,
-                      ten.K_11, ten.K_22, f->mask_bits, part,                  F,              f->gtemp, f->gsalt,
+    adj::GatherArgs a{L, g, gi, set->eq_of_state_type, gTp, gSp, f->mask_bits, part, F, f->gtemp, f->gsalt,
                       f->gK_iso};
     adj::adj_gather_kernel<<<grd, block, 0, s>>>(a);
     if ((st = check_launch("adj_gather_kernel"))) return st;
