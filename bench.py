@@ -462,20 +462,22 @@ def run_gb300(args):
     # end to end through the host-buffer step API
     v = dev.variables
     pin = lambda: torch.empty((X, Y, Z), dtype=torch.float64).pin_memory()  # noqa: E731
-    hT, hS, oT, oS, odT, odS = (pin() for _ in range(6))
+    hT, hS = pin(), pin()
     hT.copy_(torch.from_numpy(np.ascontiguousarray(host.temp[..., 1])))
     hS.copy_(torch.from_numpy(np.ascontiguousarray(host.salt[..., 1])))
-    staging = torch.empty((6, X, Y, Z), dtype=torch.float64, device=device)
+    outs = [[pin() for _ in range(4)] for _ in range(2)]  # alternate output buffers
+    pipe = stepper.pipeline()
     e2e_steps = max(3, min(args.steps, 20))
-    for _ in range(2):
-        stepper.step_host(hT, hS, oT, oS, odT, odS, staging)
+    for n in range(2):
+        pipe.submit(hT, hS, *outs[n % 2])
+    pipe.finish()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        stepper.step_host(hT, hS, oT, oS, odT, odS, staging)
-    torch.cuda.synchronize()
+    for n in range(e2e_steps):
+        pipe.submit(hT, hS, *outs[n % 2])
+    pipe.finish()
     e2e_s = time.perf_counter() - t0
     e2e_cells, e2e_s = aggregate_over_ranks(cells * e2e_steps, e2e_s, dist, device)
     e2e_value = e2e_cells / e2e_s
@@ -517,7 +519,8 @@ def run_gb300(args):
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 2 * X * Y * Z * 8,
                 "d2h_bytes_per_step": 4 * X * Y * Z * 8, "steps": e2e_steps,
-                "api": "IsoneutralStepper.step_host (pinned host buffers, reference layout)"},
+                "api": "IsoneutralStepper.pipeline().submit per step: pinned host buffers in the reference layout, "
+                       "uploads and downloads on their own streams overlapping the neighbouring steps' kernels"},
         "f32split": {"value": split_value, "unit": "cells/s", "ms_per_step": split_ms / args.steps,
                      "speedup_vs_f64": split_value / value,
                      "tracer_rel_maxnorm_err_vs_f64": split_err,

@@ -362,6 +362,39 @@ def test_host_buffer_step_matches_device_step():
     assert np.array_equal(outs[3].numpy(), a.download("dsalt_iso"))
 
 
+def test_host_pipeline_matches_serial_host_steps():
+    """Independent batches through the overlapped-copy pipeline equal lone step_host calls."""
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    host = synthetic.make_state(30, 20, 12, seed=6, eq_of_state_type=3, land_fraction=0.3)
+    a = IsoneutralStepper(DeviceState.from_host(host))
+    b = IsoneutralStepper(DeviceState.from_host(host))
+    X, Y, Z = a.dev.X, a.dev.Y, a.dev.Z
+    rng = np.random.default_rng(3)
+    pin = lambda x: torch.from_numpy(np.ascontiguousarray(x)).pin_memory()  # noqa: E731
+    batches = []
+    for _ in range(4):
+        dT = rng.normal(0.0, 0.05, (X, Y, Z)) * host.maskT
+        batches.append((pin(host.temp[..., host.tau] + dT), pin(host.salt[..., host.tau])))
+    serial = []
+    for hT, hS in batches:
+        outs = [torch.empty((X, Y, Z), dtype=torch.float64).pin_memory() for _ in range(4)]
+        a.step_host(hT, hS, *outs)
+        serial.append([o.numpy().copy() for o in outs])
+    pipe = b.pipeline()
+    piped = []
+    for hT, hS in batches:
+        outs = [torch.empty((X, Y, Z), dtype=torch.float64).pin_memory() for _ in range(4)]
+        pipe.submit(hT, hS, *outs)
+        piped.append(outs)
+    pipe.finish()
+    for want, got in zip(serial, piped):
+        for w, g in zip(want, got):
+            np.testing.assert_array_equal(g.numpy(), w)
+
+
 def test_vertmix_and_streamfunction_vs_reference_golden():
     """vertmix_tempsalt and the GM streamfunction diagnostics against the reference's outputs."""
     from veros_gb300.isoneutral import isoneutral_diag_streamfunction_kernel

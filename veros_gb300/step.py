@@ -114,8 +114,85 @@ class IsoneutralStepper:
         out_dsalt.copy_(staging[5], non_blocking=True)
         torch.cuda.current_stream(self.dev.device).synchronize()
 
+    def pipeline(self):
+        """A :class:`HostPipeline` of this stepper (independent host batches, copies overlapped)."""
+        return HostPipeline(self)
+
     def launches_per_step(self):
         """Kernels of this library one step enqueues: prepare, pre, one flux
         kernel for temp and salt, one shared implicit solve and, with the
         energy branch, two energy kernels."""
         return 1 + 1 + 1 + 1 + (2 if self.dev.settings.enable_conserve_energy else 0)
+
+
+class HostPipeline:
+    """Independent batches from and to host buffers with the copies overlapped.
+
+    Each :meth:`submit` is one step of :meth:`IsoneutralStepper.step_host`:
+    temp and salt at tau from pinned host tensors in the reference layout in,
+    the new level and ``dtemp_iso``/``dsalt_iso`` out to pinned host tensors.
+    The upload of a batch runs on its own stream while the previous batch's
+    kernels run, and its download on a second stream while the next batch's
+    kernels run; device staging is double buffered and guarded by events, so
+    batch n's results equal those of a lone ``step_host`` call.
+
+    :meth:`submit` returns without waiting: the input tensors must not be
+    changed, nor the outputs read, before the returned event has completed
+    (``event.synchronize()``) or :meth:`finish` has returned.
+    """
+
+    def __init__(self, stepper):
+        self.st = stepper
+        dev = stepper.dev
+        self.device = dev.device
+        shape = (dev.X, dev.Y, dev.Z)
+        self.stage_in = [torch.empty((2, *shape), dtype=torch.float64, device=self.device) for _ in range(2)]
+        self.stage_out = [torch.empty((4, *shape), dtype=torch.float64, device=self.device) for _ in range(2)]
+        self.h2d = torch.cuda.Stream(self.device)
+        self.d2h = torch.cuda.Stream(self.device)
+        self.in_free = [None, None]  # compute done reading stage_in[b]
+        self.out_free = [None, None]  # download done reading stage_out[b]
+        self.n = 0
+
+    def submit(self, temp_tau, salt_tau, out_temp, out_salt, out_dtemp, out_dsalt):
+        b = self.n % 2
+        v = self.st.dev.variables
+        compute = torch.cuda.current_stream(self.device)
+        stage_in, stage_out = self.stage_in[b], self.stage_out[b]
+        with torch.cuda.stream(self.h2d):
+            if self.in_free[b] is not None:
+                self.h2d.wait_event(self.in_free[b])
+            stage_in[0].copy_(temp_tau, non_blocking=True)
+            stage_in[1].copy_(salt_tau, non_blocking=True)
+            uploaded = torch.cuda.Event()
+            uploaded.record(self.h2d)
+        compute.wait_event(uploaded)
+        v.temp[..., v.tau].copy_(stage_in[0])
+        v.salt[..., v.tau].copy_(stage_in[1])
+        self.in_free[b] = torch.cuda.Event()
+        self.in_free[b].record(compute)
+        self.st.step(1)
+        if self.out_free[b] is not None:
+            compute.wait_event(self.out_free[b])
+        new = v.tau
+        stage_out[0].copy_(v.temp[..., new])
+        stage_out[1].copy_(v.salt[..., new])
+        stage_out[2].copy_(v.dtemp_iso)
+        stage_out[3].copy_(v.dsalt_iso)
+        ready = torch.cuda.Event()
+        ready.record(compute)
+        with torch.cuda.stream(self.d2h):
+            self.d2h.wait_event(ready)
+            out_temp.copy_(stage_out[0], non_blocking=True)
+            out_salt.copy_(stage_out[1], non_blocking=True)
+            out_dtemp.copy_(stage_out[2], non_blocking=True)
+            out_dsalt.copy_(stage_out[3], non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(self.d2h)
+        self.out_free[b] = done
+        self.n += 1
+        return done
+
+    def finish(self):
+        """Wait for every submitted batch."""
+        torch.cuda.synchronize(self.device)
