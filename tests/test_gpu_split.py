@@ -1,11 +1,11 @@
 """The FP32/FP64-split form against the FP64 path.
 
-Split form: tracers, tracer gradients, slope denominators and slopes, and the
-implicit solve in FP64; diffusivities, tensors, fluxes, taper, tendencies and
-dissipation in FP32. Stated error budget (relative max-norm against the FP64
-result of the same state, per output field): tracers <= 1e-6 (the north-star
-bound); tensors, tendencies and dissipation <= 1e-4. The measured figures
-are printed by the tests and recorded in the design notes.
+Split form: tracers, tracer differences, the clamped slope denominators and
+the implicit solve in FP64; slopes, taper, diffusivities, tensors, fluxes,
+tendencies and dissipation in FP32. Error budget (relative max-norm against
+the FP64 result of the same state, per output field): tracers <= 1e-6;
+tensors, tendencies and dissipation <= 1e-4. The tests print the measured
+figures.
 """
 
 import numpy as np

@@ -2,7 +2,8 @@
 
 Each ``csrc/*.cu`` file compiles to an object in parallel; the objects link
 into ``veros_gb300/libveros_gb300.so`` with the CUDA runtime linked
-statically, so the library needs only the driver at run time.
+statically, so the library needs only the CUDA driver library (libcuda) at
+run time.
 """
 
 import concurrent.futures as cf
