@@ -3,9 +3,9 @@ taper 0.5 * (1 + tanh(x)) of veros/core/isoneutral/isoneutral.py:10-15.
 
 The kernel picks entry n = round(P (x - X0)) (P entries per unit) from the
 low word of x*P + (1.5*2^52 - P*X0) and evaluates the entry's Taylor
-polynomial at b = x - (X0 + n/P). This restates that arithmetic in NumPy
-(the product x*P is exact for a power-of-two P, so a plain add rounds like
-the kernel's fused multiply-add) and checks the result against mpmath on
+polynomial at b = x - c_n, c_n = X0 + n/P stored at the end of the row.
+This restates that arithmetic in NumPy (the product x*P is exact for a
+power-of-two P, so a plain add rounds like the kernel's fused multiply-add) and checks the result against mpmath on
 random arguments and on both edges of every interval, within the table's
 truncation bound.
 """
@@ -29,9 +29,10 @@ def _table():
     n = int(re.search(r"kTaperN = (\d+)", txt).group(1))
     deg = int(re.search(r"kTaperDeg = (\d+)", txt).group(1))
     rows = re.findall(r"\{([^{}]+)\},", txt.split("kTaperCoef")[1])
-    coef = np.array([[float(v) for v in r.split(",")] for r in rows])
-    assert coef.shape == (n, deg + 1)
-    return x0, per, coef
+    table = np.array([[float(v) for v in r.split(",")] for r in rows])
+    assert table.shape == (n, deg + 2)
+    assert np.array_equal(table[:, deg + 1], x0 + np.arange(n) / per)  # each row's centre
+    return x0, per, table
 
 
 def _taper_table(x, x0, per, coef):
@@ -40,8 +41,8 @@ def _taper_table(x, x0, per, coef):
     lo, hi = np.int64(np.uint32(bits & 0xFFFFFFFF)).astype(np.int32), bits >> 32
     if hi != 0x43380000 or not 0 <= lo < coef.shape[0]:
         return None
-    b = (y - MAGIC) * (-1.0 / per) + (x - x0)
-    deg = coef.shape[1] - 1
+    deg = coef.shape[1] - 2
+    b = x - coef[lo, deg + 1]
     r = coef[lo, deg]
     for k in range(deg - 1, -1, -1):
         r = r * b + coef[lo, k]

@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const Eos eos{a.eos};
   const double rT = wetP ? eos.drdT(Tc, a.g.zt[k]) : 0.0, rS = wetP ? eos.drdS() : 0.0;
   // the clamped reciprocals 1/(min(0, G) - epsln) of the forward; G >= 0 gives exactly R_flat
-  const double R_flat = detail::recip_neg(fmin(0.0, 0.0) - kEpsln);
+  const double R_flat = detail::recip_neg(fmin0(0.0) - kEpsln);
   const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
 
   // which faces carry a term: face h (east/north terms) and face v (top terms)

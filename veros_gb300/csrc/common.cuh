@@ -51,6 +51,50 @@ inline bool grid_complete(const VgGrid *g) {
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// FP64 helpers that keep work off the FP64 pipe (one FP64 warp instruction
+// costs tens of issue cycles on GB300; integer and FP32 instructions do not
+// compete for that pipe).
+
+// min(0, x) from the sign bit
+__device__ __forceinline__ double fmin0(double x) { return __double_as_longlong(x) < 0 ? x : 0.0; }
+
+// max(a, b) by an integer comparison of the bit patterns mapped to a monotone order
+__device__ __forceinline__ double dmax(double a, double b) {
+  long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  ia ^= (ia >> 63) & 0x7FFFFFFFFFFFFFFFLL;
+  ib ^= (ib >> 63) & 0x7FFFFFFFFFFFFFFFLL;
+  return ia >= ib ? a : b;
+}
+
+// double -> float by truncating the mantissa (|x| within the FP32 normal range)
+__device__ __forceinline__ float dtof_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned e = (unsigned)((int)((b >> 52) & 0x7FF) - 1023 + 127);
+  const unsigned m = (unsigned)(b >> 29) & 0x7FFFFFu;
+  return __uint_as_float(sign | (e << 23) | m);
+}
+
+// float -> double, exact for FP32 normal numbers
+__device__ __forceinline__ double ftod(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long e = (unsigned long long)(((u >> 23) & 0xFFu) - 127 + 1023) << 52;
+  const unsigned long long m = (unsigned long long)(u & 0x7FFFFFu) << 29;
+  return __longlong_as_double((long long)(sign | e | m));
+}
+
+// 1/d for d of FP32-normal magnitude: an FP32 reciprocal of the truncated d,
+// refined by two Newton-Raphson steps r <- r + r (1 - d r), each of which
+// squares the relative error (2^-22 -> 2^-44 -> below the final rounding).
+__device__ __forceinline__ double recip_newton(double d) {
+  double r = ftod(__frcp_rn(dtof_trunc(d)));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 // Equation-of-state derivatives for eq types 1-4
 // (veros/core/density/linear_eq.py:36-43, nonlinear_eq1.py:39-47,
 //  nonlinear_eq2.py:57-66, nonlinear_eq3.py:39-47).

@@ -453,7 +453,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         const double ak = k == ks ? 0.0 : pm(-delta_prev, idzt);  // a_tri, zero at the edge (operators.py:72)
         const double bk = pfma(k == ks ? delta : delta + delta_prev, idzt, 1.0);  // b_tri, b_tri_edge at ks
         const double ck = pm(-delta, idzt);                                      // c_tri (0 on the top level)
-        const double den = 1.0 / pfma(-ak, cp, bk);
+        const double den = recip_newton(pfma(-ak, cp, bk));  // pivot >= the diagonal's excess over 1
         cp = pm(ck, den);
         cps[(size_t)k * nb + t] = cp;
 #pragma unroll

@@ -4,7 +4,7 @@ The taper of veros/core/isoneutral/isoneutral.py:10-15 is
 f(x) = 0.5 * (1 + tanh(x)) with x = (iso_slopec - |s|) / iso_dslope. For
 the centres c_n = X0 + n/256, n = 0..(X1-X0)*256, the table holds the Taylor
 coefficients f^(k)(c_n)/k!, k = 0..4, computed with mpmath at 40 significant
-digits and rounded to double; entry n serves |x - c_n| <= 1/512, so the table
+digits and rounded to double, followed by c_n itself; entry n serves |x - c_n| <= 1/512, so the table
 covers [X0 - 1/512, X1 + 1/512). The truncation error is below 2e-15
 (max |f^(5)| < 8 on the range, (1/512)^5 / 5!), 1e-15 of the taper's range
 and far below the 1e-12 bar of the outputs. Centres on the 1/256 grid let
@@ -27,7 +27,7 @@ def main():
     rows = []
     for i in range(n):
         c = mp.mpf(X0) + mp.mpf(i) / PER_UNIT
-        coef = mp.taylor(f, c, DEG)
+        coef = mp.taylor(f, c, DEG) + [c]  # the row's centre last
         rows.append("  {" + ", ".join(repr(float(v)) for v in coef) + "},")
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "taper_table.inc")
     with open(out, "w") as fh:
@@ -38,7 +38,8 @@ def main():
         fh.write("constexpr double kTaperPerUnit = %d.0;\n" % PER_UNIT)
         fh.write("constexpr int kTaperN = %d;\n" % n)
         fh.write("constexpr int kTaperDeg = %d;\n" % DEG)
-        fh.write("static __device__ const double kTaperCoef[%d][%d] = {\n" % (n, DEG + 1))
+        fh.write("// row n: f^(k)(c_n)/k! for k = 0..%d, then c_n\n" % DEG)
+        fh.write("static __device__ const double kTaperCoef[%d][%d] = {\n" % (n, DEG + 2))
         fh.write("\n".join(rows))
         fh.write("\n};\n")
     print(out)

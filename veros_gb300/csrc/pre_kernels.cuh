@@ -30,8 +30,9 @@
 //   Taylor polynomial of degree 4 about the points -4 + n/256 (taper_table.inc,
 //   truncation error < 2e-15), the library tanh elsewhere, and an FP32 exp
 //   below x = -10 where the taper is below 2e-9.
-// * The two clamped reciprocals 1/(min(0, G) - epsln) per point use
-//   recip_neg: an FP32 reciprocal refined by two Newton-Raphson steps.
+// * The two clamped reciprocals 1/(min(0, G) - epsln) per point use an FP32
+//   reciprocal refined by two Newton-Raphson steps; min(0, .), max(.) and the
+//   FP64 <-> FP32 conversions around it are integer operations.
 // * Faces whose mask is zero skip the slope work and store the zeros the
 //   reference's mask multiplication produces.
 //
@@ -117,15 +118,16 @@ struct Slope {
 // The table entry nearest to x is n = round(256 (x - X0)): x*256 + (1.5*2^52 -
 // 256*X0) rounds to an integer (the ulp at 1.5*2^52 is 1), whose low word is n
 // and whose high word is that of 1.5*2^52 for every n in the table (so
-// infinities and NaN fail the test and take the tail path).
-static __device__ __forceinline__ double taper_of(double s, double slopec, double inv_dslope) {
+// infinities and NaN fail the test and take the tail path). Each table row
+// ends with its centre X0 + n/256. sc = slopec / dslope.
+static __device__ __forceinline__ double taper_of(double s, double sc, double inv_dslope) {
   constexpr double kMagic = 6755399441055744.0;  // 1.5 * 2^52
-  const double x = (slopec - fabs(s)) * inv_dslope;
+  const double x = fma(fabs(s), -inv_dslope, sc);
   const double y = fma(x, kTaperPerUnit, kMagic - kTaperX0 * kTaperPerUnit);
   const int n = __double2loint(y);
   if (__double2hiint(y) == 0x43380000 && (unsigned)n < (unsigned)kTaperN) {
-    const double b = fma(y - kMagic, -1.0 / kTaperPerUnit, x - kTaperX0);  // x - (X0 + n/256)
     const double *c = kTaperCoef[n];
+    const double b = x - __ldg(c + kTaperDeg + 1);
     double r = __ldg(c + 4);
     r = fma(r, b, __ldg(c + 3));
     r = fma(r, b, __ldg(c + 2));
@@ -136,17 +138,8 @@ static __device__ __forceinline__ double taper_of(double s, double slopec, doubl
   return 0.5 * (1.0 + tanh(x));
 }
 
-// 1/d for d = min(0, G) - epsln, i.e. d in (-inf, -1e-20]: an FP32 reciprocal
-// (d and 1/d are within FP32 range) refined by two Newton-Raphson steps
-// r <- r + r (1 - d r), each of which squares the relative error (2^-23 ->
-// 2^-46 -> below the final rounding): within one ulp of the quotient.
-static __device__ __forceinline__ double recip_neg(double d) {
-  double r = (double)__frcp_rn((float)d);
-  double e = fma(-d, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-d, r, 1.0);
-  return fma(r, e, r);
-}
+// 1/d for d = min(0, G) - epsln, i.e. d in (-inf, -1e-20]
+static __device__ __forceinline__ double recip_neg(double d) { return recip_newton(d); }
 
 // Split form: slope, taper argument and taper in FP32 (the slope's clamped
 // denominator was formed in FP64).
@@ -155,16 +148,21 @@ static __device__ __forceinline__ float taper_of_split(float s, double slopec, d
   return 0.5f * (1.0f + tanhf(x));
 }
 
+// sc = slopec / dslope (the FP64 taper's argument offset)
 template <typename F>
-__device__ __forceinline__ F taper_t(F s, double slopec, double inv_dslope);
+__device__ __forceinline__ F taper_t(F s, double slopec, double sc, double inv_dslope);
 template <>
-__device__ __forceinline__ double taper_t<double>(double s, double slopec, double inv_dslope) {
-  return taper_of(s, slopec, inv_dslope);
+__device__ __forceinline__ double taper_t<double>(double s, double slopec, double sc, double inv_dslope) {
+  return taper_of(s, sc, inv_dslope);
 }
 template <>
-__device__ __forceinline__ float taper_t<float>(float s, double slopec, double inv_dslope) {
+__device__ __forceinline__ float taper_t<float>(float s, double slopec, double sc, double inv_dslope) {
   return taper_of_split(s, slopec, inv_dslope);
 }
+
+// max(K_iso_steep, x): FP64 by integer comparison, FP32 as is
+__device__ __forceinline__ double max_t(double a, double b) { return dmax(a, b); }
+__device__ __forceinline__ float max_t(float a, float b) { return fmaxf(a, b); }
 
 // taper * s^2 for the K_33 sums
 template <typename F>
@@ -289,8 +287,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         q[Q_SX][p] = F(dSx);
         q[Q_TY][p] = F(dTy);
         q[Q_SY][p] = F(dSy);
-        q[Q_R0][p] = F(recip_neg(fmin(0.0, G0) - kEpsln));
-        q[Q_R1][p] = F(recip_neg(fmin(0.0, G1) - kEpsln));
+        q[Q_R0][p] = F(recip_neg(fmin0(G0) - kEpsln));
+        q[Q_R1][p] = F(recip_neg(fmin0(G1) - kEpsln));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
@@ -300,12 +298,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   };
 
   // slope (h, v) of plane point p: isoneutral.py:118-122, :155-159, :187-189, :205-207
+  const double sc = a.slopec * a.inv_dslope;
   auto slope_of = [&](const F(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
     if (!need) return Slope<F>{F(0), F(0)};
     const int pg = (h == 0 || h == 2) ? p : (h == 1 ? p - 1 : p - PX);
     const int qT = h < 2 ? Q_TX : Q_TY, qS = h < 2 ? Q_SX : Q_SY;
     const F s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
-    return Slope<F>{taper_t<F>(s, a.slopec, a.inv_dslope), s};
+    return Slope<F>{taper_t<F>(s, a.slopec, sc, a.inv_dslope), s};
   };
 
   const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
@@ -412,9 +411,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
           const F t0 = cur[S_XE0 + kr].t, t1 = pb[PB_T_XW0 + kr][pc + 1];
-          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t0);
+          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t0);
           a.Aez[o + kr * a.sr] = t0 * F(cur[S_XE0 + kr].s);
-          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t1);
+          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t1);
           a.Aez[o + a.sp + kr * a.sr] = pb[PB_TS_XW0 + kr][pc + 1];
         }
       } else {
@@ -442,9 +441,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
           const F t0 = cur[S_YN0 + kr].t, t1 = pb[PB_T_YS0 + kr][pc + PX];
-          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t0);
+          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t0);
           a.Anz[o + kr * a.sr] = t0 * F(cur[S_YN0 + kr].s);
-          sumz += F(zdzw[k - 1 + kr]) * max(F(a.ksteep), diffloc * t1);
+          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t1);
           a.Anz[o + a.sp + kr * a.sr] = pb[PB_TS_YS0 + kr][pc + PX];
         }
       } else {
