@@ -95,6 +95,45 @@ __device__ __forceinline__ double recip_newton(double d) {
   return fma(r, e, r);
 }
 
+// FP64 -> FP32 rounded to nearest (ties away from zero) by integer
+// operations; magnitudes below the FP32 normal range flush to a signed zero,
+// above it to infinity. The split form's conversions use it.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFULL) + (1ULL << 28);  // round at FP32's last bit
+  const int e2 = e + (int)(m >> 52);                                      // carry into the exponent
+  if (e2 <= 0) return __uint_as_float(sign);
+  if (e2 >= 255) return __uint_as_float(sign | 0x7F800000u);
+  return __uint_as_float(sign | ((unsigned)e2 << 23) | ((unsigned)(m >> 29) & 0x7FFFFFu));
+}
+
+// FP32 -> FP64 by integer operations, exact (FP32 denormals flush to zero)
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned ef = (u >> 23) & 0xFFu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long m = (unsigned long long)(u & 0x7FFFFFu) << 29;
+  if (ef == 0) return __longlong_as_double((long long)sign);
+  if (ef == 255) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ULL | m));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(ef - 127 + 1023) << 52) | m));
+}
+
+// Conversions between the FP64 path and the derived-field type F
+template <typename F>
+__device__ __forceinline__ F to_F(double x);
+template <>
+__device__ __forceinline__ double to_F<double>(double x) {
+  return x;
+}
+template <>
+__device__ __forceinline__ float to_F<float>(double x) {
+  return d2f_int(x);
+}
+__device__ __forceinline__ double to_D(double x) { return x; }
+__device__ __forceinline__ double to_D(float x) { return f2d_int(x); }
+
 // Equation-of-state derivatives for eq types 1-4
 // (veros/core/density/linear_eq.py:36-43, nonlinear_eq1.py:39-47,
 //  nonlinear_eq2.py:57-66, nonlinear_eq3.py:39-47).

@@ -86,7 +86,7 @@ static __device__ __forceinline__ float pfma(float x, float y, float z) { return
 template <typename F>
 __device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int k, F inv_cost_dxu, F c[5]) {
   const Layout &L = a.L;
-  const F s1 = F(a.s1);  // +-1: s1 * (sum) equals the sum of s1 * K
+  const F s1 = to_F<F>(a.s1);  // +-1: s1 * (sum) equals the sum of s1 * K
   F diffloc;
   if (k >= 1)
     diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + 1) + ld(a.K, o + 1 - L.plane)));
@@ -106,11 +106,11 @@ __device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long l
   const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + 1);
   const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + 1 - dm);
   const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + 1 + dp);
-  F sumz = pm(c[0], F(t0 - t0m));
-  sumz = pfma(c[1], F(t1 - t1m), sumz);
-  sumz = pfma(c[2], F(t0p - t0), sumz);
-  sumz = pfma(c[3], F(t1p - t1), sumz);
-  return pfma(sumz, q_dzt, pm(F(t1 - t0), c[4]));
+  F sumz = pm(c[0], to_F<F>(t0 - t0m));
+  sumz = pfma(c[1], to_F<F>(t1 - t1m), sumz);
+  sumz = pfma(c[2], to_F<F>(t0p - t0), sumz);
+  sumz = pfma(c[3], to_F<F>(t1p - t1), sumz);
+  return pfma(sumz, q_dzt, pm(to_F<F>(t1 - t0), c[4]));
 }
 
 // north face of cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
@@ -118,7 +118,7 @@ template <typename F>
 __device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, int k, F inv_dyu, F c[5]) {
   const Layout &L = a.L;
   const long long P = L.pitch;
-  const F s1 = F(a.s1);
+  const F s1 = to_F<F>(a.s1);
   F diffloc;
   if (k >= 1)
     diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + P) + ld(a.K, o + P - L.plane)));
@@ -140,17 +140,17 @@ __device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long 
   const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + P);
   const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + P - dm);
   const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + P + dp);
-  F sumz = pm(c[0], F(t0 - t0m));
-  sumz = pfma(c[1], F(t1 - t1m), sumz);
-  sumz = pfma(c[2], F(t0p - t0), sumz);
-  sumz = pfma(c[3], F(t1p - t1), sumz);
-  return pm(cosu, pfma(sumz, q_dzt, pm(F(t1 - t0), c[4])));
+  F sumz = pm(c[0], to_F<F>(t0 - t0m));
+  sumz = pfma(c[1], to_F<F>(t1 - t1m), sumz);
+  sumz = pfma(c[2], to_F<F>(t0p - t0), sumz);
+  sumz = pfma(c[3], to_F<F>(t1p - t1), sumz);
+  return pm(cosu, pfma(sumz, q_dzt, pm(to_F<F>(t1 - t0), c[4])));
 }
 
 // top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111)
 template <typename F>
 __device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F c[8]) {
-  const F diffloc = F(a.s2) * ld(a.K, o);
+  const F diffloc = to_F<F>(a.s2) * ld(a.K, o);
   const F dx = pm(diffloc, inv_cost), ds = pm(diffloc, cosu_s), dc = pm(diffloc, cosu_c);
   c[0] = pm(dx, ld(a.Abx, o));
   c[1] = pm(dx, ld(a.Abx, o + a.sr));
@@ -167,14 +167,14 @@ __device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long lo
                                       F q_dyt_cost) {
   const long long P = L.pitch, Q = L.plane;
   const double tc = __ldg(tr + o), tcu = __ldg(tr + o + Q);
-  F sumx = pm(c[0], F(tc - __ldg(tr + o - 1)));
-  sumx = pfma(c[1], F(tcu - __ldg(tr + o - 1 + Q)), sumx);
-  sumx = pfma(c[2], F(__ldg(tr + o + 1) - tc), sumx);
-  sumx = pfma(c[3], F(__ldg(tr + o + 1 + Q) - tcu), sumx);
-  F sumy = pm(c[4], F(tc - __ldg(tr + o - P)));
-  sumy = pfma(c[5], F(tcu - __ldg(tr + o - P + Q)), sumy);
-  sumy = pfma(c[6], F(__ldg(tr + o + P) - tc), sumy);
-  sumy = pfma(c[7], F(__ldg(tr + o + P + Q) - tcu), sumy);
+  F sumx = pm(c[0], to_F<F>(tc - __ldg(tr + o - 1)));
+  sumx = pfma(c[1], to_F<F>(tcu - __ldg(tr + o - 1 + Q)), sumx);
+  sumx = pfma(c[2], to_F<F>(__ldg(tr + o + 1) - tc), sumx);
+  sumx = pfma(c[3], to_F<F>(__ldg(tr + o + 1 + Q) - tcu), sumx);
+  F sumy = pm(c[4], to_F<F>(tc - __ldg(tr + o - P)));
+  sumy = pfma(c[5], to_F<F>(tcu - __ldg(tr + o - P + Q)), sumy);
+  sumy = pfma(c[6], to_F<F>(__ldg(tr + o + P) - tc), sumy);
+  sumy = pfma(c[7], to_F<F>(__ldg(tr + o + P + Q) - tcu), sumy);
   return pfma(sumx, q_dxt, pm(sumy, q_dyt_cost));
 }
 
@@ -269,7 +269,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     // reads before level k+2's writes to the same buffer
     const int b = k & 1;
     const long long o = L.at(i, j, k);
-    const F qz = F(zq_dzt[k]);
+    const F qz = to_F<F>(zq_dzt[k]);
     F fe[NTR], fn[NTR], ft[NTR];
 #pragma unroll
     for (int r = 0; r < NTR; ++r) fe[r] = fn[r] = ft[r] = 0.0;
@@ -303,28 +303,28 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
         const double zc = uc[r] - vc[r], ze = ue[r] - ve[r], zn = un[r] - vn[r];
         const double he = ve[r] - vc[r], hn = vn[r] - vc[r];  // east and north differences at level k
         // east face (diffusion.py:25-47)
-        F sz = pm(ce[0], F(dzc[r]));
-        sz = pfma(ce[1], F(dze[r]), sz);
-        sz = pfma(ce[2], F(zc), sz);
-        sz = pfma(ce[3], F(ze), sz);
-        fe[r] = pfma(sz, qz, pm(F(he), ce[4]));
+        F sz = pm(ce[0], to_F<F>(dzc[r]));
+        sz = pfma(ce[1], to_F<F>(dze[r]), sz);
+        sz = pfma(ce[2], to_F<F>(zc), sz);
+        sz = pfma(ce[3], to_F<F>(ze), sz);
+        fe[r] = pfma(sz, qz, pm(to_F<F>(he), ce[4]));
         // north face (diffusion.py:52-77)
-        F sn = pm(cn[0], F(dzc[r]));
-        sn = pfma(cn[1], F(dzn[r]), sn);
-        sn = pfma(cn[2], F(zc), sn);
-        sn = pfma(cn[3], F(zn), sn);
-        fn[r] = pm(cosu_c, pfma(sn, qz, pm(F(hn), cn[4])));
+        F sn = pm(cn[0], to_F<F>(dzc[r]));
+        sn = pfma(cn[1], to_F<F>(dzn[r]), sn);
+        sn = pfma(cn[2], to_F<F>(zc), sn);
+        sn = pfma(cn[3], to_F<F>(zn), sn);
+        fn[r] = pm(cosu_c, pfma(sn, qz, pm(to_F<F>(hn), cn[4])));
         // horizontal differences on level k+1
         const double hw1 = uc[r] - uw[r], he1 = ue[r] - uc[r], hs1 = uc[r] - us[r], hn1 = un[r] - uc[r];
         if (up) {  // top face (diffusion.py:85-111)
-          F sx = pm(ct[0], F(hw[r]));
-          sx = pfma(ct[1], F(hw1), sx);
-          sx = pfma(ct[2], F(he), sx);
-          sx = pfma(ct[3], F(he1), sx);
-          F sy = pm(ct[4], F(hs[r]));
-          sy = pfma(ct[5], F(hs1), sy);
-          sy = pfma(ct[6], F(hn), sy);
-          sy = pfma(ct[7], F(hn1), sy);
+          F sx = pm(ct[0], to_F<F>(hw[r]));
+          sx = pfma(ct[1], to_F<F>(hw1), sx);
+          sx = pfma(ct[2], to_F<F>(he), sx);
+          sx = pfma(ct[3], to_F<F>(he1), sx);
+          F sy = pm(ct[4], to_F<F>(hs[r]));
+          sy = pfma(ct[5], to_F<F>(hs1), sy);
+          sy = pfma(ct[6], to_F<F>(hn), sy);
+          sy = pfma(ct[7], to_F<F>(hn1), sy);
           ft[r] = pfma(sx, q_dxt, pm(sy, q_dyt_cost));
         }
         vc[r] = uc[r];
@@ -359,9 +359,9 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       for (int r = 0; r < NTR; ++r) {
         const DiffArgs<F> &t = A[r];
         F e = pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy));
-        e = pfma(ft[r] - ft_prev[r], F(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
+        e = pfma(ft[r] - ft_prev[r], to_F<F>(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
         t.dtr_iso[o] = add_(t.dtr_iso[o], e);
-        t.trp[o] = radd(t.trp[o], rmul(t.dt, (double)e));
+        t.trp[o] = radd(t.trp[o], rmul(t.dt, to_D(e)));
       }
     }
     if (own) {
@@ -423,7 +423,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
   for (int u = 0; u < PF; ++u) {
     const int k = ks + u;
     const long long o = base + (long long)min(k, Z - 1) * L.plane;
-    qK[u] = k < Z - 1 ? (double)ld(a.K33, o) : 0.0;
+    qK[u] = k < Z - 1 ? to_D(ld(a.K33, o)) : 0.0;
 #pragma unroll
     for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? (double)trp[r][o] : 0.0;
   }
@@ -446,7 +446,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         const int kn = k + PF;
         if (kn < Z) {
           const long long on = base + (long long)kn * L.plane;
-          qK[u] = kn < Z - 1 ? (double)ld(a.K33, on) : 0.0;
+          qK[u] = kn < Z - 1 ? to_D(ld(a.K33, on)) : 0.0;
 #pragma unroll
           for (int r = 0; r < NRHS; ++r) qT[u][r] = (double)trp[r][on];
         }
@@ -480,7 +480,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
           t1[u][r] = (double)trp[r][o];
-          d1[u][r] = (double)dtr[r][o];
+          d1[u][r] = to_D(dtr[r][o]);
         }
       }
     }
@@ -494,7 +494,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         for (int r = 0; r < NRHS; ++r) {
           x[r] = pfma(-c, x[r], dps[((size_t)r * Z + k) * nb + t]);
           trp[r][o] = x[r];
-          dtr[r][o] = F(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
+          dtr[r][o] = to_F<F>(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
         }
       }
     }

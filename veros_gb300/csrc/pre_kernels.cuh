@@ -142,22 +142,27 @@ static __device__ __forceinline__ double taper_of(double s, double sc, double in
 static __device__ __forceinline__ double recip_neg(double d) { return recip_newton(d); }
 
 // Split form: slope, taper argument and taper in FP32 (the slope's clamped
-// denominator was formed in FP64).
-static __device__ __forceinline__ float taper_of_split(float s, double slopec, double inv_dslope) {
-  const float x = ((float)slopec - fabsf(s)) * (float)inv_dslope;
+// denominator was formed in FP64); slopec_f, inv_dslope_f are FP32 copies.
+static __device__ __forceinline__ float taper_of_split(float s, float slopec_f, float inv_dslope_f) {
+  const float x = (slopec_f - fabsf(s)) * inv_dslope_f;
   return 0.5f * (1.0f + tanhf(x));
 }
 
-// sc = slopec / dslope (the FP64 taper's argument offset)
+// The taper's constants in both precisions, formed once per CTA
+struct TaperConsts {
+  double sc, inv_dslope;       // FP64 path: slopec / dslope and 1 / dslope
+  float slopec_f, inv_dslope_f;  // split form
+};
+
 template <typename F>
-__device__ __forceinline__ F taper_t(F s, double slopec, double sc, double inv_dslope);
+__device__ __forceinline__ F taper_t(F s, const TaperConsts &c);
 template <>
-__device__ __forceinline__ double taper_t<double>(double s, double slopec, double sc, double inv_dslope) {
-  return taper_of(s, sc, inv_dslope);
+__device__ __forceinline__ double taper_t<double>(double s, const TaperConsts &c) {
+  return taper_of(s, c.sc, c.inv_dslope);
 }
 template <>
-__device__ __forceinline__ float taper_t<float>(float s, double slopec, double sc, double inv_dslope) {
-  return taper_of_split(s, slopec, inv_dslope);
+__device__ __forceinline__ float taper_t<float>(float s, const TaperConsts &c) {
+  return taper_of_split(s, c.slopec_f, c.inv_dslope_f);
 }
 
 // max(K_iso_steep, x): FP64 by integer comparison, FP32 as is
@@ -252,11 +257,11 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         mk = __ldg(a.m + o);
         const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
         if (mk & VG_MASK_T) {
-          const F Tf = F(Tc);
+          const F Tf = to_F<F>(Tc);
           if (a.eos_type == 1)
             rT = F(-Eos::betaT * Eos::rho0);
           else if (a.eos_type == 3)
-            rT = -(F(Eos::betaTs3) * (Tf - F(Eos::theta0)) + F(zeos[lev])) * F(Eos::rho0);
+            rT = -(F(Eos::betaTs3) * (Tf - F(Eos::theta0)) + to_F<F>(zeos[lev])) * F(Eos::rho0);
           else
             rT = -(F(Eos::betaT) + F(2.0 * Eos::betaTs24) * (Tf - F(Eos::theta0))) * F(Eos::rho0);
           rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
@@ -278,17 +283,18 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       }
       if (store) {
         // vertical density gradients in FP64 (exact products of the split form's FP32 values)
-        const double G0 = (double)rT * carryT[s] + (double)rS * carryS[s];  // face below (kr = 0)
-        const double G1 = (double)rT * dTz + (double)rS * dSz;                   // face above (kr = 1)
+        const double rTd = to_D(rT), rSd = to_D(rS);
+        const double G0 = rTd * carryT[s] + rSd * carryS[s];  // face below (kr = 0)
+        const double G1 = rTd * dTz + rSd * dSz;                   // face above (kr = 1)
         F(*q)[NP] = sm.q[buf];
         q[Q_RT][p] = rT;
         q[Q_RS][p] = rS;
-        q[Q_TX][p] = F(dTx);
-        q[Q_SX][p] = F(dSx);
-        q[Q_TY][p] = F(dTy);
-        q[Q_SY][p] = F(dSy);
-        q[Q_R0][p] = F(recip_neg(fmin0(G0) - kEpsln));
-        q[Q_R1][p] = F(recip_neg(fmin0(G1) - kEpsln));
+        q[Q_TX][p] = to_F<F>(dTx);
+        q[Q_SX][p] = to_F<F>(dSx);
+        q[Q_TY][p] = to_F<F>(dTy);
+        q[Q_SY][p] = to_F<F>(dSy);
+        q[Q_R0][p] = to_F<F>(recip_neg(fmin0(G0) - kEpsln));
+        q[Q_R1][p] = to_F<F>(recip_neg(fmin0(G1) - kEpsln));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
@@ -298,13 +304,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   };
 
   // slope (h, v) of plane point p: isoneutral.py:118-122, :155-159, :187-189, :205-207
-  const double sc = a.slopec * a.inv_dslope;
+  const TaperConsts tc{a.slopec * a.inv_dslope, a.inv_dslope, (float)a.slopec, (float)a.inv_dslope};
   auto slope_of = [&](const F(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
     if (!need) return Slope<F>{F(0), F(0)};
     const int pg = (h == 0 || h == 2) ? p : (h == 1 ? p - 1 : p - PX);
     const int qT = h < 2 ? Q_TX : Q_TY, qS = h < 2 ? Q_SX : Q_SY;
     const F s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
-    return Slope<F>{taper_t<F>(s, a.slopec, sc, a.inv_dslope), s};
+    return Slope<F>{taper_t<F>(s, tc), s};
   };
 
   const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
@@ -394,6 +400,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     if (k + 1 < Z) slopes_level(k + 1, (k + 1) & 1, nxt);
     const F(*pb)[NP] = sm.pub[k & 1];
     const long long o = L.at(i, j, k);
+    // the face terms' grid factors in the derived-field type
+    const F dzwF[2] = {to_F<F>(zdzw[k > 0 ? k - 1 : 0]), to_F<F>(zdzw[k])}, qzF = to_F<F>(zq_dzt[k]);
+    const F ksteepF = to_F<F>(a.ksteep);
     unsigned mk = 0;
     if (east || north || top) mk = __ldg(a.m + o);
 
@@ -411,9 +420,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
           const F t0 = cur[S_XE0 + kr].t, t1 = pb[PB_T_XW0 + kr][pc + 1];
-          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t0);
+          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t0);
           a.Aez[o + kr * a.sr] = t0 * F(cur[S_XE0 + kr].s);
-          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t1);
+          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t1);
           a.Aez[o + a.sp + kr * a.sr] = pb[PB_TS_XW0 + kr][pc + 1];
         }
       } else {
@@ -424,7 +433,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           a.Aez[o + a.sp + kr * a.sr] = 0.0;
         }
       }
-      a.K11[o] = sumz * F(zq_dzt[k]);
+      a.K11[o] = sumz * qzF;
     }
 
     // north face: Ai_nz, K_22 (isoneutral.py:137-168); jp = 0 is this point, jp = 1 the north neighbour
@@ -441,9 +450,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
           const F t0 = cur[S_YN0 + kr].t, t1 = pb[PB_T_YS0 + kr][pc + PX];
-          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t0);
+          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t0);
           a.Anz[o + kr * a.sr] = t0 * F(cur[S_YN0 + kr].s);
-          sumz += F(zdzw[k - 1 + kr]) * max_t(F(a.ksteep), diffloc * t1);
+          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t1);
           a.Anz[o + a.sp + kr * a.sr] = pb[PB_TS_YS0 + kr][pc + PX];
         }
       } else {
@@ -454,13 +463,15 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           a.Anz[o + a.sp + kr * a.sr] = 0.0;
         }
       }
-      a.K22[o] = sumz * F(zq_dzt[k]);
+      a.K22[o] = sumz * qzF;
     }
 
     // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224); kr = 0 is this point's upper slopes,
     // kr = 1 the lower slopes of the point above
     if (top && k < Z - 1) {
       F sumx = 0.0, sumy = 0.0;
+      const F dxuF[2] = {to_F<F>(sm.dxu[tx]), to_F<F>(sm.dxu[tx + 1])};
+      const F factyF[2] = {to_F<F>(sm.facty[ty]), to_F<F>(sm.facty[ty + 1])};
       if (mk & VG_MASK_W) {
         const F Kc = __ldg(a.K + o);
 #pragma unroll
@@ -471,14 +482,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
             const F ai = sl.t * F(sl.s);
             // taper*s^2 as (taper*s)*s: reuses Ai and stays finite where an FP32 s^2
             // would overflow under a vanishing taper
-            sumx += F(sm.dxu[tx + ip]) * Kc * sq_term<F>(sl.t, ai, sl.s);
+            sumx += dxuF[ip] * Kc * sq_term<F>(sl.t, ai, sl.s);
             a.Abx[o + ip * a.sp + kr * a.sr] = ai;
           }
 #pragma unroll
           for (int jp = 0; jp < 2; ++jp) {
             const Slope<F> sl = kr == 0 ? cur[jp ? S_YN1 : S_YS1] : nxt[jp ? S_YN0 : S_YS0];
             const F ai = sl.t * F(sl.s);
-            sumy += F(sm.facty[ty + jp]) * Kc * sq_term<F>(sl.t, ai, sl.s);
+            sumy += factyF[jp] * Kc * sq_term<F>(sl.t, ai, sl.s);
             a.Aby[o + jp * a.sp + kr * a.sr] = ai;
           }
         }
@@ -490,7 +501,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           a.Aby[oc] = 0.0;
         }
       }
-      a.K33[o] = sumx * F(sm.qinv_dxt[tx + 1]) + sumy * F(sm.qinv_dyt_cost[ty + 1]);
+      a.K33[o] = sumx * to_F<F>(sm.qinv_dxt[tx + 1]) + sumy * to_F<F>(sm.qinv_dyt_cost[ty + 1]);
     }
 #pragma unroll
     for (int n = 0; n < NS; ++n) cur[n] = nxt[n];
