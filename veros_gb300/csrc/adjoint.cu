@@ -59,7 +59,10 @@ enum { F_GTP = kTensorFields, F_GSP, F_GK33, F_PART };
 enum { P_LRT = 0, P_WT = 1, P_WS = 5, P_GZT = 9, P_GZS = 11, P_LVD = 13, P_LDL = 17, P_LKW = 21, P_N = 23 };
 // the forward's per-point tapers, slopes and reciprocals (detail::SLOPE_*)
 constexpr int F_SLOPES = F_PART + P_N;
-constexpr int kFields = F_SLOPES + detail::SLOPE_FIELDS;
+// mu = dt dL/dT_p on interior wet cells, scaled per direction: mu / (cost dxt),
+// mu / (cost dyt), mu / dzt for temp (0..2) and salt (3..5)
+constexpr int F_NU = F_SLOPES + detail::SLOPE_FIELDS;
+constexpr int kFields = F_NU + 6;
 
 inline size_t table_doubles(const Layout &L) { return 3 * (size_t)L.X + 4 * (size_t)L.Y + 3 * (size_t)L.Z; }
 
@@ -131,6 +134,8 @@ struct ImpArgs {
   const double *__restrict__ gTn;  // dL/dT_{n+1}
   const double *__restrict__ gSn;
   double *gTp, *gSp, *gK33;  // dL/d(right-hand side), dL/dK_33
+  double *nu;                // the scaled adjoint sources of the explicit part (F_NU)
+  long long field;
 };
 
 // Row k of the forward matrix: a_k = -delta_{k-1}/dzt_k, c_k = -delta_k/dzt_k,
@@ -151,14 +156,19 @@ __global__ void __launch_bounds__(64) adj_implicit_kernel(ImpArgs a) {
   const bool interior = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
   const int ks = interior ? a.kbot[base] - 1 : -1;  // create_water_masks (utilities.py:38-48)
   const int kw = (ks >= 0 && ks < Z) ? ks : Z;
-  // cells outside the solve pass their adjoint through
+  const long long F = a.field;
+  // cells outside the solve pass their adjoint through; dry or halo cells have no explicit part
   for (int k = 0; k < kw; ++k) {
     const long long o = base + (long long)k * L.plane;
     a.gTp[o] = a.gTn[o];
     a.gSp[o] = a.gSn[o];
     a.gK33[o] = 0.0;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) a.nu[n * F + o] = 0.0;
   }
   if (kw == Z) return;
+  // the explicit tendency's metric factors (diffusion.py:116-139)
+  const double fx = a.dt * a.gi.inv_dxt[i] * a.gi.inv_cost[j], fy = a.dt * a.gi.inv_dyt[j] * a.gi.inv_cost[j];
 
   double cp = 0.0, dp0 = 0.0, dp1 = 0.0, delta_prev = 0.0;
   for (int k = ks; k < Z; ++k) {
@@ -192,6 +202,13 @@ __global__ void __launch_bounds__(64) adj_implicit_kernel(ImpArgs a) {
     a.gTp[o] = n0;
     a.gSp[o] = n1;
     a.gK33[o] = gk;
+    const double fz = a.dt * a.gi.inv_dzt[k];
+    a.nu[o] = n0 * fx;
+    a.nu[F + o] = n0 * fy;
+    a.nu[2 * F + o] = n0 * fz;
+    a.nu[3 * F + o] = n1 * fx;
+    a.nu[4 * F + o] = n1 * fy;
+    a.nu[5 * F + o] = n1 * fz;
     y0 = n0;
     y1 = n1;
     xu0 = x0;
@@ -207,29 +224,19 @@ struct SlopeArgs {
   Grid g;
   GridInv gi;
   int eos;
-  double slopec, inv_dslope, ksteep, dt;
+  double slopec, inv_dslope, ksteep;
   const double *__restrict__ T;
   const double *__restrict__ S;
   const double *__restrict__ K;
-  const double *__restrict__ gTp;
-  const double *__restrict__ gSp;
   const double *__restrict__ gK33;
   const uint8_t *__restrict__ m;
   const double *__restrict__ slopes;  // the forward's tapers, slopes and reciprocals
+  const double *__restrict__ nu;      // the scaled adjoint sources of the explicit part
   const double *__restrict__ K11;     // the forward's tensor
   const double *__restrict__ K22;
   double *part;
   long long field;
 };
-
-// dt * dL/dT_p on interior wet points: the adjoint of the explicit tendency
-// (diffusion.py:116-139, 191-192)
-__device__ __forceinline__ double mu_at(const Layout &L, const uint8_t *m, const double *gp, double dt, long long o,
-                                        int i, int j) {
-  if (i < 2 || i >= L.X - 2 || j < 2 || j >= L.Y - 2) return 0.0;
-  if (!(__ldg(m + o) & VG_MASK_T)) return 0.0;
-  return dt * __ldg(gp + o);
-}
 
 __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const Layout &L = a.L;
@@ -279,7 +286,8 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const Eos eos{a.eos};
   const double rT = wetP ? eos.drdT(Tc, a.g.zt[k]) : 0.0, rS = wetP ? eos.drdS() : 0.0;
   // the clamped reciprocals 1/(min(0, G) - epsln) of the forward; G >= 0 gives exactly R_flat
-  const double R_flat = detail::recip_neg(fmin0(0.0) - kEpsln);
+  const long long R_flat_bits = __double_as_longlong(detail::recip_neg(fmin0(0.0) - kEpsln));
+  const double c2 = -2.0 * a.inv_dslope;
   const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
 
   // which faces carry a term: face h (east/north terms) and face v (top terms)
@@ -287,42 +295,35 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
                       colN && j >= 1 && j < Y - 2 && mH[2], colN && j >= 2 && j < Y - 1 && mH[3]};
   const bool vT[2] = {inter && mWv[0], inter && mWv[1]};
 
-  // adjoints of the fluxes on the faces (diffusion.py:116-139)
+  // adjoints of the fluxes on the faces (diffusion.py:116-139) from the
+  // scaled sources nu: lambda_fe(i) = nu_x(i) - nu_x(i+1), and so on
   double lfT[4] = {0, 0, 0, 0}, lfS[4] = {0, 0, 0, 0}, lftT[2] = {0, 0}, lftS[2] = {0, 0};
   {
-    const double cT = mu_at(L, m, a.gTp, a.dt, o, i, j), cS = mu_at(L, m, a.gSp, a.dt, o, i, j);
+    const double *nu = a.nu + o;
+    auto nT = [&](int n, long long off) { return __ldg(nu + n * F + off); };
     if (vE[0]) {
-      const double eT = mu_at(L, m, a.gTp, a.dt, o + 1, i + 1, j), eS = mu_at(L, m, a.gSp, a.dt, o + 1, i + 1, j);
-      lfT[0] = (cT * gi.inv_dxt[i] - eT * gi.inv_dxt[i + 1]) * icx;
-      lfS[0] = (cS * gi.inv_dxt[i] - eS * gi.inv_dxt[i + 1]) * icx;
+      lfT[0] = nT(0, 0) - nT(0, 1);
+      lfS[0] = nT(3, 0) - nT(3, 1);
     }
     if (vE[1]) {
-      const double wT = mu_at(L, m, a.gTp, a.dt, o - 1, i - 1, j), wS = mu_at(L, m, a.gSp, a.dt, o - 1, i - 1, j);
-      lfT[1] = (wT * gi.inv_dxt[i - 1] - cT * gi.inv_dxt[i]) * icx;
-      lfS[1] = (wS * gi.inv_dxt[i - 1] - cS * gi.inv_dxt[i]) * icx;
+      lfT[1] = nT(0, -1) - nT(0, 0);
+      lfS[1] = nT(3, -1) - nT(3, 0);
     }
-    const double cy = gi.inv_dyt[j] * icx;
     if (vE[2]) {
-      const double nT = mu_at(L, m, a.gTp, a.dt, o + PW, i, j + 1), nS = mu_at(L, m, a.gSp, a.dt, o + PW, i, j + 1);
-      const double ny = gi.inv_dyt[j + 1] * gi.inv_cost[j + 1];
-      lfT[2] = a.g.cosu[j] * (cT * cy - nT * ny);
-      lfS[2] = a.g.cosu[j] * (cS * cy - nS * ny);
+      lfT[2] = a.g.cosu[j] * (nT(1, 0) - nT(1, PW));
+      lfS[2] = a.g.cosu[j] * (nT(4, 0) - nT(4, PW));
     }
     if (vE[3]) {
-      const double sT = mu_at(L, m, a.gTp, a.dt, o - PW, i, j - 1), sS = mu_at(L, m, a.gSp, a.dt, o - PW, i, j - 1);
-      const double sy = gi.inv_dyt[j - 1] * gi.inv_cost[j - 1];
-      lfT[3] = a.g.cosu[j - 1] * (sT * sy - cT * cy);
-      lfS[3] = a.g.cosu[j - 1] * (sS * sy - cS * cy);
+      lfT[3] = a.g.cosu[j - 1] * (nT(1, -PW) - nT(1, 0));
+      lfS[3] = a.g.cosu[j - 1] * (nT(4, -PW) - nT(4, 0));
     }
     if (vT[0]) {
-      const double dT = mu_at(L, m, a.gTp, a.dt, o - PL, i, j), dS = mu_at(L, m, a.gSp, a.dt, o - PL, i, j);
-      lftT[0] = dT * gi.inv_dzt[k - 1] - cT * gi.inv_dzt[k];
-      lftS[0] = dS * gi.inv_dzt[k - 1] - cS * gi.inv_dzt[k];
+      lftT[0] = nT(2, -PL) - nT(2, 0);
+      lftS[0] = nT(5, -PL) - nT(5, 0);
     }
     if (vT[1]) {
-      const double uT = mu_at(L, m, a.gTp, a.dt, o + PL, i, j), uS = mu_at(L, m, a.gSp, a.dt, o + PL, i, j);
-      lftT[1] = cT * gi.inv_dzt[k] - uT * gi.inv_dzt[k + 1];
-      lftS[1] = cS * gi.inv_dzt[k] - uS * gi.inv_dzt[k + 1];
+      lftT[1] = nT(2, 0) - nT(2, PL);
+      lftS[1] = nT(5, 0) - nT(5, PL);
     }
   }
 
@@ -377,8 +378,12 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
       if (!Ef && !Tf) continue;
       const double s = __ldg(a.slopes + o + (detail::SLOPE_S + h * 2 + v) * F);
       const double t = __ldg(a.slopes + o + (detail::SLOPE_T + h * 2 + v) * F);
-      const double sg = (s > 0.0) ? 1.0 : (s < 0.0 ? -1.0 : 0.0);
-      const double tp = -2.0 * sg * t * (1.0 - t) * a.inv_dslope;  // d taper / ds
+      // d taper / ds = -2 sign(s) t (1 - t) / dslope (0 at s = 0); the sign by integer operations
+      const long long sb = __double_as_longlong(s);
+      const double tq = t * (1.0 - t) * c2;
+      const double tp = (sb & 0x7FFFFFFFFFFFFFFFLL) ? __longlong_as_double(__double_as_longlong(tq) ^
+                                                                            (sb & (long long)0x8000000000000000ULL))
+                                                    : 0.0;
       const double tst = t + s * tp;                              // d (taper s) / ds
       const double ts = t * s;
       double gs = 0.0;
@@ -386,7 +391,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
         // Ai = taper s, K_11 += dzw max(K_iso_steep, diffloc taper) / (4 dzt)
         const double lfv = lfT[h] * vdT[v] + lfS[h] * vdS[v];
         const double dlq = dl[h] * q;
-        const double kq = dl[h] * t > a.ksteep ? gKh[h] * dzwv[v] * q : 0.0;
+        const double kq = dgt(dl[h] * t, a.ksteep) ? gKh[h] * dzwv[v] * q : 0.0;
         gs += lfv * dlq * tst + kq * dl[h] * tp;
         ldl[h] += kq * t + lfv * ts * q;
         lvd[0][v] += lfT[h] * ts * dlq;
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
         lhd[1][h] += lftS[v] * f;
       }
       const double lN = -gs * R[v];
-      if (R[v] != R_flat) lG[v] -= gs * s * R[v];  // d min(0, G)/dG = 1 where G < 0
+      if (__double_as_longlong(R[v]) != R_flat_bits) lG[v] -= gs * s * R[v];  // d min(0, G)/dG = 1 where G < 0
       lrT += lN * gxT[h];
       nsum[h] += lN;
     }
@@ -578,11 +583,12 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
     return st;
   double *gTp = base + adj::F_GTP * F, *gSp = base + adj::F_GSP * F, *gK33 = base + adj::F_GK33 * F;
   double *part = base + adj::F_PART * F;
+  double *nu = base + adj::F_NU * F;
 
   // 3. implicit part
   {
-    adj::ImpArgs a{L, gi, set->dt_tracer, f->kbot, ten.K_33, f->temp_new, f->salt_new, f->gtemp_new, f->gsalt_new,
-                   gTp, gSp, gK33};
+    adj::ImpArgs a{L,   gi,  set->dt_tracer, f->kbot, ten.K_33, f->temp_new, f->salt_new, f->gtemp_new,
+                   f->gsalt_new, gTp, gSp, gK33, nu, F};
     int nb = 64;
     size_t smem = 3 * (size_t)L.Z * nb * sizeof(double);
     if (smem > 160 * 1024) {
@@ -601,9 +607,9 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   const dim3 block(32, 4), grd((L.X + 31) / 32, (L.Y + 3) / 4, L.Z);
   // 4. slope adjoints
   {
-    adj::SlopeArgs a{L,          g,          gi,      set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
-                     set->K_iso_steep, set->dt_tracer, f->temp, f->salt, f->K_iso, gTp, gSp, gK33, f->mask_bits,
-                     slopes,     ten.K_11,   ten.K_22, part, F};
+    adj::SlopeArgs a{L,      g,    gi,       set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
+                     set->K_iso_steep, f->temp, f->salt, f->K_iso, gK33, f->mask_bits, slopes, nu, ten.K_11,
+                     ten.K_22, part, F};
     adj::adj_slope_kernel<<<grd, block, 0, s>>>(a);
     if ((st = check_launch("adj_slope_kernel"))) return st;
   }

@@ -66,6 +66,14 @@ __device__ __forceinline__ double dmax(double a, double b) {
   return ia >= ib ? a : b;
 }
 
+// a > b by an integer comparison of the bit patterns mapped to a monotone order
+__device__ __forceinline__ bool dgt(double a, double b) {
+  long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  ia ^= (ia >> 63) & 0x7FFFFFFFFFFFFFFFLL;
+  ib ^= (ib >> 63) & 0x7FFFFFFFFFFFFFFFLL;
+  return ia > ib;
+}
+
 // double -> float by truncating the mantissa (|x| within the FP32 normal range)
 __device__ __forceinline__ float dtof_trunc(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);

@@ -305,11 +305,15 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 
   // slope (h, v) of plane point p: isoneutral.py:118-122, :155-159, :187-189, :205-207
   const TaperConsts tc{a.slopec * a.inv_dslope, a.inv_dslope, (float)a.slopec, (float)a.inv_dslope};
-  auto slope_of = [&](const F(*q)[NP], int p, int h, int v, bool need) -> Slope<F> {
-    if (!need) return Slope<F>{F(0), F(0)};
+  // the numerator drdT dT/dh + drdS dS/dh, shared by the two slopes of face h
+  auto numer_of = [&](const F(*q)[NP], int p, int h) -> F {
     const int pg = (h == 0 || h == 2) ? p : (h == 1 ? p - 1 : p - PX);
     const int qT = h < 2 ? Q_TX : Q_TY, qS = h < 2 ? Q_SX : Q_SY;
-    const F s = -(q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg]) * q[v ? Q_R1 : Q_R0][p];
+    return q[Q_RT][p] * q[qT][pg] + q[Q_RS][p] * q[qS][pg];
+  };
+  auto slope_of = [&](const F(*q)[NP], int p, F numer, int v, bool need) -> Slope<F> {
+    if (!need) return Slope<F>{F(0), F(0)};
+    const F s = -numer * q[v ? Q_R1 : Q_R0][p];
     return Slope<F>{taper_t<F>(s, tc), s};
   };
 
@@ -340,9 +344,12 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                         (qm[pc - PX] & VG_MASK_V) != 0};
     const bool mWv[2] = {(m & kMaskWBelow) != 0, (m & VG_MASK_W) != 0};
 #pragma unroll
-    for (int h = 0; h < 4; ++h)
-#pragma unroll
-      for (int v = 0; v < 2; ++v) out[h * 2 + v] = slope_of(q, pc, h, v, (v == 1 || lev > 0) && (mH[h] || mWv[v]));
+    for (int h = 0; h < 4; ++h) {
+      const bool need0 = lev > 0 && (mH[h] || mWv[0]), need1 = mH[h] || mWv[1];
+      const F numer = (need0 || need1) ? numer_of(q, pc, h) : F(0);
+      out[h * 2] = slope_of(q, pc, numer, 0, need0);
+      out[h * 2 + 1] = slope_of(q, pc, numer, 1, need1);
+    }
     if (a.slopes && lev < ke && own_in) {
       double *sl = a.slopes + L.at(i0 + tx, j0 + ty, lev);
       const long long F_ = a.slope_field;
@@ -364,9 +371,10 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     if (pring >= 0) {
       const bool mHr = hring == 1 ? (qm[pring - 1] & VG_MASK_U) != 0 : (qm[pring - PX] & VG_MASK_V) != 0;
       const int base_t = hring == 1 ? PB_T_XW0 : PB_T_YS0, base_ts = hring == 1 ? PB_TS_XW0 : PB_TS_YS0;
+      const F numer = mHr ? numer_of(q, pring, hring) : F(0);
 #pragma unroll
       for (int v = 0; v < 2; ++v) {
-        const Slope<F> sl = slope_of(q, pring, hring, v, mHr && (v == 1 || lev > 0));
+        const Slope<F> sl = slope_of(q, pring, numer, v, mHr && (v == 1 || lev > 0));
         pb[base_t + v][pring] = sl.t;
         pb[base_ts + v][pring] = sl.t * F(sl.s);
         if (a.slopes && lev < ke && ring_store && ring_i < L.X && ring_j < L.Y) {
