@@ -83,15 +83,17 @@ static __device__ __forceinline__ float pfma(float x, float y, float z) { return
 // tensor once. Operand order per tracer is the reference's.
 
 // east face of cell (i, j, k), valid for i in [1, X-2), j in [2, Y-2) (diffusion.py:25-47)
+// diffloc of an east/north face: the mean of K1 = s1 K over the face's two
+// points on levels k and k-1 (diffusion.py:21-23, :48-50), from the pair sums
+// K(P) + K(P') of the two levels (s1 = +-1)
 template <typename F>
-__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, int k, F inv_cost_dxu, F c[5]) {
-  const Layout &L = a.L;
-  const F s1 = to_F<F>(a.s1);  // +-1: s1 * (sum) equals the sum of s1 * K
-  F diffloc;
-  if (k >= 1)
-    diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + 1) + ld(a.K, o + 1 - L.plane)));
-  else
-    diffloc = F(0.5) * (s1 * (ld(a.K, o) + ld(a.K, o + 1)));
+__device__ __forceinline__ F face_diffloc(F pair, F pair_below, int k, double s1) {
+  const F q = s1 > 0.0 ? (k >= 1 ? F(0.25) : F(0.5)) : (k >= 1 ? F(-0.25) : F(-0.5));
+  return q * (k >= 1 ? pair + pair_below : pair);
+}
+
+template <typename F>
+__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_cost_dxu, F c[5]) {
   c[0] = pm(diffloc, ld(a.Aez, o));
   c[1] = pm(diffloc, ld(a.Aez, o + a.sp));
   c[2] = pm(diffloc, ld(a.Aez, o + a.sr));
@@ -115,15 +117,7 @@ __device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long l
 
 // north face of cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
 template <typename F>
-__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, int k, F inv_dyu, F c[5]) {
-  const Layout &L = a.L;
-  const long long P = L.pitch;
-  const F s1 = to_F<F>(a.s1);
-  F diffloc;
-  if (k >= 1)
-    diffloc = F(0.25) * (s1 * (ld(a.K, o) + ld(a.K, o - L.plane) + ld(a.K, o + P) + ld(a.K, o + P - L.plane)));
-  else
-    diffloc = F(0.5) * (s1 * (ld(a.K, o) + ld(a.K, o + P)));
+__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_dyu, F c[5]) {
   c[0] = pm(diffloc, ld(a.Anz, o));
   c[1] = pm(diffloc, ld(a.Anz, o + a.sp));
   c[2] = pm(diffloc, ld(a.Anz, o + a.sr));
@@ -150,7 +144,7 @@ __device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long 
 // top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111)
 template <typename F>
 __device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F c[8]) {
-  const F diffloc = to_F<F>(a.s2) * ld(a.K, o);
+  const F diffloc = a.s2 == 1.0 ? ld(a.K, o) : to_F<F>(a.s2) * ld(a.K, o);  // K2 = s2 K (diffusion.py:16)
   const F dx = pm(diffloc, inv_cost), ds = pm(diffloc, cosu_s), dc = pm(diffloc, cosu_c);
   c[0] = pm(dx, ld(a.Abx, o));
   c[1] = pm(dx, ld(a.Abx, o + a.sr));
@@ -293,8 +287,15 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
         }
       }
       F ce[5], cn[5];
-      east_coef(a, o, k, inv_cost_dxu, ce);
-      north_coef(a, o, k, inv_dyu, cn);
+      const F kc = ld(a.K, o), pe = kc + ld(a.K, o + 1), pn = kc + ld(a.K, o + P);
+      F pe_below = 0, pn_below = 0;
+      if (k >= 1) {
+        const F kd = ld(a.K, o - Q);
+        pe_below = kd + ld(a.K, o + 1 - Q);
+        pn_below = kd + ld(a.K, o + P - Q);
+      }
+      east_coef(a, o, face_diffloc(pe, pe_below, k, a.s1), inv_cost_dxu, ce);
+      north_coef(a, o, face_diffloc(pn, pn_below, k, a.s1), inv_dyu, cn);
       F ct[8];
       if (up) top_coef(a, o, inv_cost, cosu_s, cosu_c, ct);
 #pragma unroll
@@ -342,14 +343,18 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     if (halo_n) {
       const long long oh = L.at(hi_n, j0 - 1, k);
       F cn[5];
-      north_coef(a, oh, k, h_inv_dyu, cn);
+      const F pn = ld(a.K, oh) + ld(a.K, oh + L.pitch);
+      const F pnb = k >= 1 ? ld(a.K, oh - L.plane) + ld(a.K, oh + L.pitch - L.plane) : F(0);
+      north_coef(a, oh, face_diffloc(pn, pnb, k, a.s1), h_inv_dyu, cn);
 #pragma unroll
       for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu, qz);
     }
     if (halo_e) {
       const long long oh = L.at(i0 - 1, hj_e, k);
       F ce[5];
-      east_coef(a, oh, k, h_inv_cost_dxu, ce);
+      const F pe = ld(a.K, oh) + ld(a.K, oh + 1);
+      const F peb = k >= 1 ? ld(a.K, oh - L.plane) + ld(a.K, oh + 1 - L.plane) : F(0);
+      east_coef(a, oh, face_diffloc(pe, peb, k, a.s1), h_inv_cost_dxu, ce);
 #pragma unroll
       for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce, qz);
     }
@@ -361,7 +366,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
         F e = pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy));
         e = pfma(ft[r] - ft_prev[r], to_F<F>(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
         t.dtr_iso[o] = add_(t.dtr_iso[o], e);
-        t.trp[o] = radd(t.trp[o], rmul(t.dt, to_D(e)));
+        t.trp[o] = fma(t.dt, to_D(e), t.trp[o]);  // tr[taup1] += dt * dtr (diffusion.py:192)
       }
     }
     if (own) {
