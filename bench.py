@@ -393,6 +393,134 @@ def run_quarter_degree(device, steps=100):
     return out
 
 
+def run_aux(device, reps=20):
+    """The path's neighbouring kernels, each timed alone on the 1-degree
+    workload (360 x 180 x 60): vertical mixing of temp and salt
+    (vertmix_kernel), the streamfunction diagnostics (streamfunction_kernel),
+    the generic solve_implicit in the reference's (X, Y, Z) layout
+    (pivoting_solve_kernel), the XLA TDMA custom-call target in its
+    system-fastest layout (xla_thomas_kernel), and the energy branch of the
+    step (one energy_kernel launch for temp and salt plus the flux stores
+    it reads, as the difference between the energy and the plain diffusion
+    stage).
+
+    Each call runs after a 256 MiB write that evicts the 129 MB L2, and is
+    timed alone with CUDA events on torch's current stream; ms is the median
+    over ``reps`` calls. GB/s = algorithmic bytes of the call (bytes per cell
+    below x cells) / ms."""
+    import ctypes
+
+    import torch
+
+    from veros_gb300 import _capi, isoneutral, synthetic, thermodynamics
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    peak, peak_kind = _peaks()
+    host = synthetic.global_1deg_state(seed=0)
+    dev = DeviceState.from_host(host, device=device)
+    IsoneutralStepper(dev).step(1)  # Ai_ez / Ai_nz for the streamfunction
+    torch.cuda.synchronize()
+    lib = _capi.load()
+    cells_pad = dev.plane * dev.Z
+    kb = host.arrays["kbot"].reshape(-1)  # one column per (i, j), halo included
+    ncols, nz = kb.size, host.nz
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        ms = []
+        for _ in range(reps):
+            flush.fill_(1)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+
+    out = {"workload": f"{host.nx}x{host.ny}x{host.nz} at 1 degree, eq 3", "reps": reps,
+           "timing": "median of per-call CUDA events, L2 evicted before each call", "peak_gbs": peak,
+           "peak_source": peak_kind, "kernels": {}}
+
+    def report(name, kernel, ms, nbytes, cells, note):
+        gbs = nbytes / (ms / 1e3) / 1e9
+        out["kernels"][name] = {"kernel": kernel, "ms": ms, "cells": cells, "algorithmic_bytes": nbytes,
+                                "achieved_gbs": gbs, "frac": gbs / peak, "bytes": note}
+
+    report("vertmix_tempsalt", "vertmix_kernel", timed(lambda: thermodynamics.run_vertmix(dev)), 56 * cells_pad,
+           cells_pad,
+           "kappaH 8, temp and salt read+write 32, dtemp_vmix and dsalt_vmix 16")
+    report("isoneutral_diag_streamfunction", "streamfunction_kernel",
+           timed(lambda: isoneutral._run_streamfunction(dev)), 88 * cells_pad, cells_pad,
+           "K_gm 8, Ai_ez 32, Ai_nz 32, B1_gm and B2_gm 16")
+
+    g = torch.Generator(device="cpu").manual_seed(5)
+    shp = (ncols, nz)
+    av = -torch.rand(shp, generator=g, dtype=torch.float64).to(device)
+    cv = -torch.rand(shp, generator=g, dtype=torch.float64).to(device)
+    bv = (3.0 + torch.rand(shp, generator=g, dtype=torch.float64)).to(device)
+    dv = torch.randn(shp, generator=g, dtype=torch.float64).to(device)
+    ks = torch.from_numpy(np.where(kb > 0, kb - 1, nz)).to(device)  # land columns: no water
+    kk = torch.arange(nz, device=device)
+    water = (kk[None, :] >= ks[:, None].long()).to(torch.uint8).contiguous()
+    edge = (kk[None, :] == ks[:, None].long()).to(torch.uint8).contiguous()
+    res = torch.empty(shp, dtype=torch.float64, device=device)
+    bad = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def generic():
+        st = lib.vg_solve_implicit_f64(ncols, 1, nz, nz, 0, 1, av.data_ptr(), bv.data_ptr(), cv.data_ptr(),
+                                       dv.data_ptr(), water.data_ptr(), edge.data_ptr(), None, None, res.data_ptr(),
+                                       bad.data_ptr(), torch.cuda.current_stream(device).cuda_stream)
+        _capi.check(st, "solve_implicit")
+
+    nwet = int(water.sum())
+    report("solve_implicit", "pivoting_solve_kernel", timed(generic), 42 * nwet + 10 * (ncols * nz - nwet),
+           ncols * nz, "water cells: a, b, c, d 32, water and edge masks 2, solution 8; other cells: masks 2, "
+           "zero 8; (X, Y, Z) layout")
+
+    at, bt, ct, dt_ = (x.t().contiguous() for x in (av, bv, cv, dv))
+    outt = torch.empty_like(dt_)
+    bufs = (ctypes.c_void_p * 6)(*(t.data_ptr() for t in (at, bt, ct, dt_, outt, outt)))
+    desc = np.array([ncols, nz], dtype=np.int32).tobytes()
+
+    def xla():
+        lib.vg_tdma_cuda_double(ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream), bufs, desc,
+                                len(desc))
+
+    report("tdma_cuda_double", "xla_thomas_kernel", timed(xla), 40 * ncols * nz, ncols * nz,
+           "a, b, c, d 32, solution 8; system-fastest layout")
+    if _capi.last_error():
+        raise RuntimeError(_capi.last_error())
+    del av, bv, cv, dv, at, bt, ct, dt_, outt, res, water, edge
+
+    stages = {}
+    for energy in (False, True):
+        h = host.copy()
+        h.settings["enable_conserve_energy"] = energy
+        d = DeviceState.from_host(h, device=device)
+        stp = IsoneutralStepper(d)
+        for _ in range(3):
+            stp.step_stages()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(reps)]
+        for e in ev:
+            stp.step_stages(e)
+        torch.cuda.synchronize()
+        stages[energy] = float(np.median([e[2].elapsed_time(e[3]) for e in ev]))
+        del d, stp
+    extra = stages[True] - stages[False]
+    out["energy_branch"] = {"diffusion_stage_ms": stages[False], "diffusion_stage_ms_energy": stages[True],
+                            "extra_ms": extra,
+                            "achieved_gbs": 105 * cells_pad / (extra / 1e3) / 1e9 if extra > 0 else None,
+                            "bytes": "energy_kernel per cell: per tracer int_drhodX 8, east/north/top fluxes 24, "
+                                     "tracer 8; K_33 8, P_diss_iso read+write 16, mask 1"}
+    del dev, flush
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -484,7 +612,7 @@ def run_gb300(args):
 
     launches = args.steps * stepper.launches_per_step()
     ensemble = adjoint = None
-    if not (args.no_ensemble and args.no_adjoint and not args.quarter_degree):
+    if not (args.no_ensemble and args.no_adjoint and not args.quarter_degree and not args.aux):
         del dev, stepper
         torch.cuda.empty_cache()
     if not args.no_ensemble:
@@ -492,6 +620,7 @@ def run_gb300(args):
     if not args.no_adjoint:
         adjoint = run_adjoint(device)
     quarter = run_quarter_degree(device) if args.quarter_degree else None
+    aux = run_aux(device) if args.aux else None
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -530,6 +659,7 @@ def run_gb300(args):
         "ensemble": ensemble,
         "adjoint": adjoint,
         "quarter_degree": quarter,
+        "aux": aux,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))
@@ -548,6 +678,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 8-step rollout adjoint measurement")
     ap.add_argument("--quarter-degree", action="store_true",
                     help="add the 0.25-degree split-versus-FP64 measurement (100 steps, ~25 GB of device memory)")
+    ap.add_argument("--aux", action="store_true",
+                    help="add per-kernel timings of vertical mixing, streamfunction, the generic and XLA tridiagonal "
+                         "solves and the energy branch (1 degree)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -103,6 +103,14 @@ __device__ __forceinline__ double recip_newton(double d) {
   return fma(r, e, r);
 }
 
+// 1/d for any d: recip_newton where the FP32 seed is a normal number
+// (|d| in [2^-125, 2^125)), the IEEE quotient elsewhere (zero, subnormal,
+// huge, inf, NaN), chosen by an integer test of the exponent field.
+__device__ __forceinline__ double recip_any(double d) {
+  const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(d) >> 52) & 0x7FFu;
+  return (e - (1023u - 125u) < 250u) ? recip_newton(d) : 1.0 / d;
+}
+
 // FP64 -> FP32 rounded to nearest (ties away from zero) by integer
 // operations; magnitudes below the FP32 normal range flush to a signed zero,
 // above it to infinity. The split form's conversions use it.

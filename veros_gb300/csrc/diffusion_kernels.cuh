@@ -1,7 +1,8 @@
 // Isoneutral tracer diffusion (FP64), the work of
 // veros/core/isoneutral/diffusion.py:9-295 and veros/core/diffusion.py:9-62.
 //
-// Two launches per tracer (three with the energy branch):
+// Two launches per tracer, or per temp-and-salt pair (one more with the
+// energy branch):
 //  1. flux_div_kernel  2.5-D tiled: a CTA owns 32 x 8 interior columns and
 //                      walks k upward. Per level it forms the east, north and
 //                      top fluxes (diffusion.py:9-113) of its faces plus the
@@ -15,9 +16,10 @@
 //                      c'/d' live in shared memory, shared by temp and salt
 //                      when both are diffused together, and the second
 //                      dtracer_iso term (:204).
-//  3. energy_kernel    (enable_conserve_energy) dissipation on the W grid and
-//                      the vertical-mixing term added to P_diss (:234-281),
-//                      from the fluxes step 1 saved in the scratch buffer.
+//  3. energy_kernel    (enable_conserve_energy) one thread per column and
+//                      chunk of levels: dissipation on the W grid and the
+//                      vertical-mixing term added to P_diss (:234-281), from
+//                      the fluxes step 1 saved in the scratch buffer.
 #pragma once
 
 #include "common.cuh"
@@ -540,69 +542,118 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs<F> a, DiffArgs<F>
   implicit_body<F, NRHS>(a, b2, smem, blockIdx.x);
 }
 
-// Scratch flux readers: zero outside the ranges the reference defines.
+// Energy branch (veros/core/isoneutral/diffusion.py:234-281 with
+// veros/core/diffusion.py:9-62) for one tracer, or for temp then salt, which
+// add into the same P_diss in that order. One thread per column (i, j),
+// i in [1, X-2], j in [1, Y-2], walking the levels [k0, k0 + kc) of one chunk;
+// the dissipation at k + 1, which the W-grid interpolation at k needs, and
+// int_drhodX at k + 1 are carried to the next level. Divisions by the grid
+// spacings are multiplications by reciprocals that each CTA forms once in
+// shared memory (1/dxt of its columns, the 1/cost factors of its rows, and per
+// level 1/dzw, -g/rho_0/dzw and dzw_pad/dzw). Every product and sum is rounded
+// explicitly, so the one- and two-tracer launches give identical bits.
 template <typename F>
-__device__ __forceinline__ F fe_at(const DiffArgs<F> &a, int i, int j, int k) {
-  return (i >= 1 && i < a.L.X - 2 && j >= 2 && j < a.L.Y - 2) ? a.fe[a.L.at(i, j, k)] : F(0.0);
-}
+struct EnergyColumn {
+  bool fe0, fe1, fn0, fn1;  // saved east/north fluxes exist at i, i-1 / j, j-1
+  F cx, cy;                 // 0.5 g / rho_0 / (dxt cost), ... / (dyt cost)
+};
+
+// Dissipation at T point o (diffusion.py:9-36); *I0 receives int_drhodX there.
 template <typename F>
-__device__ __forceinline__ F fn_at(const DiffArgs<F> &a, int i, int j, int k) {
-  return (i >= 2 && i < a.L.X - 2 && j >= 1 && j < a.L.Y - 2) ? a.fn[a.L.at(i, j, k)] : F(0.0);
+__device__ __forceinline__ F diss_col(const DiffArgs<F> &a, const EnergyColumn<F> &c, long long o, long long pitch,
+                                      F *I0) {
+  const F I = ld(a.idr, o);
+  *I0 = I;
+  const F fe0 = c.fe0 ? ld(a.fe, o) : F(0.0), fe1 = c.fe1 ? ld(a.fe, o - 1) : F(0.0);
+  const F fn0 = c.fn0 ? ld(a.fn, o) : F(0.0), fn1 = c.fn1 ? ld(a.fn, o - pitch) : F(0.0);
+  const F ex = pfma(ld(a.idr, o + 1) - I, fe0, pm(I - ld(a.idr, o - 1), fe1));
+  const F ny = pfma(ld(a.idr, o + pitch) - I, fn0, pm(I - ld(a.idr, o - pitch), fn1));
+  return pfma(ex, c.cx, pm(ny, c.cy));
 }
 
-// Dissipation at T points (veros/core/diffusion.py:9-36); zero on the outer ring.
-template <typename F>
-__device__ __forceinline__ F diss_at(const DiffArgs<F> &a, int i, int j, int k) {
-  const Layout &L = a.L;
-  const long long o = L.at(i, j, k);
-  const F c = F(0.5 * a.grav / a.rho0);
-  const F I0 = ld(a.idr, o);
-  const F ex = (ld(a.idr, o + 1) - I0) * fe_at(a, i, j, k) + (I0 - ld(a.idr, o - 1)) * fe_at(a, i - 1, j, k);
-  const F ny =
-      (ld(a.idr, o + L.pitch) - I0) * fn_at(a, i, j, k) + (I0 - ld(a.idr, o - L.pitch)) * fn_at(a, i, j - 1, k);
-  const double cost = a.g.cost[j];
-  return c * ex / F(a.g.dxt[i] * cost) + c * ny / F(a.g.dyt[j] * cost);
-}
+constexpr int kEnergyTX = 32, kEnergyTY = 4, kEnergyMaxZ = 512;
 
-template <typename F>
-__global__ void __launch_bounds__(128) energy_kernel(DiffArgs<F> a) {
-  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = 1 + blockIdx.y;
-  const int k = blockIdx.z;
-  const Layout &L = a.L;
-  if (i >= L.X - 1) return;
+template <typename F, int NTR>
+__global__ void __launch_bounds__(kEnergyTX *kEnergyTY) energy_kernel(DiffArgs<F> a0, DiffArgs<F> a1, int kc) {
+  __shared__ double inv_dxt[kEnergyTX], c_cost[kEnergyTY], c_dyt_cost[kEnergyTY];
+  __shared__ F gidz[kEnergyMaxZ], idz_s[kEnergyMaxZ], ratio_s[kEnergyMaxZ];
+  const Layout &L = a0.L;
   const int Z = L.Z;
-  const long long o = L.at(i, j, k);
-  const int ks = a.kbot[L.at2(i, j)] - 1;
-  const bool land = ks >= 0;  // "land_mask" of create_water_masks: column has water
-
-  // dissipation_on_wgrid (veros/core/diffusion.py:39-62)
-  const F d0 = diss_at(a, i, j, k);
-  F dw;
-  if (k < Z - 1) {
-    const F d1 = diss_at(a, i, j, k + 1);
-    const F edge = (land && k == ks) ? F(1.0) : F(0.0);
-    const F water = (land && k > ks) ? F(1.0) : F(0.0);
-    const F dzw_pad = F(a.g.dzw[k > 0 ? k - 1 : 0]);
-    dw = (F(0.5) * (d0 + d1) + F(0.5) * (d0 * dzw_pad / F(a.g.dzw[k]))) * edge + F(0.5) * (d0 + d1) * water;
-  } else {
-    dw = d0 * (land ? F(1.0) : F(0.0));
-  }
-  F P = a.P[o] + dw;
-
-  // vertical-mixing term (diffusion.py:254-279)
-  if (i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2 && k < Z - 1) {
-    const F mW = (__ldg(a.m + o) & VG_MASK_W) ? F(1.0) : F(0.0);
-    const F fxa = (-ld(a.idr, o + L.plane) + ld(a.idr, o)) / F(a.g.dzw[k]);
-    const F g = F(-a.grav / a.rho0) * fxa;
-    if (a.iso) {
-      const F dtrz = F(a.trp[o + L.plane] - a.trp[o]);
-      P = P + g * (a.ft[o] * mW + ld(a.K33, o) * dtrz / F(a.g.dzw[k]) * mW);
-    } else {
-      P = P + g * a.ft[o] * mW;
+  const int k0 = blockIdx.z * kc, k1 = min(Z, k0 + kc);
+  const int i = 1 + blockIdx.x * kEnergyTX + threadIdx.x;
+  const int j = 1 + blockIdx.y * kEnergyTY + threadIdx.y;
+  {
+    const int tid = threadIdx.y * kEnergyTX + threadIdx.x;
+    const double c = 0.5 * a0.grav / a0.rho0;
+    if (tid < kEnergyTX) {
+      const int ii = 1 + blockIdx.x * kEnergyTX + tid;
+      inv_dxt[tid] = ii < L.X - 1 ? 1.0 / a0.g.dxt[ii] : 0.0;
+    } else if (tid < kEnergyTX + kEnergyTY) {
+      const int r = tid - kEnergyTX, jj = 1 + blockIdx.y * kEnergyTY + r;
+      const double cost = jj < L.Y - 1 ? a0.g.cost[jj] : 1.0;
+      c_cost[r] = c / cost;
+      c_dyt_cost[r] = jj < L.Y - 1 ? c / (a0.g.dyt[jj] * cost) : 0.0;
+    }
+    for (int t = tid; t < k1 - k0; t += kEnergyTX * kEnergyTY) {
+      const int k = k0 + t;
+      const double idz = 1.0 / a0.g.dzw[k];
+      idz_s[t] = to_F<F>(idz);
+      gidz[t] = to_F<F>(-a0.grav / a0.rho0 * idz);
+      ratio_s[t] = to_F<F>(a0.g.dzw[k > 0 ? k - 1 : 0] / a0.g.dzw[k]);  // dzw_pad[k] / dzw[k] (diffusion.py:53-55)
     }
   }
-  a.P[o] = P;
+  __syncthreads();
+  if (i >= L.X - 1 || j >= L.Y - 1) return;
+  const DiffArgs<F> *A[2] = {&a0, &a1};
+
+  const int ks = a0.kbot[L.at2(i, j)] - 1;
+  const bool land = ks >= 0;  // "land_mask" of create_water_masks: the column has water
+  const bool inner = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  EnergyColumn<F> col;
+  col.fe0 = i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  col.fe1 = i >= 2 && col.fe0;
+  col.fn0 = i >= 2 && i < L.X - 2 && j < L.Y - 2;
+  col.fn1 = j >= 2 && col.fn0;
+  col.cx = to_F<F>(pm(c_cost[threadIdx.y], inv_dxt[threadIdx.x]));
+  col.cy = to_F<F>(c_dyt_cost[threadIdx.y]);
+  const F ratio = (land && ks >= k0 && ks < k1) ? ratio_s[ks - k0] : F(0.0);
+
+  const long long pitch = L.pitch, plane = L.plane;
+  long long o = L.at(i, j, k0);
+  F d0[NTR], Ic[NTR];
+#pragma unroll
+  for (int t = 0; t < NTR; ++t) d0[t] = diss_col(*A[t], col, o, pitch, &Ic[t]);
+  for (int k = k0; k < k1; ++k, o += plane) {
+    const bool below = k < Z - 1;
+    const bool mW = inner && below && (__ldg(a0.m + o) & VG_MASK_W);
+    const F gz = gidz[k - k0], idz = idz_s[k - k0];
+    F P = a0.P[o];
+#pragma unroll
+    for (int t = 0; t < NTR; ++t) {
+      const DiffArgs<F> &a = *A[t];
+      F d1 = F(0.0), In = F(0.0);
+      F dw;
+      if (below) {
+        d1 = diss_col(a, col, o + plane, pitch, &In);
+        const F h = pm(F(0.5), d0[t] + d1);
+        dw = (land && k == ks) ? pfma(F(0.5), pm(d0[t], ratio), h) : ((land && k > ks) ? h : F(0.0));
+      } else {
+        dw = land ? d0[t] : F(0.0);
+      }
+      P = P + dw;
+      // vertical-mixing term (diffusion.py:254-279); zero where maskW is:
+      // P += (-g/rho_0 fxa) (flux_top + K_33 dtr/dzw), fxa = (I_k - I_k+1) / dzw
+      if (mW) {
+        const F g = pm(Ic[t] - In, gz);
+        F term = ld(a.ft, o);
+        if (a.iso) term = pfma(pm(ld(a.K33, o), to_F<F>(a.trp[o + plane] - a.trp[o])), idz, term);
+        P = pfma(g, term, P);
+      }
+      d0[t] = d1;
+      Ic[t] = In;
+    }
+    a0.P[o] = P;
+  }
 }
 
 // Validates one tracer's arguments and fills its DiffArgs.

@@ -40,11 +40,45 @@ int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) 
   return check_launch("implicit_kernel");
 }
 
+// Levels per CTA of energy_kernel. The kernel is bound by the FP64 pipe,
+// which an SM's resident CTAs share, so the cost of a chunking is the CTAs an
+// SM receives times the levels per CTA, counting a chunk's extra dissipation
+// evaluation at its top as half a level.
+inline int energy_kchunk(int ctas_per_chunk, int Z) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    sms = std::max(1, sms);
+  }
+  int best = Z;
+  double best_cost = 1e300;
+  for (int nch = 1; nch <= std::min(Z, 64); ++nch) {
+    const int kc = (Z + nch - 1) / nch, n = (Z + kc - 1) / kc;
+    const long long ctas = (long long)ctas_per_chunk * n;
+    const double cost = (double)((ctas + sms - 1) / sms) * (kc + 0.5);
+    if (cost < best_cost) best_cost = cost, best = kc;
+  }
+  return best;
+}
+
+// One tracer, or temp and salt together when they add into the same P_diss.
 template <typename F>
-int launch_energy(const DiffArgs<F> &a, cudaStream_t s) {
-  dim3 block(128);
-  dim3 g((a.L.X - 2 + 127) / 128, a.L.Y - 2, a.L.Z);
-  energy_kernel<F><<<g, block, 0, s>>>(a);
+int launch_energy(const DiffArgs<F> &a, const DiffArgs<F> *b, cudaStream_t s) {
+  if (a.L.Z > kEnergyMaxZ) return fail(VG_ERR_SHAPE, "energy_kernel: Z=%d above %d", a.L.Z, kEnergyMaxZ);
+  dim3 block(kEnergyTX, kEnergyTY);
+  const int gx = (a.L.X - 2 + kEnergyTX - 1) / kEnergyTX, gy = (a.L.Y - 2 + kEnergyTY - 1) / kEnergyTY;
+  if (b && b->P == a.P) {
+    const int kc = energy_kchunk(gx * gy, a.L.Z);
+    energy_kernel<F, 2><<<dim3(gx, gy, (a.L.Z + kc - 1) / kc), block, 0, s>>>(a, *b, kc);
+    return check_launch("energy_kernel");
+  }
+  const int kc = energy_kchunk(gx * gy, a.L.Z);
+  energy_kernel<F, 1><<<dim3(gx, gy, (a.L.Z + kc - 1) / kc), block, 0, s>>>(a, a, kc);
+  int st = check_launch("energy_kernel");
+  if (st || !b) return st;
+  energy_kernel<F, 1><<<dim3(gx, gy, (a.L.Z + kc - 1) / kc), block, 0, s>>>(*b, *b, kc);
   return check_launch("energy_kernel");
 }
 
@@ -64,7 +98,7 @@ int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div<F, 1>(a, a, s))) return st;
   if (a.iso && (st = launch_implicit<F, 1>(a, a, s))) return st;
-  if (a.save_fluxes && (st = launch_energy(a, s))) return st;
+  if (a.save_fluxes && (st = launch_energy<F>(a, nullptr, s))) return st;
   return VG_OK;
 }
 
@@ -87,10 +121,7 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div<F, 2>(aT, aS, s))) return st;
   if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
-  if (aT.save_fluxes) {
-    if ((st = launch_energy(aT, s))) return st;
-    if ((st = launch_energy(aS, s))) return st;
-  }
+  if (aT.save_fluxes && (st = launch_energy<F>(aT, &aS, s))) return st;
   return VG_OK;
 }
 

@@ -45,65 +45,139 @@ struct GenSrc {
 };
 
 // One thread per column. Shared memory holds the eliminated diagonal and
-// right-hand side of the column, laid out [k][field][thread]; the solution
+// right-hand side of the column, laid out [field][k][thread]; the solution
 // reuses the diagonal slots.
-__global__ void pivoting_solve_kernel(TriArgs p) {
+constexpr int kTriMaxThreads = 128;
+
+__global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs p) {
   extern __shared__ double sm[];
+  __shared__ int ks_s[kTriMaxThreads], perm_s[kTriMaxThreads];
   const int t = threadIdx.x;
   const int nb = blockDim.x;
-  const int s = blockIdx.x * nb + t;
-  if (s >= p.nsys) return;
-  const long long base = p.sx * (long long)(s % p.nsx) + p.sy * (long long)(s / p.nsx);
   const int nz = p.nz;
+  auto base_of = [&](int s) { return p.sx * (long long)(s % p.nsx) + p.sy * (long long)(s / p.nsx); };
 
-  // water/edge form check (create_water_masks, utilities.py:38-48)
-  int ks = -1;
-  bool bad = false;
-  for (int k = 0; k < nz; ++k) {
-    const long long o = base + p.sz * k;
-    const bool w = p.water[o] != 0, e = p.edge[o] != 0;
-    if (ks < 0 && w) ks = k;
-    if (w != (ks >= 0) || e != (ks == k)) bad = true;
+  // water/edge form check of the thread's own column (create_water_masks,
+  // utilities.py:38-48) and the zero output of its rows k < ks
+  {
+    const int s = blockIdx.x * nb + t;
+    int ks = -1;
+    if (s < p.nsys) {
+      const long long base = base_of(s);
+      bool bad = false;
+#pragma unroll 4
+      for (int k = 0; k < nz; ++k) {
+        const long long o = base + p.sz * k;
+        const bool w = p.water[o] != 0, e = p.edge[o] != 0;
+        if (ks < 0 && w) ks = k;
+        if (w != (ks >= 0) || e != (ks == k)) bad = true;
+      }
+      if (bad && p.bad) atomicAdd(p.bad, 1);
+      for (int k = 0; k < (ks < 0 ? nz : ks); ++k) p.out[base + p.sz * k] = 0.0;
+    }
+    ks_s[t] = ks;
   }
-  if (bad && p.bad) atomicAdd(p.bad, 1);
-
-  for (int k = 0; k < (ks < 0 ? nz : ks); ++k) p.out[base + p.sz * k] = 0.0;
-  if (ks < 0) return;
+  __syncthreads();
+  // The CTA's columns ranked by their number of water rows (most first, ties
+  // by position), so that the lanes of a warp solve systems of similar size.
+  {
+    const int n = ks_s[t] < 0 ? 0 : nz - ks_s[t];
+    int rank = 0;
+    for (int u = 0; u < nb; ++u) {
+      const int m = ks_s[u] < 0 ? 0 : nz - ks_s[u];
+      rank += (m > n) || (m == n && u < t);
+    }
+    perm_s[rank] = t;
+  }
+  __syncthreads();
+  const int s = blockIdx.x * nb + perm_s[t];
+  const int ks = ks_s[perm_s[t]];
+  if (s >= p.nsys || ks < 0) return;
+  const long long base = base_of(s);
   GenSrc src{p, base, ks};
   double *Ds = sm + t;
   double *Bs = sm + (size_t)nz * nb + t;
 
+  // Loads run PF levels ahead of the elimination's serial chain (software
+  // pipelining); the arithmetic is dgtsv's, operation for operation.
+  constexpr int PF = 4;
+  double qa[PF], qb[PF], qc[PF], qd[PF];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = ks + 1 + u;
+    qa[u] = k < nz ? src.a(k) : 0.0;
+    qb[u] = k < nz ? p.b[src.at(k)] : 0.0;
+    qc[u] = k < nz - 1 ? src.c(k) : 0.0;
+    qd[u] = k < nz ? p.d[src.at(k)] : 0.0;
+  }
   // elimination without interchange while dgtsv would take that branch
   bool interchange = false;
   double Dp = src.b(ks), Bp = src.d(ks), cp = ks < nz - 1 ? src.c(ks) : 0.0;
   Ds[(size_t)ks * nb] = Dp;
   Bs[(size_t)ks * nb] = Bp;
-  for (int k = ks + 1; k < nz && !interchange; ++k) {
-    const double dl = src.a(k);
-    if (fabs(Dp) < fabs(dl)) {
-      interchange = true;
-      break;
+  for (int k0 = ks + 1; k0 < nz && !interchange; k0 += PF) {
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 + u;
+      if (k < nz && !interchange) {
+        const double dl = qa[u], bk = qb[u], ck = qc[u], dk = qd[u];
+        const int kn = k + PF;
+        if (kn < nz) {
+          qa[u] = src.a(kn);
+          qb[u] = p.b[src.at(kn)];
+          qc[u] = kn < nz - 1 ? src.c(kn) : 0.0;
+          qd[u] = p.d[src.at(kn)];
+        }
+        if (fabs(Dp) < fabs(dl)) {
+          interchange = true;
+        } else {
+          const double fact = rdiv(dl, Dp);
+          Dp = rsub(bk, rmul(fact, cp));
+          Bp = rsub(dk, rmul(fact, Bp));
+          cp = ck;
+          Ds[(size_t)k * nb] = Dp;
+          Bs[(size_t)k * nb] = Bp;
+        }
+      }
     }
-    const double fact = rdiv(dl, Dp);
-    Dp = rsub(src.b(k), rmul(fact, cp));
-    Bp = rsub(src.d(k), rmul(fact, Bp));
-    cp = k < nz - 1 ? src.c(k) : 0.0;
-    Ds[(size_t)k * nb] = Dp;
-    Bs[(size_t)k * nb] = Bp;
   }
   if (interchange) {
     dgtsv_slow_solve(src, ks, nz, Ds, nb);
   } else {
-    double x = 0.0;
-    for (int k = nz - 1; k >= ks; --k) {
-      const double Dk = Ds[(size_t)k * nb], Bk = Bs[(size_t)k * nb];
-      x = (k == nz - 1) ? rdiv(Bk, Dk) : rdiv(rsub(Bk, rmul(src.c(k), x)), Dk);
-      Ds[(size_t)k * nb] = x;
+    double qcb[PF];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = nz - 2 - u;
+      qcb[u] = k >= ks ? src.c(k) : 0.0;
+    }
+    double x = rdiv(Bs[(size_t)(nz - 1) * nb], Ds[(size_t)(nz - 1) * nb]);
+    Ds[(size_t)(nz - 1) * nb] = x;
+    for (int k0 = nz - 2; k0 >= ks; k0 -= PF) {
+#pragma unroll
+      for (int u = 0; u < PF; ++u) {
+        const int k = k0 - u;
+        if (k >= ks) {
+          const double ck = qcb[u];
+          if (k - PF >= ks) qcb[u] = src.c(k - PF);
+          x = rdiv(rsub(Bs[(size_t)k * nb], rmul(ck, x)), Ds[(size_t)k * nb]);
+          Ds[(size_t)k * nb] = x;
+        }
+      }
     }
   }
   for (int k = ks; k < nz; ++k) p.out[base + p.sz * k] = Ds[(size_t)k * nb];
 }
 
+// Reciprocal of a pivot: the FP32 division in single precision; in double,
+// recip_any (an FP32 seed refined by two Newton steps, within an ulp of the
+// quotient) in place of the IEEE division, which takes tens of FP64
+// instructions.
+__device__ __forceinline__ float pivot_recip(float x) { return 1.0f / x; }
+__device__ __forceinline__ double pivot_recip(double x) { return recip_any(x); }
+
+// One thread per system; c' in shared memory [k][thread], d' in the output
+// (overwritten by the solution in the back substitution). Both sweeps load PF
+// levels ahead of their serial chain.
 template <typename F>
 __global__ void xla_thomas_kernel(const F *__restrict__ a, const F *__restrict__ b, const F *__restrict__ c,
                                   const F *__restrict__ d, F *__restrict__ out, int nsys, int depth) {
@@ -112,25 +186,62 @@ __global__ void xla_thomas_kernel(const F *__restrict__ a, const F *__restrict__
   const int t = threadIdx.x, nb = blockDim.x;
   const int s = blockIdx.x * nb + t;
   if (s >= nsys) return;
-  long long o = s;
-  F cm = c[o] / b[o];
-  F dm = d[o] / b[o];
+  const long long n = nsys;
+  constexpr int PF = 4;
+  F qa[PF], qb[PF], qc[PF], qd[PF];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const long long o = s + n * min(1 + u, depth - 1);
+    qa[u] = a[o];
+    qb[u] = b[o];
+    qc[u] = c[o];
+    qd[u] = d[o];
+  }
+  const F r0 = pivot_recip(b[s]);
+  F cm = c[s] * r0;
+  F dm = d[s] * r0;
   cp[t] = cm;
-  out[o] = dm;
-  for (int k = 1; k < depth; ++k) {
-    o += nsys;
-    const F ak = a[o];
-    const F den = F(1) / (b[o] - ak * cm);
-    cm = c[o] * den;
-    dm = (d[o] - ak * dm) * den;
-    cp[(size_t)k * nb + t] = cm;
-    out[o] = dm;
+  out[s] = dm;
+  for (int k0 = 1; k0 < depth; k0 += PF) {
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 + u;
+      if (k < depth) {
+        const F ak = qa[u], bk = qb[u], ck = qc[u], dk = qd[u];
+        const int kn = k + PF;
+        if (kn < depth) {
+          const long long on = s + n * kn;
+          qa[u] = a[on];
+          qb[u] = b[on];
+          qc[u] = c[on];
+          qd[u] = d[on];
+        }
+        const F den = pivot_recip(bk - ak * cm);
+        cm = ck * den;
+        dm = (dk - ak * dm) * den;
+        cp[(size_t)k * nb + t] = cm;
+        out[s + n * k] = dm;
+      }
+    }
+  }
+  F qo[PF];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = depth - 2 - u;
+    qo[u] = k >= 0 ? out[s + n * k] : F(0);
   }
   F x = dm;
-  for (int k = depth - 2; k >= 0; --k) {
-    o -= nsys;
-    x = out[o] - cp[(size_t)k * nb + t] * x;
-    out[o] = x;
+  for (int k0 = depth - 2; k0 >= 0; k0 -= PF) {
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 - u;
+      if (k >= 0) {
+        const F ok = qo[u];
+        if (k - PF >= 0) qo[u] = out[s + n * (k - PF)];
+        x = ok - cp[(size_t)k * nb + t] * x;
+        out[s + n * k] = x;
+      }
+    }
   }
 }
 
@@ -157,8 +268,8 @@ void xla_tdma(void *stream, void **buffers, const char *opaque, size_t opaque_le
   const F *c = static_cast<const F *>(buffers[2]);
   const F *d = static_cast<const F *>(buffers[3]);
   F *out = static_cast<F *>(buffers[4]);
-  int nb = 128;
-  while (nb > 32 && (size_t)nb * desc.system_depth * sizeof(F) > 96 * 1024) nb /= 2;
+  // one warp per CTA: the CTAs of a launch are spread evenly over the SMs
+  const int nb = 32;
   const size_t smem = (size_t)nb * desc.system_depth * sizeof(F);
   if (smem > 200 * 1024) {
     fail(VG_ERR_SHAPE, "%s: system_depth %d too deep", name, desc.system_depth);
@@ -195,7 +306,7 @@ extern "C" int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, lo
   if (nsys == 0) return VG_OK;
   if (nsys > 0x7fffffffLL) return fail(VG_ERR_SHAPE, "too many columns");
   TriArgs p{nsx, (int)nsys, nz, s_x, s_y, s_z, a, b, c, d, b_edge, d_edge, water, edge, out, bad_columns};
-  int nb = 128;
+  int nb = kTriMaxThreads;
   while (nb > 32 && (size_t)nb * nz * 2 * sizeof(double) > 100 * 1024) nb /= 2;
   const size_t smem = (size_t)nb * nz * 2 * sizeof(double);
   if (smem > 48 * 1024) {

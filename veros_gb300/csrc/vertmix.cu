@@ -28,19 +28,64 @@ struct VmixArgs {
   double *dvmix[2];
 };
 
-__global__ void __launch_bounds__(64) vertmix_kernel(VmixArgs a) {
+__device__ __forceinline__ double vm_mul(double x, double y) { return __dmul_rn(x, y); }
+__device__ __forceinline__ double vm_fma(double x, double y, double z) { return __fma_rn(x, y, z); }
+
+// One thread per column. Shared memory holds the per-level tables dt/dzw
+// (the reference's own quotient, so delta keeps its rounding) and 1/dzt, and
+// the eliminated c' of the CTA's columns, laid out [k][thread]; the
+// eliminated right-hand sides d' go to dtemp_vmix / dsalt_vmix, which the
+// back substitution then overwrites with the tendencies (the column stays in
+// L2 between the two sweeps). Divisions by dzt are multiplications by the
+// table's reciprocals and each pivot costs one reciprocal (an FP32 seed
+// refined by Newton steps). Both sweeps load PF levels ahead of their serial
+// chain, so the chain waits for FP64 latency rather than for memory.
+constexpr int kVmixThreads = 128;
+
+__global__ void __launch_bounds__(kVmixThreads) vertmix_kernel(VmixArgs a) {
   extern __shared__ double smem[];
   const Layout &L = a.L;
   const int Z = L.Z;
   const int t = threadIdx.x, nb = blockDim.x;
-  double *cps = smem;
-  double *dps = smem + (size_t)Z * nb;  // [r][k][thread]
-  const int col = blockIdx.x * nb + t;
-  if (col >= L.X * L.Y) return;
+  double *dtdzw = smem, *inv_dzt = smem + Z;
+  double *cps = smem + 2 * Z;
+  for (int k = t; k < Z; k += nb) {
+    dtdzw[k] = a.dt / a.g.dzw[k];
+    inv_dzt[k] = 1.0 / a.g.dzt[k];
+  }
+  // The CTA's columns ranked by their number of water levels (most first,
+  // ties by position), so that the lanes of a warp walk columns of similar
+  // length: each thread counts the columns ahead of its own and the thread of
+  // that rank takes it.
+  __shared__ int nlev_s[kVmixThreads];
+  __shared__ int perm_s[kVmixThreads];
+  const int ncols = L.X * L.Y;
+  auto ks_of = [&](int c) {
+    const int ci = c % L.X, cj = c / L.X;
+    const bool interior = ci >= 2 && ci < L.X - 2 && cj >= 2 && cj < L.Y - 2;
+    return interior ? a.kbot[L.at2(ci, cj)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
+  };
+  {
+    const int c = blockIdx.x * nb + t;
+    const int k = c < ncols ? ks_of(c) : -1;
+    nlev_s[t] = (k >= 0 && k < Z) ? Z - k : 0;
+  }
+  __syncthreads();
+  {
+    const int n = nlev_s[t];
+    int rank = 0;
+    for (int u = 0; u < nb; ++u) {
+      const int m = nlev_s[u];
+      rank += (m > n) || (m == n && u < t);
+    }
+    perm_s[rank] = t;
+  }
+  __syncthreads();
+  const int col = blockIdx.x * nb + perm_s[t];
+  if (col >= ncols) return;
   const int i = col % L.X, j = col / L.X;
   const long long base = L.at2(i, j);
-  const bool interior = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
-  const int ks = interior ? a.kbot[base] - 1 : -1;  // create_water_masks (utilities.py:38-48)
+  const int ks = ks_of(col);
   // dtemp_vmix starts as the old level; outside the water cells the update is (old - old)/dt = 0
   for (int k = 0; k < (ks >= 0 && ks < Z ? ks : Z); ++k) {
     const long long o = base + (long long)k * L.plane;
@@ -49,37 +94,92 @@ __global__ void __launch_bounds__(64) vertmix_kernel(VmixArgs a) {
   }
   if (ks < 0 || ks >= Z) return;
 
+  constexpr int PF = 4;
+  double qK[PF], qT[PF][2];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = ks + u;
+    const long long o = base + (long long)min(k, Z - 1) * L.plane;
+    qK[u] = k < Z - 1 ? a.kappaH[o] : 0.0;
+    qT[u][0] = k < Z ? a.tr[0][o] : 0.0;
+    qT[u][1] = k < Z ? a.tr[1][o] : 0.0;
+  }
   double delta_prev = 0.0, cp = 0.0, dp[2] = {0.0, 0.0};
-  for (int k = ks; k < Z; ++k) {
-    const long long o = base + (long long)k * L.plane;
-    const double dzt = a.g.dzt[k];
-    const double delta = k < Z - 1 ? rmul(rdiv(a.dt, a.g.dzw[k]), a.kappaH[o]) : 0.0;
-    const double ak = k == ks ? 0.0 : rdiv(-delta_prev, dzt);  // a_tri, zero at the edge (operators.py:72)
-    const double bk = k == ks ? radd(1.0, rdiv(delta, dzt)) : radd(1.0, rdiv(radd(delta, delta_prev), dzt));
-    const double ck = k < Z - 1 ? rdiv(-delta, dzt) : 0.0;
-    const double den = 1.0 / (bk - ak * cp);
-    cp = ck * den;
-    cps[(size_t)k * nb + t] = cp;
+  for (int k0 = ks; k0 < Z; k0 += PF) {
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 + u;
+      if (k < Z) {
+        const long long o = base + (long long)k * L.plane;
+        const double idzt = inv_dzt[k];
+        const double delta = k < Z - 1 ? vm_mul(dtdzw[k], qK[u]) : 0.0;  // thermodynamics.py:267-270
+        double d[2] = {qT[u][0], qT[u][1]};
+        const int kn = k + PF;
+        if (kn < Z) {
+          const long long on = base + (long long)kn * L.plane;
+          qK[u] = kn < Z - 1 ? a.kappaH[on] : 0.0;
+          qT[u][0] = a.tr[0][on];
+          qT[u][1] = a.tr[1][on];
+        }
+        const double ak = k == ks ? 0.0 : vm_mul(-delta_prev, idzt);  // a_tri, zero at the edge (operators.py:72)
+        const double bk = vm_fma(k == ks ? delta : delta + delta_prev, idzt, 1.0);  // b_tri, b_tri_edge at ks
+        const double ck = vm_mul(-delta, idzt);                                      // c_tri (0 on the top level)
+        const double den = recip_newton(vm_fma(-ak, cp, bk));  // pivot >= the diagonal's excess over 1
+        cp = vm_mul(ck, den);
+        cps[(size_t)k * nb + t] = cp;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          if (k == Z - 1) d[r] = vm_fma(vm_mul(a.dt, a.forc[r][base]), idzt, d[r]);  // thermodynamics.py:279, :287
+          dp[r] = vm_mul(vm_fma(-ak, dp[r], d[r]), den);
+          a.dvmix[r][o] = dp[r];
+        }
+        delta_prev = delta;
+      }
+    }
+  }
+  // back substitution from the top level down to ks; slot u holds level k - u
+  double qD[PF][2], qO[PF][2];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = Z - 1 - u;
+    const long long o = base + (long long)max(k, ks) * L.plane;
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
-      double d = a.tr[r][o];
-      if (k == Z - 1) d = radd(d, rdiv(rmul(a.dt, a.forc[r][base]), dzt));  // thermodynamics.py:279, :287
-      dp[r] = (d - ak * dp[r]) * den;
-      dps[((size_t)r * Z + k) * nb + t] = dp[r];
+      qD[u][r] = k >= ks ? a.dvmix[r][o] : 0.0;
+      qO[u][r] = k >= ks ? a.tr[r][o] : 0.0;
     }
-    delta_prev = delta;
   }
   double x[2] = {0.0, 0.0};
   const double inv_dt = 1.0 / a.dt;
-  for (int k = Z - 1; k >= ks; --k) {
-    const long long o = base + (long long)k * L.plane;
-    const double c = cps[(size_t)k * nb + t];
+  for (int k0 = Z - 1; k0 >= ks; k0 -= PF) {
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      x[r] = dps[((size_t)r * Z + k) * nb + t] - c * x[r];
-      const double old = a.tr[r][o];
-      a.tr[r][o] = x[r];
-      a.dvmix[r][o] = (x[r] - old) * inv_dt;  // thermodynamics.py:289-290
+    for (int u = 0; u < PF; ++u) {
+      const int k = k0 - u;
+      if (k >= ks) {
+        const long long o = base + (long long)k * L.plane;
+        const double c = cps[(size_t)k * nb + t];
+        double dk[2], old[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          dk[r] = qD[u][r];
+          old[r] = qO[u][r];
+        }
+        const int kn = k - PF;
+        if (kn >= ks) {
+          const long long on = base + (long long)kn * L.plane;
+#pragma unroll
+          for (int r = 0; r < 2; ++r) {
+            qD[u][r] = a.dvmix[r][on];
+            qO[u][r] = a.tr[r][on];
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          x[r] = vm_fma(-c, x[r], dk[r]);
+          a.tr[r][o] = x[r];
+          a.dvmix[r][o] = vm_mul(x[r] - old[r], inv_dt);  // thermodynamics.py:289-290
+        }
+      }
     }
   }
 }
@@ -149,8 +249,12 @@ extern "C" int vg_vertmix_tempsalt_f64(const VgDomain *dom, const VgGrid *grid, 
   a.forc[1] = forc_salt_surface;
   a.dvmix[0] = dtemp_vmix;
   a.dvmix[1] = dsalt_vmix;
-  const int nb = 64;
-  const size_t smem = 3 * (size_t)a.L.Z * nb * sizeof(double);
+  // columns per CTA: 128, fewer where the c' of 128 deep columns would not fit
+  int nb = kVmixThreads;
+  while (nb > 32 && (2 + (size_t)nb) * a.L.Z * sizeof(double) > 100 * 1024) nb /= 2;
+  const size_t smem = (2 + (size_t)nb) * a.L.Z * sizeof(double);
+  if (smem > 227 * 1024)
+    return fail(VG_ERR_SHAPE, "vg_vertmix_tempsalt_f64: Z=%d too deep for the shared-memory factorisation", a.L.Z);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(vertmix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "vertmix_kernel smem %zu: %s", smem, cudaGetErrorString(e));

@@ -121,8 +121,8 @@ class IsoneutralStepper:
     def launches_per_step(self):
         """Kernels of this library one step enqueues: prepare, pre, one flux
         kernel for temp and salt, one shared implicit solve and, with the
-        energy branch, two energy kernels."""
-        return 1 + 1 + 1 + 1 + (2 if self.dev.settings.enable_conserve_energy else 0)
+        energy branch, one energy kernel for both tracers."""
+        return 1 + 1 + 1 + 1 + (1 if self.dev.settings.enable_conserve_energy else 0)
 
 
 class HostPipeline:
