@@ -232,8 +232,25 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_kernel_ab:
+        line["kernel_ab"] = _reference_kernel_ab_line()
     print(json.dumps(line))
     return 0
+
+
+def _reference_kernel_ab_line():
+    try:
+        import torch
+    except ImportError:
+        return {"unavailable": "torch not importable"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(device)
+    try:
+        return reference_kernel_ab(device)
+    except RuntimeError as e:
+        return {"unavailable": str(e).splitlines()[0]}
 
 
 def run_ensemble(device, steps=20):
@@ -393,6 +410,70 @@ def run_quarter_degree(device, steps=100):
     return out
 
 
+# The tridiagonal A/B workload: one system per column of the 1-degree domain
+# (364 x 184 with the halo) and its 60 levels
+TDMA_NSYS, TDMA_DEPTH = (WORKLOAD["nx"] + 4) * (WORKLOAD["ny"] + 4), WORKLOAD["nz"]
+
+
+def tridiag_inputs(device, ncols, nz):
+    """Seeded diagonally dominant systems, (columns, levels) row-major: a, b, c, d."""
+    import torch
+
+    g = torch.Generator(device="cpu").manual_seed(5)
+    shp = (ncols, nz)
+    a = -torch.rand(shp, generator=g, dtype=torch.float64)
+    c = -torch.rand(shp, generator=g, dtype=torch.float64)
+    b = 3.0 + torch.rand(shp, generator=g, dtype=torch.float64)
+    d = torch.randn(shp, generator=g, dtype=torch.float64)
+    return tuple(x.to(device) for x in (a, b, c, d))
+
+
+def time_call(fn, flush, reps=20):
+    """Median of ``reps`` single-call CUDA-event timings (ms) on torch's current
+    stream, each after a write of ``flush`` (larger than L2) and after 3 warm-up calls."""
+    import torch
+
+    for _ in range(3):
+        fn()
+    ms = []
+    for _ in range(reps):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    return float(np.median(ms))
+
+
+def reference_kernel_ab(device, reps=20):
+    """The reference's own CUDA TDMA kernel (TridiagKernel<double>, built from
+    its source for sm_103a, launched with its launcher's configuration) on the
+    tridiagonal A/B workload, timed like the aux kernels."""
+    import torch
+
+    from oracle import ref_tdma
+
+    if not ref_tdma.available():
+        return {"unavailable": "reference TDMA cubin or launcher not built (oracle/_ref)"}
+    kern = ref_tdma.ReferenceTdma()
+    av, bv, cv, dv = tridiag_inputs(device, TDMA_NSYS, TDMA_DEPTH)
+    bufs = [x.t().contiguous() for x in (av, bv, cv, dv)]
+    bufs += [torch.empty_like(bufs[3]), torch.empty_like(bufs[3])]  # out, workspace (c')
+    ptrs = [t.data_ptr() for t in bufs]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    ms = time_call(lambda: kern(stream, ptrs, TDMA_NSYS, TDMA_DEPTH, True), flush, reps)
+    nbytes = 40 * TDMA_NSYS * TDMA_DEPTH
+    return {"kernel": "TridiagKernel<double> (veros/core/special/cuda_tdma_kernels.cu:19-63)",
+            "launch": "128 threads, min(1024, ceil(nsys/128)) blocks (cuda_tdma_kernels.cu:96-98)",
+            "systems": TDMA_NSYS, "depth": TDMA_DEPTH, "ms": ms,
+            "achieved_gbs": nbytes / (ms / 1e3) / 1e9,
+            "bytes": "a, b, c, d 32, solution 8 per cell (its c' workspace round trip not counted)",
+            "timing": "median of per-call CUDA events, L2 evicted before each call"}
+
+
 def run_aux(device, reps=20):
     """The path's neighbouring kernels, each timed alone on the 1-degree
     workload (360 x 180 x 60): vertical mixing of temp and salt
@@ -425,21 +506,11 @@ def run_aux(device, reps=20):
     cells_pad = dev.plane * dev.Z
     kb = host.arrays["kbot"].reshape(-1)  # one column per (i, j), halo included
     ncols, nz = kb.size, host.nz
+    assert (ncols, nz) == (TDMA_NSYS, TDMA_DEPTH)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
 
     def timed(fn):
-        for _ in range(3):
-            fn()
-        ms = []
-        for _ in range(reps):
-            flush.fill_(1)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            fn()
-            b.record()
-            b.synchronize()
-            ms.append(a.elapsed_time(b))
-        return float(np.median(ms))
+        return time_call(fn, flush, reps)
 
     out = {"workload": f"{host.nx}x{host.ny}x{host.nz} at 1 degree, eq 3", "reps": reps,
            "timing": "median of per-call CUDA events, L2 evicted before each call", "peak_gbs": peak,
@@ -457,12 +528,8 @@ def run_aux(device, reps=20):
            timed(lambda: isoneutral._run_streamfunction(dev)), 88 * cells_pad, cells_pad,
            "K_gm 8, Ai_ez 32, Ai_nz 32, B1_gm and B2_gm 16")
 
-    g = torch.Generator(device="cpu").manual_seed(5)
     shp = (ncols, nz)
-    av = -torch.rand(shp, generator=g, dtype=torch.float64).to(device)
-    cv = -torch.rand(shp, generator=g, dtype=torch.float64).to(device)
-    bv = (3.0 + torch.rand(shp, generator=g, dtype=torch.float64)).to(device)
-    dv = torch.randn(shp, generator=g, dtype=torch.float64).to(device)
+    av, bv, cv, dv = tridiag_inputs(device, ncols, nz)
     ks = torch.from_numpy(np.where(kb > 0, kb - 1, nz)).to(device)  # land columns: no water
     kk = torch.arange(nz, device=device)
     water = (kk[None, :] >= ks[:, None].long()).to(torch.uint8).contiguous()
@@ -491,7 +558,8 @@ def run_aux(device, reps=20):
                                 len(desc))
 
     report("tdma_cuda_double", "xla_thomas_kernel", timed(xla), 40 * ncols * nz, ncols * nz,
-           "a, b, c, d 32, solution 8; system-fastest layout")
+           "a, b, c, d 32, solution 8; system-fastest layout; the same systems as the reference arm's "
+           "kernel_ab (the reference's own TDMA kernel)")
     if _capi.last_error():
         raise RuntimeError(_capi.last_error())
     del av, bv, cv, dv, at, bt, ct, dt_, outt, res, water, edge
@@ -678,6 +746,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 8-step rollout adjoint measurement")
     ap.add_argument("--quarter-degree", action="store_true",
                     help="add the 0.25-degree split-versus-FP64 measurement (100 steps, ~25 GB of device memory)")
+    ap.add_argument("--no-kernel-ab", action="store_true",
+                    help="reference arm: skip the reference's CUDA TDMA kernel timing")
     ap.add_argument("--aux", action="store_true",
                     help="add per-kernel timings of vertical mixing, streamfunction, the generic and XLA tridiagonal "
                          "solves and the energy branch (1 degree)")

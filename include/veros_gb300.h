@@ -343,7 +343,8 @@ int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid *grid, cons
  * k == ks. b_edge/d_edge may be NULL. Outside water the output is 0.
  * Columns whose masks do not have that form are counted into *bad_columns
  * (device int, may be NULL) and solved over their water cells only.
- * Elimination uses partial pivoting, as LAPACK dgtsv does. */
+ * Elimination uses partial pivoting, as LAPACK dgtsv does. out may not
+ * overlap an input (VG_ERR_ARG). */
 int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, long long s_y, long long s_z,
                           const double *a, const double *b, const double *c, const double *d,
                           const uint8_t *water, const uint8_t *edge,

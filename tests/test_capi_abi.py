@@ -107,6 +107,14 @@ def test_tridiag_shape_checks(lib):
     assert st == _capi.VG_ERR_SHAPE
     st = lib.vg_solve_implicit_f64(4, 4, 10, 1, 4, 16, *([None] * 11))
     assert st == _capi.VG_ERR_ARG
+    # the output may not overlap an input (checked on the pointers, before any
+    # launch; only overlapping cases here, which never reach the device);
+    # 16 columns x 10 levels of doubles span 1280 bytes
+    base = 1 << 40
+    arrs = [base + n * 4096 for n in range(6)] + [None, None]  # a b c d water edge b_edge d_edge
+    for out in (arrs[3], arrs[1] + 1272, arrs[4] - 1279, arrs[0] - 1272):
+        st = lib.vg_solve_implicit_f64(4, 4, 10, 10, 40, 1, *arrs, out, None, None)
+        assert st == _capi.VG_ERR_ARG and "overlaps" in _capi.last_error()
     # the XLA-style entry keeps the error instead of exiting
     desc = b"\x00" * 4
     lib.vg_tdma_cuda_double(None, (ctypes.c_void_p * 6)(), desc, len(desc))

@@ -187,6 +187,47 @@ def test_xla_tdma_entry_point(dtype):
         assert _rel(out[:, s], ref) <= tol, s
 
 
+@pytest.mark.parametrize("dtype", ["double", "float"])
+def test_xla_tdma_matches_reference_cuda_kernel(dtype):
+    """vg_tdma_cuda_* against the reference's own CUDA kernel (TridiagKernel,
+    veros/core/special/cuda_tdma_kernels.cu:19-63, built from its source for
+    sm_103a) on the same buffers: the same Thomas recurrence, with a
+    reciprocal within an ulp of the reference's quotient in double."""
+    import ctypes
+
+    from oracle import ref_tdma
+    from veros_gb300 import _capi
+
+    if not ref_tdma.available():
+        pytest.skip("reference TDMA kernel not built (oracle/_ref)")
+    ref = ref_tdma.ReferenceTdma()
+    rng = np.random.default_rng(7)
+    nsys, depth = 5000, 60
+    tdt, ndt, tol = (torch.float64, np.float64, 1e-13) if dtype == "double" else (torch.float32, np.float32, 1e-5)
+    a = -rng.random((depth, nsys))
+    c = -rng.random((depth, nsys))
+    b = 2.2 + rng.random((depth, nsys))
+    d = rng.standard_normal((depth, nsys))
+    ins = [torch.from_numpy(x.astype(ndt)).cuda() for x in (a, b, c, d)]
+    outs = {}
+    for who in ("ours", "reference"):
+        out, ws = torch.empty((depth, nsys), dtype=tdt, device="cuda"), torch.empty((depth, nsys), dtype=tdt,
+                                                                                    device="cuda")
+        ptrs = [t.data_ptr() for t in ins] + [out.data_ptr(), ws.data_ptr()]
+        stream = torch.cuda.current_stream().cuda_stream
+        if who == "ours":
+            desc = np.array([nsys, depth], dtype=np.int32).tobytes()
+            getattr(_capi.load(), f"vg_tdma_cuda_{dtype}")(ctypes.c_void_p(stream), (ctypes.c_void_p * 6)(*ptrs),
+                                                          desc, len(desc))
+        else:
+            ref(stream, ptrs, nsys, depth, dtype == "double")
+        torch.cuda.synchronize()
+        outs[who] = out.cpu().numpy().astype(np.float64)
+    assert _capi.last_error() == ""
+    scale = np.abs(outs["reference"]).max(axis=0)
+    assert np.all(np.abs(outs["ours"] - outs["reference"]).max(axis=0) <= tol * scale)
+
+
 def _oracle_steps(host, n):
     from oracle import isoneutral_oracle as orc
 

@@ -44,9 +44,11 @@ struct GenSrc {
   __device__ double d(int k) const { return (k == ks && p.d_edge) ? p.d_edge[at(k)] : p.d[at(k)]; }
 };
 
-// One thread per column. Shared memory holds the eliminated diagonal and
-// right-hand side of the column, laid out [field][k][thread]; the solution
-// reuses the diagonal slots.
+// One thread per column. Shared memory holds the eliminated diagonal of the
+// CTA's columns, laid out [k][thread]; the eliminated right-hand side goes
+// to the output, which the back substitution overwrites with the solution
+// (the column stays in L2 between the sweeps). With an interchange the
+// column is re-solved from the inputs into the diagonal slots.
 constexpr int kTriMaxThreads = 128;
 
 __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs p) {
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   const long long base = base_of(s);
   GenSrc src{p, base, ks};
   double *Ds = sm + t;
-  double *Bs = sm + (size_t)nz * nb + t;
+  double *out = p.out + base;  // the eliminated right-hand side, then the solution
 
   // Loads run PF levels ahead of the elimination's serial chain (software
   // pipelining); the arithmetic is dgtsv's, operation for operation.
@@ -114,7 +116,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   bool interchange = false;
   double Dp = src.b(ks), Bp = src.d(ks), cp = ks < nz - 1 ? src.c(ks) : 0.0;
   Ds[(size_t)ks * nb] = Dp;
-  Bs[(size_t)ks * nb] = Bp;
+  out[p.sz * ks] = Bp;
   for (int k0 = ks + 1; k0 < nz && !interchange; k0 += PF) {
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
@@ -136,36 +138,41 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
           Bp = rsub(dk, rmul(fact, Bp));
           cp = ck;
           Ds[(size_t)k * nb] = Dp;
-          Bs[(size_t)k * nb] = Bp;
+          out[p.sz * k] = Bp;
         }
       }
     }
   }
   if (interchange) {
+    // the row sources are the inputs, which the output does not overlap
     dgtsv_slow_solve(src, ks, nz, Ds, nb);
-  } else {
-    double qcb[PF];
+    for (int k = ks; k < nz; ++k) out[p.sz * k] = Ds[(size_t)k * nb];
+    return;
+  }
+  double qcb[PF], qbs[PF];
+#pragma unroll
+  for (int u = 0; u < PF; ++u) {
+    const int k = nz - 2 - u;
+    qcb[u] = k >= ks ? src.c(k) : 0.0;
+    qbs[u] = k >= ks ? out[p.sz * k] : 0.0;
+  }
+  double x = rdiv(out[p.sz * (nz - 1)], Ds[(size_t)(nz - 1) * nb]);
+  out[p.sz * (nz - 1)] = x;
+  for (int k0 = nz - 2; k0 >= ks; k0 -= PF) {
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
-      const int k = nz - 2 - u;
-      qcb[u] = k >= ks ? src.c(k) : 0.0;
-    }
-    double x = rdiv(Bs[(size_t)(nz - 1) * nb], Ds[(size_t)(nz - 1) * nb]);
-    Ds[(size_t)(nz - 1) * nb] = x;
-    for (int k0 = nz - 2; k0 >= ks; k0 -= PF) {
-#pragma unroll
-      for (int u = 0; u < PF; ++u) {
-        const int k = k0 - u;
-        if (k >= ks) {
-          const double ck = qcb[u];
-          if (k - PF >= ks) qcb[u] = src.c(k - PF);
-          x = rdiv(rsub(Bs[(size_t)k * nb], rmul(ck, x)), Ds[(size_t)k * nb]);
-          Ds[(size_t)k * nb] = x;
+      const int k = k0 - u;
+      if (k >= ks) {
+        const double ck = qcb[u], bk = qbs[u];
+        if (k - PF >= ks) {
+          qcb[u] = src.c(k - PF);
+          qbs[u] = out[p.sz * (k - PF)];
         }
+        x = rdiv(rsub(bk, rmul(ck, x)), Ds[(size_t)k * nb]);
+        out[p.sz * k] = x;
       }
     }
   }
-  for (int k = ks; k < nz; ++k) p.out[base + p.sz * k] = Ds[(size_t)k * nb];
 }
 
 // Reciprocal of a pivot: the FP32 division in single precision; in double,
@@ -305,10 +312,26 @@ extern "C" int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, lo
   const long long nsys = (long long)nsx * nsy;
   if (nsys == 0) return VG_OK;
   if (nsys > 0x7fffffffLL) return fail(VG_ERR_SHAPE, "too many columns");
+  {
+    // the output holds intermediate values while the inputs are still read:
+    // it may not overlap them (element offsets span [lo, hi] in every array)
+    long long lo = 0, hi = 0;
+    for (const long long span : {s_x * (nsx - 1), s_y * (nsy - 1), s_z * (nz - 1)}) (span < 0 ? lo : hi) += span;
+    const char *o0 = reinterpret_cast<const char *>(out + lo), *o1 = reinterpret_cast<const char *>(out + hi + 1);
+    auto overlaps = [&](const void *q, size_t elem) {
+      if (!q) return false;
+      const char *q0 = static_cast<const char *>(q) + lo * (long long)elem;
+      const char *q1 = static_cast<const char *>(q) + (hi + 1) * (long long)elem;
+      return q0 < o1 && o0 < q1;
+    };
+    if (overlaps(a, 8) || overlaps(b, 8) || overlaps(c, 8) || overlaps(d, 8) || overlaps(b_edge, 8) ||
+        overlaps(d_edge, 8) || overlaps(water, 1) || overlaps(edge, 1))
+      return fail(VG_ERR_ARG, "vg_solve_implicit_f64: out overlaps an input");
+  }
   TriArgs p{nsx, (int)nsys, nz, s_x, s_y, s_z, a, b, c, d, b_edge, d_edge, water, edge, out, bad_columns};
   int nb = kTriMaxThreads;
-  while (nb > 32 && (size_t)nb * nz * 2 * sizeof(double) > 100 * 1024) nb /= 2;
-  const size_t smem = (size_t)nb * nz * 2 * sizeof(double);
+  while (nb > 32 && (size_t)nb * nz * sizeof(double) > 100 * 1024) nb /= 2;
+  const size_t smem = (size_t)nb * nz * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(pivoting_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pivoting_solve_kernel smem: %s", cudaGetErrorString(e));
