@@ -26,8 +26,8 @@
 //   are skipped.
 // * Grid divisions become multiplications by reciprocals computed once per
 //   CTA; slope divisions become multiplications by the shared reciprocals.
-// * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-6
-//   Taylor polynomial of degree 4 about the points -4 + n/256 (taper_table.inc,
+// * The taper 0.5*(1+tanh(x)) (isoneutral.py:10-15) is a piecewise degree-4
+//   Taylor polynomial about the points -4 + n/256 on [-4, 2] (taper_table.inc,
 //   truncation error < 2e-15), the library tanh elsewhere, and an FP32 exp
 //   below x = -10 where the taper is below 2e-9.
 // * The two clamped reciprocals 1/(min(0, G) - epsln) per point use an FP32

@@ -193,12 +193,25 @@ struct SfArgs {
   double *B1, *B2;
 };
 
-// K_gm edge-padded in z (utilities.py:24-35), averaged onto the face
-__device__ __forceinline__ double kgm_face(const SfArgs &a, long long o, long long dn, int k) {
-  const long long up = k > 0 ? -a.L.plane : 0;  // pad: level k-1 clamps to 0
-  return 0.25 * (a.Kgm[o] + a.Kgm[o + up] + a.Kgm[o + dn] + a.Kgm[o + dn + up]);
+// x / 16 through the exponent field: exact, as the multiplication by 2^-4
+// is, whenever the result is a normal number; zeros, subnormal results, inf
+// and NaN take the multiplication. An integer subtraction instead of an FP64
+// multiply (the FP64 pipe bounds this kernel).
+__device__ __forceinline__ double div16(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long e = (b >> 52) & 0x7FF;
+  return (e > 4 && e < 0x7FF) ? __longlong_as_double(b - (4LL << 52)) : x * 0.0625;
 }
 
+// Sum of the four K_gm around a face, K_gm edge-padded in z (utilities.py:24-35),
+// added in the reference's order; the face value is this sum / 4.
+__device__ __forceinline__ double kgm_sum(const SfArgs &a, long long o, long long dn, int k) {
+  const long long up = k > 0 ? -a.L.plane : 0;  // pad: level k-1 clamps to 0
+  return a.Kgm[o] + a.Kgm[o + up] + a.Kgm[o + dn] + a.Kgm[o + dn + up];
+}
+
+// 0.25 * (0.25 * sum) * s = (sum * s) / 16 exactly: both quarter scalings are
+// exact, so one product and an exponent shift give the reference's bits.
 __global__ void __launch_bounds__(128) streamfunction_kernel(SfArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y, k = blockIdx.z;
@@ -207,15 +220,13 @@ __global__ void __launch_bounds__(128) streamfunction_kernel(SfArgs a) {
   const long long o = L.at(i, j, k);
   // B2_gm[1:-2, 2:-2] (isoneutral.py:241-244)
   if (i >= 1 && i < L.X - 2 && j >= 2 && j < L.Y - 2) {
-    const double diffloc = kgm_face(a, o, 1, k);
     const double s = a.Aez[o] + a.Aez[o + a.sr] + a.Aez[o + a.sp] + a.Aez[o + a.sp + a.sr];
-    a.B2[o] = 0.25 * diffloc * s;
+    a.B2[o] = div16(kgm_sum(a, o, 1, k) * s);
   }
   // B1_gm[2:-2, 1:-2] (isoneutral.py:249-252)
   if (i >= 2 && i < L.X - 2 && j >= 1 && j < L.Y - 2) {
-    const double diffloc = kgm_face(a, o, L.pitch, k);
     const double s = a.Anz[o] + a.Anz[o + a.sr] + a.Anz[o + a.sp] + a.Anz[o + a.sp + a.sr];
-    a.B1[o] = -0.25 * diffloc * s;
+    a.B1[o] = div16(kgm_sum(a, o, L.pitch, k) * -s);
   }
 }
 
