@@ -94,84 +94,109 @@ __device__ __forceinline__ F face_diffloc(F pair, F pair_below, int k, double s1
   return q * (k >= 1 ? pair + pair_below : pair);
 }
 
+// c[0..3]: the four slope components of the face; c[4]: K_11 / (cost dxu);
+// c[5]: diffloc / (4 dzt), which scales the sum of the four vertical terms
+// once instead of each component.
 template <typename F>
-__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_cost_dxu, F c[5]) {
-  c[0] = pm(diffloc, ld(a.Aez, o));
-  c[1] = pm(diffloc, ld(a.Aez, o + a.sp));
-  c[2] = pm(diffloc, ld(a.Aez, o + a.sr));
-  c[3] = pm(diffloc, ld(a.Aez, o + a.sp + a.sr));
+__device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_cost_dxu, F q_dzt,
+                                          F c[6]) {
+  c[0] = ld(a.Aez, o);
+  c[1] = ld(a.Aez, o + a.sp);
+  c[2] = ld(a.Aez, o + a.sr);
+  c[3] = ld(a.Aez, o + a.sp + a.sr);
   c[4] = pm(inv_cost_dxu, ld(a.K11, o));
+  c[5] = pm(diffloc, q_dzt);
+}
+
+// flux of one tracer through a face from the face coefficients and the
+// tracer differences: the two lower and the two upper vertical differences
+// of the face's points, and the difference across the face
+template <typename F>
+__device__ __forceinline__ F face_flux(const F c[6], double z0m, double z1m, double z0p, double z1p, double h) {
+  F sumz = pm(c[0], to_F<F>(z0m));
+  sumz = pfma(c[1], to_F<F>(z1m), sumz);
+  sumz = pfma(c[2], to_F<F>(z0p), sumz);
+  sumz = pfma(c[3], to_F<F>(z1p), sumz);
+  return pfma(sumz, c[5], pm(to_F<F>(h), c[4]));
 }
 
 template <typename F>
-__device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long long o, int k, const F c[5], F q_dzt) {
+__device__ __forceinline__ F east_flux(const Layout &L, const double *tr, long long o, int k, const F c[6]) {
   const long long dm = k > 0 ? L.plane : 0;  // edge padding in z (utilities.py:24-35)
   const long long dp = k < L.Z - 1 ? L.plane : 0;
   const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + 1);
   const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + 1 - dm);
   const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + 1 + dp);
-  F sumz = pm(c[0], to_F<F>(t0 - t0m));
-  sumz = pfma(c[1], to_F<F>(t1 - t1m), sumz);
-  sumz = pfma(c[2], to_F<F>(t0p - t0), sumz);
-  sumz = pfma(c[3], to_F<F>(t1p - t1), sumz);
-  return pfma(sumz, q_dzt, pm(to_F<F>(t1 - t0), c[4]));
+  return face_flux(c, t0 - t0m, t1 - t1m, t0p - t0, t1p - t1, t1 - t0);
 }
 
 // north face of cell (i, j, k), valid for i in [2, X-2), j in [1, Y-2) (diffusion.py:52-77)
 template <typename F>
-__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_dyu, F c[5]) {
-  c[0] = pm(diffloc, ld(a.Anz, o));
-  c[1] = pm(diffloc, ld(a.Anz, o + a.sp));
-  c[2] = pm(diffloc, ld(a.Anz, o + a.sr));
-  c[3] = pm(diffloc, ld(a.Anz, o + a.sp + a.sr));
+__device__ __forceinline__ void north_coef(const DiffArgs<F> &a, long long o, F diffloc, F inv_dyu, F q_dzt,
+                                           F c[6]) {
+  c[0] = ld(a.Anz, o);
+  c[1] = ld(a.Anz, o + a.sp);
+  c[2] = ld(a.Anz, o + a.sr);
+  c[3] = ld(a.Anz, o + a.sp + a.sr);
   c[4] = pm(inv_dyu, ld(a.K22, o));
+  c[5] = pm(diffloc, q_dzt);
 }
 
 template <typename F>
-__device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long long o, int k, const F c[5], F cosu,
-                                        F q_dzt) {
+__device__ __forceinline__ F north_flux(const Layout &L, const double *tr, long long o, int k, const F c[6],
+                                        F cosu) {
   const long long P = L.pitch;
   const long long dm = k > 0 ? L.plane : 0;
   const long long dp = k < L.Z - 1 ? L.plane : 0;
   const double t0 = __ldg(tr + o), t1 = __ldg(tr + o + P);
   const double t0m = __ldg(tr + o - dm), t1m = __ldg(tr + o + P - dm);
   const double t0p = __ldg(tr + o + dp), t1p = __ldg(tr + o + P + dp);
-  F sumz = pm(c[0], to_F<F>(t0 - t0m));
-  sumz = pfma(c[1], to_F<F>(t1 - t1m), sumz);
-  sumz = pfma(c[2], to_F<F>(t0p - t0), sumz);
-  sumz = pfma(c[3], to_F<F>(t1p - t1), sumz);
-  return pm(cosu, pfma(sumz, q_dzt, pm(to_F<F>(t1 - t0), c[4])));
+  return pm(cosu, face_flux(c, t0 - t0m, t1 - t1m, t0p - t0, t1p - t1, t1 - t0));
 }
 
-// top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111)
+// top face of interior cell (i, j, k < Z-1) (diffusion.py:85-111).
+// c[0..3]: the x slope components; c[4..7]: the y slope components times
+// cosu of their face; c[8] = K2 / (4 dxt cost) and c[9] = K2 / (4 dyt cost)
+// scale the two sums once.
 template <typename F>
-__device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F inv_cost, F cosu_s, F cosu_c, F c[8]) {
+__device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F qx_cost, F q_dyt_cost, F cosu_s,
+                                         F cosu_c, F c[10]) {
   const F diffloc = a.s2 == 1.0 ? ld(a.K, o) : to_F<F>(a.s2) * ld(a.K, o);  // K2 = s2 K (diffusion.py:16)
-  const F dx = pm(diffloc, inv_cost), ds = pm(diffloc, cosu_s), dc = pm(diffloc, cosu_c);
-  c[0] = pm(dx, ld(a.Abx, o));
-  c[1] = pm(dx, ld(a.Abx, o + a.sr));
-  c[2] = pm(dx, ld(a.Abx, o + a.sp));
-  c[3] = pm(dx, ld(a.Abx, o + a.sp + a.sr));
-  c[4] = pm(ds, ld(a.Aby, o));
-  c[5] = pm(ds, ld(a.Aby, o + a.sr));
-  c[6] = pm(dc, ld(a.Aby, o + a.sp));
-  c[7] = pm(dc, ld(a.Aby, o + a.sp + a.sr));
+  c[0] = ld(a.Abx, o);
+  c[1] = ld(a.Abx, o + a.sr);
+  c[2] = ld(a.Abx, o + a.sp);
+  c[3] = ld(a.Abx, o + a.sp + a.sr);
+  c[4] = pm(cosu_s, ld(a.Aby, o));
+  c[5] = pm(cosu_s, ld(a.Aby, o + a.sr));
+  c[6] = pm(cosu_c, ld(a.Aby, o + a.sp));
+  c[7] = pm(cosu_c, ld(a.Aby, o + a.sp + a.sr));
+  c[8] = pm(diffloc, qx_cost);
+  c[9] = pm(diffloc, q_dyt_cost);
+}
+
+// top flux of one tracer from the west, east, south and north differences on
+// the face's lower (k) and upper (k+1) levels
+template <typename F>
+__device__ __forceinline__ F top_face_flux(const F c[10], double w0, double w1, double e0, double e1, double s0,
+                                           double s1, double n0, double n1) {
+  F sumx = pm(c[0], to_F<F>(w0));
+  sumx = pfma(c[1], to_F<F>(w1), sumx);
+  sumx = pfma(c[2], to_F<F>(e0), sumx);
+  sumx = pfma(c[3], to_F<F>(e1), sumx);
+  F sumy = pm(c[4], to_F<F>(s0));
+  sumy = pfma(c[5], to_F<F>(s1), sumy);
+  sumy = pfma(c[6], to_F<F>(n0), sumy);
+  sumy = pfma(c[7], to_F<F>(n1), sumy);
+  return pfma(sumx, c[8], pm(sumy, c[9]));
 }
 
 template <typename F>
-__device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long long o, const F c[8], F q_dxt,
-                                      F q_dyt_cost) {
+__device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long long o, const F c[10]) {
   const long long P = L.pitch, Q = L.plane;
   const double tc = __ldg(tr + o), tcu = __ldg(tr + o + Q);
-  F sumx = pm(c[0], to_F<F>(tc - __ldg(tr + o - 1)));
-  sumx = pfma(c[1], to_F<F>(tcu - __ldg(tr + o - 1 + Q)), sumx);
-  sumx = pfma(c[2], to_F<F>(__ldg(tr + o + 1) - tc), sumx);
-  sumx = pfma(c[3], to_F<F>(__ldg(tr + o + 1 + Q) - tcu), sumx);
-  F sumy = pm(c[4], to_F<F>(tc - __ldg(tr + o - P)));
-  sumy = pfma(c[5], to_F<F>(tcu - __ldg(tr + o - P + Q)), sumy);
-  sumy = pfma(c[6], to_F<F>(__ldg(tr + o + P) - tc), sumy);
-  sumy = pfma(c[7], to_F<F>(__ldg(tr + o + P + Q) - tcu), sumy);
-  return pfma(sumx, q_dxt, pm(sumy, q_dyt_cost));
+  return top_face_flux(c, tc - __ldg(tr + o - 1), tcu - __ldg(tr + o - 1 + Q), __ldg(tr + o + 1) - tc,
+                       __ldg(tr + o + 1 + Q) - tcu, tc - __ldg(tr + o - P), tcu - __ldg(tr + o - P + Q),
+                       __ldg(tr + o + P) - tc, __ldg(tr + o + P + Q) - tcu);
 }
 
 // One tile (bx, by) and k-chunk bz of NTR tracers of one domain; the whole CTA
@@ -200,13 +225,12 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   const bool own = i < L.X - 2 && j < L.Y - 2;
   const int ic = min(i, L.X - 3), jc = min(j, L.Y - 3);
   const double cost = a.g.cost[jc];
-  const F inv_cost = F(1.0 / cost);
   const F inv_cost_dxu = F(1.0 / (cost * a.g.dxu[ic]));
   const F cosu_c = F(a.g.cosu[jc]), cosu_s = F(a.g.cosu[jc - 1]);
   const F inv_dyu = F(1.0 / a.g.dyu[jc]);
   const F inv_fx = F(1.0 / (cost * a.g.dxt[ic]));  // divergence factors (diffusion.py:127, :129)
   const F inv_fy = F(1.0 / (cost * a.g.dyt[jc]));
-  const F q_dxt = F(1.0 / (4.0 * a.g.dxt[ic]));
+  const F qx_cost = F(1.0 / (4.0 * a.g.dxt[ic] * cost));
   const F q_dyt_cost = F(1.0 / (4.0 * a.g.dyt[jc] * cost));
   // halo faces: warp 0 the south row of north faces, warp 1 the west column of east faces
   const int hi_n = i0 + lane;  // north face (hi_n, j0-1)
@@ -222,18 +246,20 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
 
   // Tracer values and differences of the own faces carried up the column:
   // per tracer the values at the own, east and north columns, their vertical
-  // differences t(k) - t(k-1) (0 at k = 0, edge padding), and the west and
-  // south differences around the own point; each level loads the level above
-  // once and forms its differences once.
+  // differences t(k) - t(k-1) (0 at k = 0, edge padding), and the four
+  // horizontal differences around the own point; each level loads the level
+  // above once and forms its differences once. The K pair sums of the east
+  // and north faces are carried the same way.
   const long long P = L.pitch, Q = L.plane;
   double vc[NTR], ve[NTR], vn[NTR];     // values at level k
   double dzc[NTR], dze[NTR], dzn[NTR];  // t(k) - t(k-1)
-  double hw[NTR], hs[NTR];              // west and south differences at level k
+  double hw[NTR], hs[NTR], he[NTR], hn[NTR];  // west, south, east, north differences at level k
   F ft_prev[NTR];
+  F pe_below = 0, pn_below = 0;  // K pair sums of the east / north face on level k-1
 #pragma unroll
   for (int r = 0; r < NTR; ++r) {
     ft_prev[r] = 0.0;
-    vc[r] = ve[r] = vn[r] = dzc[r] = dze[r] = dzn[r] = hw[r] = hs[r] = 0.0;
+    vc[r] = ve[r] = vn[r] = dzc[r] = dze[r] = dzn[r] = hw[r] = hs[r] = he[r] = hn[r] = 0.0;
   }
   if (own) {
     const long long ob = L.at(i, j, kb);
@@ -245,6 +271,8 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       vn[r] = __ldg(tr + ob + P);
       hw[r] = vc[r] - __ldg(tr + ob - 1);
       hs[r] = vc[r] - __ldg(tr + ob - P);
+      he[r] = ve[r] - vc[r];
+      hn[r] = vn[r] - vc[r];
       if (kb > 0) {
         dzc[r] = vc[r] - __ldg(tr + ob - Q);
         dze[r] = ve[r] - __ldg(tr + ob + 1 - Q);
@@ -253,10 +281,13 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     }
     if (kb > 0) {
       const long long op = L.at(i, j, kb - 1);
-      F ct[8];
-      top_coef(a, op, inv_cost, cosu_s, cosu_c, ct);
+      const F kd = ld(a.K, op);
+      pe_below = kd + ld(a.K, op + 1);
+      pn_below = kd + ld(a.K, op + P);
+      F ct[10];
+      top_coef(a, op, qx_cost, q_dyt_cost, cosu_s, cosu_c, ct);
 #pragma unroll
-      for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, op, ct, q_dxt, q_dyt_cost);
+      for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, op, ct);
     }
   }
 
@@ -288,48 +319,24 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
           uw[r] = us[r] = 0.0;
         }
       }
-      F ce[5], cn[5];
+      F ce[6], cn[6];
       const F kc = ld(a.K, o), pe = kc + ld(a.K, o + 1), pn = kc + ld(a.K, o + P);
-      F pe_below = 0, pn_below = 0;
-      if (k >= 1) {
-        const F kd = ld(a.K, o - Q);
-        pe_below = kd + ld(a.K, o + 1 - Q);
-        pn_below = kd + ld(a.K, o + P - Q);
-      }
-      east_coef(a, o, face_diffloc(pe, pe_below, k, a.s1), inv_cost_dxu, ce);
-      north_coef(a, o, face_diffloc(pn, pn_below, k, a.s1), inv_dyu, cn);
-      F ct[8];
-      if (up) top_coef(a, o, inv_cost, cosu_s, cosu_c, ct);
+      east_coef(a, o, face_diffloc(pe, pe_below, k, a.s1), inv_cost_dxu, qz, ce);
+      north_coef(a, o, face_diffloc(pn, pn_below, k, a.s1), inv_dyu, qz, cn);
+      pe_below = pe;
+      pn_below = pn;
+      F ct[10];
+      if (up) top_coef(a, o, qx_cost, q_dyt_cost, cosu_s, cosu_c, ct);
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
         // z differences above the own, east and north columns (0 on the top level)
         const double zc = uc[r] - vc[r], ze = ue[r] - ve[r], zn = un[r] - vn[r];
-        const double he = ve[r] - vc[r], hn = vn[r] - vc[r];  // east and north differences at level k
-        // east face (diffusion.py:25-47)
-        F sz = pm(ce[0], to_F<F>(dzc[r]));
-        sz = pfma(ce[1], to_F<F>(dze[r]), sz);
-        sz = pfma(ce[2], to_F<F>(zc), sz);
-        sz = pfma(ce[3], to_F<F>(ze), sz);
-        fe[r] = pfma(sz, qz, pm(to_F<F>(he), ce[4]));
-        // north face (diffusion.py:52-77)
-        F sn = pm(cn[0], to_F<F>(dzc[r]));
-        sn = pfma(cn[1], to_F<F>(dzn[r]), sn);
-        sn = pfma(cn[2], to_F<F>(zc), sn);
-        sn = pfma(cn[3], to_F<F>(zn), sn);
-        fn[r] = pm(cosu_c, pfma(sn, qz, pm(to_F<F>(hn), cn[4])));
+        // east face (diffusion.py:25-47), north face (:52-77)
+        fe[r] = face_flux(ce, dzc[r], dze[r], zc, ze, he[r]);
+        fn[r] = pm(cosu_c, face_flux(cn, dzc[r], dzn[r], zc, zn, hn[r]));
         // horizontal differences on level k+1
         const double hw1 = uc[r] - uw[r], he1 = ue[r] - uc[r], hs1 = uc[r] - us[r], hn1 = un[r] - uc[r];
-        if (up) {  // top face (diffusion.py:85-111)
-          F sx = pm(ct[0], to_F<F>(hw[r]));
-          sx = pfma(ct[1], to_F<F>(hw1), sx);
-          sx = pfma(ct[2], to_F<F>(he), sx);
-          sx = pfma(ct[3], to_F<F>(he1), sx);
-          F sy = pm(ct[4], to_F<F>(hs[r]));
-          sy = pfma(ct[5], to_F<F>(hs1), sy);
-          sy = pfma(ct[6], to_F<F>(hn), sy);
-          sy = pfma(ct[7], to_F<F>(hn1), sy);
-          ft[r] = pfma(sx, q_dxt, pm(sy, q_dyt_cost));
-        }
+        if (up) ft[r] = top_face_flux(ct, hw[r], hw1, he[r], he1, hs[r], hs1, hn[r], hn1);  // (diffusion.py:85-111)
         vc[r] = uc[r];
         ve[r] = ue[r];
         vn[r] = un[r];
@@ -338,27 +345,29 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
         dzn[r] = zn;
         hw[r] = hw1;
         hs[r] = hs1;
+        he[r] = he1;
+        hn[r] = hn1;
         fe_s[b][r][ty][tx + 1] = fe[r];
         fn_s[b][r][ty + 1][tx] = fn[r];
       }
     }
     if (halo_n) {
       const long long oh = L.at(hi_n, j0 - 1, k);
-      F cn[5];
+      F cn[6];
       const F pn = ld(a.K, oh) + ld(a.K, oh + L.pitch);
       const F pnb = k >= 1 ? ld(a.K, oh - L.plane) + ld(a.K, oh + L.pitch - L.plane) : F(0);
-      north_coef(a, oh, face_diffloc(pn, pnb, k, a.s1), h_inv_dyu, cn);
+      north_coef(a, oh, face_diffloc(pn, pnb, k, a.s1), h_inv_dyu, qz, cn);
 #pragma unroll
-      for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu, qz);
+      for (int r = 0; r < NTR; ++r) fn_s[b][r][0][lane] = north_flux(L, A[r].tr, oh, k, cn, h_cosu);
     }
     if (halo_e) {
       const long long oh = L.at(i0 - 1, hj_e, k);
-      F ce[5];
+      F ce[6];
       const F pe = ld(a.K, oh) + ld(a.K, oh + 1);
       const F peb = k >= 1 ? ld(a.K, oh - L.plane) + ld(a.K, oh + 1 - L.plane) : F(0);
-      east_coef(a, oh, face_diffloc(pe, peb, k, a.s1), h_inv_cost_dxu, ce);
+      east_coef(a, oh, face_diffloc(pe, peb, k, a.s1), h_inv_cost_dxu, qz, ce);
 #pragma unroll
-      for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce, qz);
+      for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce);
     }
     __syncthreads();
     if (own && (__ldg(a.m + o) & VG_MASK_T)) {  // maskT multiplies the divergence (diffusion.py:123-137)
