@@ -98,8 +98,10 @@ struct Smem {
   static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
   F q[2][NQ][NP];  // per-point quantities; the split form keeps them FP32 (R computed in FP64)
   F pub[2][NPB][NP];
-  double inv_dxu[PX], inv_dyu[PY], inv_cost[PY], facty[PY];
-  double qinv_dxt[PX], qinv_dyt_cost[PY], dxu[PX];
+  double inv_dxu[PX], inv_dyu[PY], inv_cost[PY];
+  // K_33 weights of the top face's slopes: dxu(i-1+ip) / (4 dxt(i)) by thread column,
+  // cosu(j-1+jp) dyu(j-1+jp) / (4 dyt(j) cost(j)) by thread row
+  double dqx[2][PX], dqy[2][PY];
   uint8_t qm[2][NP];
   // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant
 };
@@ -169,16 +171,28 @@ __device__ __forceinline__ float taper_t<float>(float s, const TaperConsts &c) {
 __device__ __forceinline__ double max_t(double a, double b) { return dmax(a, b); }
 __device__ __forceinline__ float max_t(float a, float b) { return fmaxf(a, b); }
 
-// taper * s^2 for the K_33 sums
+__device__ __forceinline__ bool nonneg(double x) { return __double_as_longlong(x) >= 0; }
+__device__ __forceinline__ bool nonneg(float x) { return __float_as_int(x) >= 0; }
+
+// sum over kr, ip of dzw(kr) max(K_iso_steep, diffloc taper(kr, ip)) for K_11 / K_22
+// (isoneutral.py:123-128, :160-165); t[0][*] = 0 on level 0. With K_iso_steep <= 0
+// and diffloc >= 0 every max is its second argument, so diffloc factors out.
 template <typename F>
-__device__ __forceinline__ F sq_term(F tp, F ai, F s);
-template <>
-__device__ __forceinline__ double sq_term<double>(double tp, double ai, double s) {
-  return ai * s;
-}
-template <>
-__device__ __forceinline__ float sq_term<float>(float tp, float ai, float s) {
-  return ai * s;
+__device__ __forceinline__ F face_sumz(const F t[2][2], const F dzwF[2], F diffloc, F ksteepF, bool lin_steep,
+                                       int k) {
+  if (lin_steep && nonneg(diffloc)) {
+    F S = dzwF[1] * (t[1][0] + t[1][1]);
+    if (k > 0) S = dzwF[0] * (t[0][0] + t[0][1]) + S;
+    return diffloc * S;
+  }
+  F sumz = 0.0;
+#pragma unroll
+  for (int kr = 0; kr < 2; ++kr) {
+    if (kr == 0 && k == 0) continue;
+    sumz += dzwF[kr] * max_t(ksteepF, diffloc * t[kr][0]);
+    sumz += dzwF[kr] * max_t(ksteepF, diffloc * t[kr][1]);
+  }
+  return sumz;
 }
 
 // One tile (bx, by) and k-chunk bz of one domain; the whole CTA takes part.
@@ -205,15 +219,23 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   for (int p = tid; p < PX; p += NT) {
     const int i = min(max(i0 - 1 + p, 0), L.X - 1);
     sm.inv_dxu[p] = 1.0 / a.g.dxu[i];
-    sm.qinv_dxt[p] = 1.0 / (4.0 * a.g.dxt[i]);
-    sm.dxu[p] = a.g.dxu[i];
   }
   for (int p = tid; p < PY; p += NT) {
     const int j = min(max(j0 - 1 + p, 0), L.Y - 1);
     sm.inv_dyu[p] = 1.0 / a.g.dyu[j];
     sm.inv_cost[p] = 1.0 / a.g.cost[j];
-    sm.facty[p] = a.g.cosu[j] * a.g.dyu[j];  // isoneutral.py:202
-    sm.qinv_dyt_cost[p] = 1.0 / (4.0 * a.g.dyt[j] * a.g.cost[j]);
+  }
+  for (int p = tid; p < TX; p += NT) {
+    const int i = min(i0 + p, L.X - 1);
+    const double q = 1.0 / (4.0 * a.g.dxt[i]);
+    sm.dqx[0][p] = a.g.dxu[i - 1] * q;
+    sm.dqx[1][p] = a.g.dxu[i] * q;
+  }
+  for (int p = tid; p < TY; p += NT) {
+    const int j = min(j0 + p, L.Y - 1);
+    const double q = 1.0 / (4.0 * a.g.dyt[j] * a.g.cost[j]);
+    sm.dqy[0][p] = a.g.cosu[j - 1] * a.g.dyu[j - 1] * q;  // facty (isoneutral.py:202)
+    sm.dqy[1][p] = a.g.cosu[j] * a.g.dyu[j] * q;
   }
   for (int k = tid; k < Z; k += NT) {
     zdzw[k] = a.g.dzw[k];
@@ -397,6 +419,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   slopes_level(kb, kb & 1, cur);
 
   const int i = i0 + tx, j = j0 + ty;
+  const bool lin_steep = a.ksteep <= 0.0;
   const bool east = i < L.X - 2 && j >= 2 && j < L.Y - 2;
   const bool north = i >= 2 && i < L.X - 2 && j < L.Y - 2;
   const bool top = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
@@ -424,15 +447,16 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                                __ldg(a.K + o + 1 - L.plane));
         else
           diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + 1));
+        F t[2][2] = {{F(0), F(0)}, {F(0), F(0)}};  // [kr][ip]
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
-          const F t0 = cur[S_XE0 + kr].t, t1 = pb[PB_T_XW0 + kr][pc + 1];
-          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t0);
-          a.Aez[o + kr * a.sr] = t0 * F(cur[S_XE0 + kr].s);
-          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t1);
+          t[kr][0] = cur[S_XE0 + kr].t;
+          t[kr][1] = pb[PB_T_XW0 + kr][pc + 1];
+          a.Aez[o + kr * a.sr] = t[kr][0] * F(cur[S_XE0 + kr].s);
           a.Aez[o + a.sp + kr * a.sr] = pb[PB_TS_XW0 + kr][pc + 1];
         }
+        sumz = face_sumz(t, dzwF, diffloc, ksteepF, lin_steep, k);
       } else {
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
@@ -454,15 +478,16 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                                __ldg(a.K + o + L.pitch - L.plane));
         else
           diffloc = F(0.5) * (__ldg(a.K + o) + __ldg(a.K + o + L.pitch));
+        F t[2][2] = {{F(0), F(0)}, {F(0), F(0)}};
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
           if (kr == 0 && k == 0) continue;
-          const F t0 = cur[S_YN0 + kr].t, t1 = pb[PB_T_YS0 + kr][pc + PX];
-          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t0);
-          a.Anz[o + kr * a.sr] = t0 * F(cur[S_YN0 + kr].s);
-          sumz += dzwF[kr] * max_t(ksteepF, diffloc * t1);
+          t[kr][0] = cur[S_YN0 + kr].t;
+          t[kr][1] = pb[PB_T_YS0 + kr][pc + PX];
+          a.Anz[o + kr * a.sr] = t[kr][0] * F(cur[S_YN0 + kr].s);
           a.Anz[o + a.sp + kr * a.sr] = pb[PB_TS_YS0 + kr][pc + PX];
         }
+        sumz = face_sumz(t, dzwF, diffloc, ksteepF, lin_steep, k);
       } else {
 #pragma unroll
         for (int kr = 0; kr < 2; ++kr) {
@@ -475,32 +500,33 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     }
 
     // top face: Ai_bx, Ai_by, K_33 (isoneutral.py:173-224); kr = 0 is this point's upper slopes,
-    // kr = 1 the lower slopes of the point above
+    // kr = 1 the lower slopes of the point above. K_33 = K_iso sum over the 8 slopes of
+    // w (taper s) s, w the slope's dqx / dqy weight: K_iso factors out of the sums.
     if (top && k < Z - 1) {
-      F sumx = 0.0, sumy = 0.0;
-      const F dxuF[2] = {to_F<F>(sm.dxu[tx]), to_F<F>(sm.dxu[tx + 1])};
-      const F factyF[2] = {to_F<F>(sm.facty[ty]), to_F<F>(sm.facty[ty + 1])};
+      F k33 = 0.0;
       if (mk & VG_MASK_W) {
-        const F Kc = __ldg(a.K + o);
+        F sx[2], sy[2];
 #pragma unroll
-        for (int kr = 0; kr < 2; ++kr) {
-#pragma unroll
-          for (int ip = 0; ip < 2; ++ip) {
-            const Slope<F> sl = kr == 0 ? cur[ip ? S_XE1 : S_XW1] : nxt[ip ? S_XE0 : S_XW0];
-            const F ai = sl.t * F(sl.s);
-            // taper*s^2 as (taper*s)*s: reuses Ai and stays finite where an FP32 s^2
-            // would overflow under a vanishing taper
-            sumx += dxuF[ip] * Kc * sq_term<F>(sl.t, ai, sl.s);
-            a.Abx[o + ip * a.sp + kr * a.sr] = ai;
-          }
-#pragma unroll
-          for (int jp = 0; jp < 2; ++jp) {
-            const Slope<F> sl = kr == 0 ? cur[jp ? S_YN1 : S_YS1] : nxt[jp ? S_YN0 : S_YS0];
-            const F ai = sl.t * F(sl.s);
-            sumy += factyF[jp] * Kc * sq_term<F>(sl.t, ai, sl.s);
-            a.Aby[o + jp * a.sp + kr * a.sr] = ai;
-          }
+        for (int ip = 0; ip < 2; ++ip) {
+          const Slope<F> s0 = cur[ip ? S_XE1 : S_XW1], s1 = nxt[ip ? S_XE0 : S_XW0];
+          const F a0 = s0.t * F(s0.s), a1 = s1.t * F(s1.s);
+          a.Abx[o + ip * a.sp] = a0;
+          a.Abx[o + ip * a.sp + a.sr] = a1;
+          // taper*s^2 as (taper*s)*s: reuses Ai and stays finite where an FP32 s^2
+          // would overflow under a vanishing taper
+          sx[ip] = a0 * F(s0.s) + a1 * F(s1.s);
         }
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp) {
+          const Slope<F> s0 = cur[jp ? S_YN1 : S_YS1], s1 = nxt[jp ? S_YN0 : S_YS0];
+          const F a0 = s0.t * F(s0.s), a1 = s1.t * F(s1.s);
+          a.Aby[o + jp * a.sp] = a0;
+          a.Aby[o + jp * a.sp + a.sr] = a1;
+          sy[jp] = a0 * F(s0.s) + a1 * F(s1.s);
+        }
+        const F w = to_F<F>(sm.dqx[0][tx]) * sx[0] + to_F<F>(sm.dqx[1][tx]) * sx[1] +
+                    to_F<F>(sm.dqy[0][ty]) * sy[0] + to_F<F>(sm.dqy[1][ty]) * sy[1];
+        k33 = __ldg(a.K + o) * w;
       } else {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -509,7 +535,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           a.Aby[oc] = 0.0;
         }
       }
-      a.K33[o] = sumx * to_F<F>(sm.qinv_dxt[tx + 1]) + sumy * to_F<F>(sm.qinv_dyt_cost[ty + 1]);
+      a.K33[o] = k33;
     }
 #pragma unroll
     for (int n = 0; n < NS; ++n) cur[n] = nxt[n];
