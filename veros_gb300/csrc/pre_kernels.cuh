@@ -143,6 +143,16 @@ static __device__ __forceinline__ double taper_of(double s, double sc, double in
 // 1/d for d = min(0, G) - epsln, i.e. d in (-inf, -1e-20]
 static __device__ __forceinline__ double recip_neg(double d) { return recip_newton(d); }
 
+// min(0, G) - epsln (isoneutral.py:121, :158, :188, :207) with the FP64
+// subtraction only where it can change G: G >= +0 gives -epsln, and for
+// |G| >= 2^-13 epsln = 1e-20 is below half an ulp of G, so G - epsln = G.
+// Sign and exponent tests are integer operations.
+static __device__ __forceinline__ double clamp_eps(double G) {
+  const long long b = __double_as_longlong(G);
+  if (b >= 0) return -kEpsln;
+  return ((b >> 52) & 0x7FF) >= 1023 - 13 ? G : G - kEpsln;
+}
+
 // Split form: slope, taper argument and taper in FP32 (the slope's clamped
 // denominator was formed in FP64); slopec_f, inv_dslope_f are FP32 copies.
 static __device__ __forceinline__ float taper_of_split(float s, float slopec_f, float inv_dslope_f) {
@@ -315,8 +325,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         q[Q_SX][p] = to_F<F>(dSx);
         q[Q_TY][p] = to_F<F>(dTy);
         q[Q_SY][p] = to_F<F>(dSy);
-        q[Q_R0][p] = to_F<F>(recip_neg(fmin0(G0) - kEpsln));
-        q[Q_R1][p] = to_F<F>(recip_neg(fmin0(G1) - kEpsln));
+        q[Q_R0][p] = to_F<F>(recip_neg(clamp_eps(G0)));
+        q[Q_R1][p] = to_F<F>(recip_neg(clamp_eps(G1)));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
       }
       carryT[s] = dTz;
@@ -430,6 +440,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     __syncthreads();
     if (k + 1 < Z) slopes_level(k + 1, (k + 1) & 1, nxt);
     const F(*pb)[NP] = sm.pub[k & 1];
+    const F(*pbn)[NP] = sm.pub[(k + 1) & 1];  // level k+1 (written only when k + 1 < Z; read only then)
     const long long o = L.at(i, j, k);
     // the face terms' grid factors in the derived-field type
     const F dzwF[2] = {to_F<F>(zdzw[k > 0 ? k - 1 : 0]), to_F<F>(zdzw[k])}, qzF = to_F<F>(zq_dzt[k]);
@@ -508,8 +519,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         F sx[2], sy[2];
 #pragma unroll
         for (int ip = 0; ip < 2; ++ip) {
+          // the west slopes' taper*s were published by slopes_level (levels k and k+1)
           const Slope<F> s0 = cur[ip ? S_XE1 : S_XW1], s1 = nxt[ip ? S_XE0 : S_XW0];
-          const F a0 = s0.t * F(s0.s), a1 = s1.t * F(s1.s);
+          const F a0 = ip ? s0.t * F(s0.s) : pb[PB_TS_XW1][pc], a1 = ip ? s1.t * F(s1.s) : pbn[PB_TS_XW0][pc];
           a.Abx[o + ip * a.sp] = a0;
           a.Abx[o + ip * a.sp + a.sr] = a1;
           // taper*s^2 as (taper*s)*s: reuses Ai and stays finite where an FP32 s^2
@@ -519,7 +531,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 #pragma unroll
         for (int jp = 0; jp < 2; ++jp) {
           const Slope<F> s0 = cur[jp ? S_YN1 : S_YS1], s1 = nxt[jp ? S_YN0 : S_YS0];
-          const F a0 = s0.t * F(s0.s), a1 = s1.t * F(s1.s);
+          const F a0 = jp ? s0.t * F(s0.s) : pb[PB_TS_YS1][pc], a1 = jp ? s1.t * F(s1.s) : pbn[PB_TS_YS0][pc];
           a.Aby[o + jp * a.sp] = a0;
           a.Aby[o + jp * a.sp + a.sr] = a1;
           sy[jp] = a0 * F(s0.s) + a1 * F(s1.s);
