@@ -99,6 +99,7 @@ struct Smem {
   F q[2][NQ][NP];  // per-point quantities; the split form keeps them FP32 (R computed in FP64)
   F pub[2][NPB][NP];
   double inv_dxu[PX], inv_dyu[PY], inv_cost[PY];
+  double inv_dxu_cost[NP];  // 1 / (dxu cost) per plane point
   // K_33 weights of the top face's slopes: dxu(i-1+ip) / (4 dxt(i)) by thread column,
   // cosu(j-1+jp) dyu(j-1+jp) / (4 dyt(j) cost(j)) by thread row
   double dqx[2][PX], dqy[2][PY];
@@ -251,9 +252,17 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     zdzw[k] = a.g.dzw[k];
     zinv_dzw[k] = 1.0 / a.g.dzw[k];
     zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
-    // eq type 3: drho/dT = -(betaTs*(T - theta0) + betaT*(1 - gammas*grav*zz*rho0))*rho0
-    const double zz = -fabs(a.g.zt[k]) - 0.0;
-    zeos[k] = Eos::betaT * (1.0 - Eos::gammas * Eos::grav * zz * Eos::rho0);
+    // drho/dT = eos_c1 T + zeos[k]: type 3 -(betaTs (T - theta0) + betaT (1 - gammas grav zz rho0)) rho0
+    // with zz = -|zt|; types 2, 4 -(betaT + 2 betaTs (T - theta0)) rho0; type 1 -betaT rho0
+    if (a.eos_type == 3) {
+      const double zz = -fabs(a.g.zt[k]) - 0.0;
+      zeos[k] = (Eos::betaTs3 * Eos::theta0 - Eos::betaT * (1.0 - Eos::gammas * Eos::grav * zz * Eos::rho0)) *
+                Eos::rho0;
+    } else if (a.eos_type == 1) {
+      zeos[k] = -Eos::betaT * Eos::rho0;
+    } else {
+      zeos[k] = (2.0 * Eos::betaTs24 * Eos::theta0 - Eos::betaT) * Eos::rho0;
+    }
   }
 
   // K_33 on the top level is zero on the whole plane (isoneutral.py:225)
@@ -263,6 +272,11 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       if (i < L.X && j < L.Y) a.K33[L.at(i, j, Z - 1)] = 0.0;
     }
   }
+  __syncthreads();
+  for (int p = tid; p < NP; p += NT) sm.inv_dxu_cost[p] = sm.inv_dxu[p % PX] * sm.inv_cost[p / PX];
+  const double eos_c1 = a.eos_type == 3 ? -Eos::betaTs3 * Eos::rho0
+                        : a.eos_type == 1 ? 0.0
+                                          : -2.0 * Eos::betaTs24 * Eos::rho0;
   __syncthreads();
 
   // ---- per-point plane quantities ------------------------------------------
@@ -289,17 +303,11 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         mk = __ldg(a.m + o);
         const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
         if (mk & VG_MASK_T) {
-          const F Tf = to_F<F>(Tc);
-          if (a.eos_type == 1)
-            rT = F(-Eos::betaT * Eos::rho0);
-          else if (a.eos_type == 3)
-            rT = -(F(Eos::betaTs3) * (Tf - F(Eos::theta0)) + to_F<F>(zeos[lev])) * F(Eos::rho0);
-          else
-            rT = -(F(Eos::betaT) + F(2.0 * Eos::betaTs24) * (Tf - F(Eos::theta0))) * F(Eos::rho0);
+          rT = to_F<F>(Tc) * to_F<F>(eos_c1) + to_F<F>(zeos[lev]);  // (isoneutral.py:40, get_rho.py:93-112)
           rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
         }
         if ((mk & VG_MASK_U) && i < L.X - 1) {
-          const double f = sm.inv_dxu[pi] * sm.inv_cost[pj];
+          const double f = sm.inv_dxu_cost[p];
           dTx = (__ldg(a.T + o + 1) - Tc) * f;
           dSx = (__ldg(a.S + o + 1) - Sc) * f;
         }
