@@ -420,6 +420,16 @@ __global__ void __launch_bounds__(TX * TY, 2) flux_div_kernel(DiffArgs<F> a, Dif
 // factorisation is shared by the tracers. Shared memory holds c'_k and d'_k of
 // each tracer, [k][thread].
 // The solve of one column (i, j) whose water starts at level ks.
+// FP32 <-> FP64 conversions of the implicit solve: hardware conversions,
+// since this latency-bound kernel leaves the FP64 pipe mostly idle (the
+// integer forms of to_F / to_D lengthen its serial chain)
+__device__ __forceinline__ double cvt_d(double x) { return x; }
+__device__ __forceinline__ double cvt_d(float x) { return (double)x; }
+template <typename F>
+__device__ __forceinline__ F cvt_f(double x) {
+  return (F)x;
+}
+
 template <typename F, int NRHS>
 __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const DiffArgs<F> &b2, const double *dtdzw,
                                                 const double *inv_dzt, double *cps, double *dps, int t, int nb,
@@ -439,7 +449,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
   for (int u = 0; u < PF; ++u) {
     const int k = ks + u;
     const long long o = base + (long long)min(k, Z - 1) * L.plane;
-    qK[u] = k < Z - 1 ? to_D(ld(a.K33, o)) : 0.0;
+    qK[u] = k < Z - 1 ? cvt_d(ld(a.K33, o)) : 0.0;
 #pragma unroll
     for (int r = 0; r < NRHS; ++r) qT[u][r] = k < Z ? (double)trp[r][o] : 0.0;
   }
@@ -462,7 +472,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         const int kn = k + PF;
         if (kn < Z) {
           const long long on = base + (long long)kn * L.plane;
-          qK[u] = kn < Z - 1 ? to_D(ld(a.K33, on)) : 0.0;
+          qK[u] = kn < Z - 1 ? cvt_d(ld(a.K33, on)) : 0.0;
 #pragma unroll
           for (int r = 0; r < NRHS; ++r) qT[u][r] = (double)trp[r][on];
         }
@@ -496,7 +506,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
           t1[u][r] = (double)trp[r][o];
-          d1[u][r] = to_D(dtr[r][o]);
+          d1[u][r] = cvt_d(dtr[r][o]);
         }
       }
     }
@@ -510,7 +520,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         for (int r = 0; r < NRHS; ++r) {
           x[r] = pfma(-c, x[r], dps[((size_t)r * Z + k) * nb + t]);
           trp[r][o] = x[r];
-          dtr[r][o] = to_F<F>(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
+          dtr[r][o] = cvt_f<F>(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
         }
       }
     }
