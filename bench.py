@@ -166,6 +166,19 @@ def _profiled_traffic(name):
     return int(v) if v is not None else None
 
 
+def _fp64_roofline(step_ms):
+    """The step against the FP64 pipe, its binding resource: FP64 warp
+    instructions per step and the pipe's peak rate from the committed ncu
+    summary, the floor they imply, and the measured step's fraction of it."""
+    name = "fp64_pipe_roofline_global1deg.md"
+    n, peak = _profiled(name, "fp64_warp_instr_per_step"), _profiled(name, "fp64_peak_warp_instr_per_s")
+    if not n or not peak:
+        return None
+    floor_ms = n / peak * 1e3
+    return {"fp64_warp_instr_per_step": n, "peak_warp_instr_per_s": peak, "floor_ms": floor_ms,
+            "frac": floor_ms / step_ms, "source": f"profiles/{name}"}
+
+
 def cpu_baseline_sample(nz_band=None, steps=1):
     """Time the oracle step on one host core on a y-band sample of the workload."""
     from oracle import isoneutral_oracle as orc
@@ -712,6 +725,7 @@ def run_gb300(args):
                      "algorithmic_bytes_per_cell": PRE_BYTES_PER_CELL,
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,
                      "fp64_pipe_pct_ncu": _profiled("pre_tile_kernel_global1deg.md", "fp64_pipe_pct"),
+                     "fp64_roofline": _fp64_roofline(ms / args.steps),
                      "note": "FP64-pipe bound on GB300 (~1 TFLOP/s FP64); HBM fraction reported as asked"},
         "cpu_baseline": base,
         "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 2 * X * Y * Z * 8,
