@@ -720,7 +720,7 @@ def run_gb300(args):
                    "parallelism": f"replicas x{world}"},
         "stage_ms": {"prepare": float(stage_ms[:, 0].mean()), "pre": pre_ms,
                      "diffusion_temp_and_salt": float(stage_ms[:, 2].mean())},
-        "roofline": {"bound": "hbm", "kernel": "pre_tile_kernel", "achieved": pre_achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "pre_span_kernel", "achieved": pre_achieved, "peak": peak,
                      "unit": "GB/s", "frac": pre_achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "algorithmic_bytes_per_cell": PRE_BYTES_PER_CELL,
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,

@@ -18,7 +18,7 @@
 //
 // Launches (one stream, in order):
 //   1. adj_tables_kernel     reciprocal grid factors
-//   2. pre_tile_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel), and
+//   2. pre_span_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel), and
 //                            per point its 8 tapers, 8 slopes and 2 clamped reciprocals
 //   3. adj_implicit_kernel   per water column: the transposed tridiagonal
 //                            system A^T y = dL/dx (one Thomas factorisation

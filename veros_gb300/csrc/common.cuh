@@ -2,6 +2,8 @@
 // indexing and small device utilities.
 #pragma once
 
+#include <algorithm>
+
 #include <cuda_runtime.h>
 #include <stdarg.h>
 #include <stdint.h>
@@ -23,6 +25,19 @@ inline int check_launch(const char *what) {
 }
 
 int validate_domain(const VgDomain *dom);
+
+// CTAs for a span kernel (an even share of W work units per CTA): every CTA
+// the device holds at once, but at least min_units units each. 0 on error.
+template <typename K>
+inline int span_ctas(K kernel, int threads, size_t smem, long long W, int min_units) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1)
+    return 0;
+  const long long by_units = (W + min_units - 1) / min_units;
+  return (int)std::max(1LL, std::min((long long)sms * per, by_units));
+}
 
 struct Layout {
   int X, Y, Z;

@@ -3,8 +3,9 @@
 //
 // Two launches per tracer, or per temp-and-salt pair (one more with the
 // energy branch):
-//  1. flux_div_kernel  2.5-D tiled: a CTA owns 32 x 8 interior columns and
-//                      walks k upward. Per level it forms the east, north and
+//  1. flux_span_kernel 2.5-D tiled: a CTA owns 32 x 8 interior columns and
+//                      walks k upward (a persistent CTA walks its share of
+//                      the domain's tile-levels). Per level it forms the east, north and
 //                      top fluxes (diffusion.py:9-113) of its faces plus the
 //                      west/south halo faces, exchanges them through shared
 //                      memory, and applies the divergence (:116-139), the
@@ -199,12 +200,12 @@ __device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long lo
                        __ldg(tr + o + P) - tc, __ldg(tr + o + P + Q) - tcu);
 }
 
-// One tile (bx, by) and k-chunk bz of NTR tracers of one domain; the whole CTA
+// One tile (bx, by) and levels [kb, ke) of NTR tracers of one domain; the whole CTA
 // (32 x TY threads) takes part. A[0..NTR-1] differ only in their tracer
 // fields; geometry, tensor and masks come from A[0]. zq_dzt: dynamic shared
 // memory of 2 Z doubles.
 template <typename F, int TY, int NTR>
-__device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_dzt, int bx, int by, int bz) {
+__device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_dzt, int bx, int by, int kb, int ke) {
   constexpr int NT = TX * TY;
   __shared__ F fe_s[2][NTR][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
   __shared__ F fn_s[2][NTR][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
@@ -214,7 +215,6 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   double *zinv_dzt = zq_dzt + Z;  // 1/(4 dzt[k]) then 1/dzt[k]
   const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX, warp = tid / 32, lane = tid % 32;
   const int i0 = 2 + bx * TX, j0 = 2 + by * TY;
-  const int kb = bz * a.kchunk, ke = min(Z, kb + a.kchunk);
   for (int k = tid; k < Z; k += NT) {
     zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
     zinv_dzt[k] = 1.0 / a.g.dzt[k];
@@ -404,11 +404,24 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   __syncthreads();
 }
 
+// One domain: every resident CTA takes an equal share of the ntiles * Z
+// tile-levels, tile-major, as one segment per tile it touches (a segment
+// starting above level 0 pays the restart of a k-chunk); the body ends with a
+// barrier before its buffers are reused.
 template <typename F, int TY, int NTR>
-__global__ void __launch_bounds__(TX * TY, 2) flux_div_kernel(DiffArgs<F> a, DiffArgs<F> b) {
+__global__ void __launch_bounds__(TX * TY, 2) flux_span_kernel(DiffArgs<F> a, DiffArgs<F> b, int ntx, int ntiles) {
   extern __shared__ double zq_dzt[];
   const DiffArgs<F> A[2] = {a, b};
-  flux_div_body<F, TY, NTR>(A, zq_dzt, blockIdx.x, blockIdx.y, blockIdx.z);
+  const int Z = a.L.Z;
+  const long long W = (long long)ntiles * Z;
+  long long p = W * blockIdx.x / gridDim.x;
+  const long long end = W * (blockIdx.x + 1) / gridDim.x;
+  while (p < end) {
+    const int t = (int)(p / Z), kb = (int)(p % Z);
+    const int ke = (int)min((long long)Z, end - (long long)t * Z);
+    flux_div_body<F, TY, NTR>(A, zq_dzt, t % ntx, t / ntx, kb, ke);
+    p = (long long)t * Z + ke;
+  }
 }
 
 // Implicit solve of NRHS tracers sharing one matrix, one thread per column.

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched(const MemberArgs<F> *_
     stage(&a, &members[w.member].pre);
     if (threadIdx.x == 0) a.kchunk = kchunk > 0 ? min(kchunk, a.L.Z) : a.L.Z;
     __syncthreads();
-    pre_tile_body<F, TY>(a, smem_raw, w.a, w.b, w.c);
+    pre_tile_body<F, TY>(a, smem_raw, w.a, w.b, w.c * a.kchunk, min(a.L.Z, (w.c + 1) * a.kchunk));
   }
 }
 
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *
     stage(&a[1], &members[w.member].dS);
     if (threadIdx.x == 0) a[0].kchunk = a[1].kchunk = kchunk > 0 ? min(kchunk, a[0].L.Z) : a[0].L.Z;
     __syncthreads();
-    flux_div_body<F, TY, 2>(a, zq_dzt, w.a, w.b, w.c);
+    flux_div_body<F, TY, 2>(a, zq_dzt, w.a, w.b, w.c * a[0].kchunk, min(a[0].L.Z, (w.c + 1) * a[0].kchunk));
   }
 }
 

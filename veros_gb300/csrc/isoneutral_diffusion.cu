@@ -13,17 +13,19 @@ namespace vg {
 namespace {
 
 // NTR = 2: temp and salt in one pass over the tensor (b: salt); NTR = 1: a alone
+// Tiles of 32 x 8 columns; every resident CTA takes an equal share of the
+// tile-levels (flux_span_kernel), at least 8 levels each.
 template <typename F, int NTR>
 int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
   constexpr int TY = 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
-  int nchunks = 1;
-  while ((long long)nbx * nby * nchunks < 4 * 152 && a.L.Z / (nchunks * 2) >= 8) nchunks *= 2;
-  a.kchunk = b.kchunk = (a.L.Z + nchunks - 1) / nchunks;
-  const int nbz = (a.L.Z + a.kchunk - 1) / a.kchunk;
   const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-  flux_div_kernel<F, TY, NTR><<<dim3(nbx, nby, nbz), TX * TY, smem, s>>>(a, b);
-  return check_launch("flux_div_kernel");
+  const long long W = (long long)nbx * nby * a.L.Z;
+  const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, W, 8);
+  if (nc < 1) return fail(VG_ERR_LAUNCH, "flux_span_kernel: occupancy query failed");
+  a.kchunk = b.kchunk = a.L.Z;
+  flux_span_kernel<F, TY, NTR><<<nc, TX * TY, smem, s>>>(a, b, nbx, nbx * nby);
+  return check_launch("flux_span_kernel");
 }
 
 template <typename F, int NRHS>

@@ -206,9 +206,10 @@ __device__ __forceinline__ F face_sumz(const F t[2][2], const F dzwF[2], F diffl
   return sumz;
 }
 
-// One tile (bx, by) and k-chunk bz of one domain; the whole CTA takes part.
+// One tile (bx, by) and levels [kb, ke) of one domain; the whole CTA takes part.
 template <typename F, int TY>
-__device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char *smem_raw, int bx, int by, int bz) {
+__device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char *smem_raw, int bx, int by, int kb,
+                                              int ke) {
   using Sm = Smem<F, TY>;
   constexpr int TX = Tile<TY>::TX, NT = Tile<TY>::NT, PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
   constexpr int kPtSlots = Tile<TY>::kPtSlots;
@@ -223,8 +224,6 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   const int tid = threadIdx.x;
   const int tx = tid % TX, ty = tid / TX;
   const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
-  const int kb = bz * a.kchunk;
-  const int ke = min(Z, kb + a.kchunk);
 
   // ---- per-CTA grid tables ------------------------------------------------
   for (int p = tid; p < PX; p += NT) {
@@ -562,10 +561,25 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   }
 }
 
+// Persistent form with an even share per CTA: the ntiles * Z tile-levels,
+// tile-major, are cut into gridDim.x equal ranges, and CTA c walks range c
+// as one segment per tile it touches (a segment starting above level 0 pays
+// the restart of a k-chunk). With a whole number of tiles per SM rarely
+// available, equal shares keep every SM busy to the end of the launch.
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) pre_tile_kernel(PreArgs<F> a) {
+__global__ void __launch_bounds__(32 * TY, 2) pre_span_kernel(PreArgs<F> a, int ntx, int ntiles) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  pre_tile_body<F, TY>(a, smem_raw, blockIdx.x, blockIdx.y, blockIdx.z);
+  const int Z = a.L.Z;
+  const long long W = (long long)ntiles * Z;
+  long long p = W * blockIdx.x / gridDim.x;
+  const long long end = W * (blockIdx.x + 1) / gridDim.x;
+  while (p < end) {
+    const int t = (int)(p / Z), kb = (int)(p % Z);
+    const int ke = (int)min((long long)Z, end - (long long)t * Z);
+    pre_tile_body<F, TY>(a, smem_raw, t % ntx, t / ntx, kb, ke);
+    __syncthreads();  // shared memory is rebuilt by the next segment
+    p = (long long)t * Z + ke;
+  }
 }
 
 }  // namespace detail
