@@ -708,7 +708,7 @@ def run_gb300(args):
     pre_ms = float(stage_ms[:, 1].mean())
     pre_achieved = PRE_BYTES_PER_CELL * cells / (pre_ms / 1e3) / 1e9
     step_achieved = STEP_BYTES_PER_CELL * cells * args.steps / (ms / 1e3) / 1e9
-    traffic = _profiled_traffic("pre_tile_kernel_global1deg.md")
+    traffic = _profiled_traffic("pre_span_kernel_global1deg.md")
     base = cpu_baseline_sample(steps=1)
     line = {
         "metric": "isoneutral step cells/s (FP64)", "value": value, "unit": "cells/s", "n_gpus": world,
@@ -724,7 +724,7 @@ def run_gb300(args):
                      "unit": "GB/s", "frac": pre_achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                      "algorithmic_bytes_per_cell": PRE_BYTES_PER_CELL,
                      "step_achieved_gbs": step_achieved, "step_frac": step_achieved / peak,
-                     "fp64_pipe_pct_ncu": _profiled("pre_tile_kernel_global1deg.md", "fp64_pipe_pct"),
+                     "fp64_pipe_pct_ncu": _profiled("pre_span_kernel_global1deg.md", "fp64_pipe_pct"),
                      "fp64_roofline": _fp64_roofline(ms / args.steps),
                      "note": "FP64-pipe bound on GB300 (~1 TFLOP/s FP64); HBM fraction reported as asked"},
         "cpu_baseline": base,
