@@ -272,6 +272,16 @@ int vg_isoneutral_streamfunction_f64(const VgDomain *dom, const double *K_gm, co
                                      const double *Ai_nz, long long ai_stride_p, long long ai_stride_r,
                                      double *B1_gm, double *B2_gm, void *stream);
 
+/* Host-layout conversion for callers that exchange fields with the reference's
+ * (X, Y, Z) arrays in NumPy's default C order (z fastest): nfields (1..8)
+ * FP64 fields from src[n] to dst[n], element (i, j, k) at
+ * (i*Y + j)*Z + k on the reference side and i + j*pitch + k*plane on the
+ * canonical side. No reference counterpart (Veros keeps one layout). */
+int vg_layout_to_canonical_f64(const VgDomain *dom, int nfields, const double *const *src, double *const *dst,
+                               void *stream);
+int vg_layout_from_canonical_f64(const VgDomain *dom, int nfields, const double *const *src, double *const *dst,
+                                 void *stream);
+
 /* ---- Batched ensemble ------------------------------------------------------
  * One isoneutral step of many domains (uneven extents and kbot) with one
  * persistent launch per stage. No reference counterpart: Veros steps one

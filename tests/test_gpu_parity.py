@@ -425,14 +425,18 @@ def test_energy_branch_per_tracer_calls_match_fused_step(precision):
     assert np.any(a.download("P_diss_iso") != 0.0)
 
 
-def test_host_buffer_step_matches_device_step():
+@pytest.mark.parametrize("precision", ["f64", "f32split"])
+def test_host_buffer_step_matches_device_step(precision):
+    """step_host (reference-layout host buffers, layout conversion on the
+    device) gives the device step's fields bit for bit, on a domain whose X
+    and Z are not multiples of the 32-wide conversion tiles."""
     from veros_gb300 import synthetic
     from veros_gb300.state import DeviceState
     from veros_gb300.step import IsoneutralStepper
 
-    host = synthetic.small_linear_state(seed=2)
-    a = DeviceState.from_host(host)
-    b = DeviceState.from_host(host)
+    host = synthetic.make_state(45, 21, 13, seed=2, eq_of_state_type=3)
+    a = DeviceState.from_host(host, precision=precision)
+    b = DeviceState.from_host(host, precision=precision)
     IsoneutralStepper(a).step(1)
     X, Y, Z = b.X, b.Y, b.Z
     hT = torch.from_numpy(np.ascontiguousarray(host.temp[..., host.tau])).pin_memory()
@@ -441,7 +445,9 @@ def test_host_buffer_step_matches_device_step():
     IsoneutralStepper(b).step_host(hT, hS, *outs)
     v = a.variables
     assert np.array_equal(outs[0].numpy(), a.download("temp")[..., v.tau])
-    assert np.array_equal(outs[3].numpy(), a.download("dsalt_iso"))
+    assert np.array_equal(outs[1].numpy(), a.download("salt")[..., v.tau])
+    assert np.array_equal(outs[2].numpy(), a.download("dtemp_iso").astype(np.float64))
+    assert np.array_equal(outs[3].numpy(), a.download("dsalt_iso").astype(np.float64))
 
 
 def test_host_pipeline_matches_serial_host_steps():

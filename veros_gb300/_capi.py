@@ -94,6 +94,12 @@ SIGNATURES = {
     "vg_last_error": (ctypes.c_char_p, []),
     "vg_version": (ctypes.c_char_p, []),
     "vg_pack_masks": (ctypes.c_int, [ctypes.POINTER(VgDomain)] + [ctypes.c_void_p] * 5 + [ctypes.c_void_p]),
+    "vg_layout_to_canonical_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                                  ctypes.c_void_p]),
+    "vg_layout_from_canonical_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_int,
+                                                    ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                                    ctypes.c_void_p]),
     "vg_isoneutral_pre_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                              ctypes.POINTER(VgIsoSettings), ctypes.c_void_p, ctypes.c_void_p,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(VgTensorFields),

@@ -40,9 +40,84 @@ __global__ void pack_masks_kernel(Layout L, const uint8_t *__restrict__ mT, cons
                      (mW[o] ? VG_MASK_W : 0u));
 }
 
+// Fields between the reference's (X, Y, Z) C-order layout (z fastest, as a
+// NumPy array of the state) and the canonical layout (x fastest, pitch and
+// plane strides): per (j, field) a 32 x 32 tile of (i, k) goes through shared
+// memory, so that both the reads and the writes run along their fastest index.
+constexpr int kMaxLayoutFields = 8;
+struct LayoutFields {
+  const double *src[kMaxLayoutFields];
+  double *dst[kMaxLayoutFields];
+};
+
+template <bool TO_CANONICAL>
+__global__ void __launch_bounds__(256) layout_kernel(Layout L, LayoutFields f) {
+  __shared__ double t[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  const int j = blockIdx.z % L.Y, n = blockIdx.z / L.Y;
+  const int i0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const long long host_row = ((long long)j) * L.Z;  // + i * Y * Z + k
+  const long long hstride_i = (long long)L.Y * L.Z;
+  const double *src = f.src[n];
+  double *dst = f.dst[n];
+  if (TO_CANONICAL) {
+    for (int r = ty; r < 32; r += 8) {  // read along k
+      const int i = i0 + r, k = k0 + tx;
+      if (i < L.X && k < L.Z) t[r][tx] = src[i * hstride_i + host_row + k];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {  // write along i
+      const int i = i0 + tx, k = k0 + r;
+      if (i < L.X && k < L.Z) dst[L.at(i, j, k)] = t[tx][r];
+    }
+  } else {
+    for (int r = ty; r < 32; r += 8) {  // read along i
+      const int i = i0 + tx, k = k0 + r;
+      if (i < L.X && k < L.Z) t[tx][r] = src[L.at(i, j, k)];
+    }
+    __syncthreads();
+    for (int r = ty; r < 32; r += 8) {  // write along k
+      const int i = i0 + r, k = k0 + tx;
+      if (i < L.X && k < L.Z) dst[i * hstride_i + host_row + k] = t[r][tx];
+    }
+  }
+}
+
+template <bool TO_CANONICAL>
+int convert_layout(const VgDomain *dom, int nfields, const double *const *src, double *const *dst, void *stream,
+                   const char *name) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  if (nfields < 1 || nfields > kMaxLayoutFields)
+    return fail(VG_ERR_ARG, "%s: nfields=%d (1..%d)", name, nfields, kMaxLayoutFields);
+  if (!src || !dst) return fail(VG_ERR_ARG, "%s: NULL pointer", name);
+  LayoutFields f{};
+  for (int n = 0; n < nfields; ++n) {
+    if (!src[n] || !dst[n]) return fail(VG_ERR_ARG, "%s: NULL field pointer", name);
+    f.src[n] = src[n];
+    f.dst[n] = dst[n];
+  }
+  const Layout L = layout_of(dom);
+  if ((long long)L.Y * nfields > 65535) return fail(VG_ERR_SHAPE, "%s: Y * nfields above 65535", name);
+  dim3 grid((L.Z + 31) / 32, (L.X + 31) / 32, L.Y * nfields);
+  layout_kernel<TO_CANONICAL><<<grid, dim3(32, 8), 0, as_stream(stream)>>>(L, f);
+  return check_launch("layout_kernel");
+}
+
 }  // namespace vg
 
 using namespace vg;
+
+extern "C" int vg_layout_to_canonical_f64(const VgDomain *dom, int nfields, const double *const *src,
+                                          double *const *dst, void *stream) {
+  return convert_layout<true>(dom, nfields, src, dst, stream, "vg_layout_to_canonical_f64");
+}
+
+extern "C" int vg_layout_from_canonical_f64(const VgDomain *dom, int nfields, const double *const *src,
+                                            double *const *dst, void *stream) {
+  return convert_layout<false>(dom, nfields, src, dst, stream, "vg_layout_from_canonical_f64");
+}
 
 extern "C" const char *vg_last_error(void) { return g_last_error; }
 

@@ -9,6 +9,8 @@ time levels is a pointer permutation with period 3, so graphs are recorded
 for each of the three phases and replayed in turn).
 """
 
+import ctypes
+
 import torch
 
 from . import _capi
@@ -98,16 +100,14 @@ class IsoneutralStepper:
         shape = (self.dev.X, self.dev.Y, self.dev.Z)
         if staging is None:
             staging = torch.empty((6, *shape), dtype=torch.float64, device=self.dev.device)
+        stream = torch.cuda.current_stream(self.dev.device).cuda_stream
         staging[0].copy_(temp_tau, non_blocking=True)
         staging[1].copy_(salt_tau, non_blocking=True)
-        v.temp[..., v.tau].copy_(staging[0])
-        v.salt[..., v.tau].copy_(staging[1])
+        _to_canonical(self.dev, staging[:2], [v.temp[..., v.tau], v.salt[..., v.tau]], stream)
         self.step(1)
         new = v.tau  # the level just written, after the rotation
-        staging[2].copy_(v.temp[..., new])
-        staging[3].copy_(v.salt[..., new])
-        staging[4].copy_(v.dtemp_iso)
-        staging[5].copy_(v.dsalt_iso)
+        _from_canonical(self.dev, [v.temp[..., new], v.salt[..., new], v.dtemp_iso, v.dsalt_iso], staging[2:6],
+                        stream)
         out_temp.copy_(staging[2], non_blocking=True)
         out_salt.copy_(staging[3], non_blocking=True)
         out_dtemp.copy_(staging[4], non_blocking=True)
@@ -123,6 +123,43 @@ class IsoneutralStepper:
         kernel for temp and salt, one shared implicit solve and, with the
         energy branch, one energy kernel for both tracers."""
         return 1 + 1 + 1 + 1 + (1 if self.dev.settings.enable_conserve_energy else 0)
+
+
+def convert_layout(dev, to_canonical, src, dst, stream):
+    """FP64 fields between the reference's (X, Y, Z) C-order layout and the
+    state's canonical layout in one launch (vg_layout_*_canonical_f64); ``src``
+    and ``dst`` are equal-length lists of device tensors (views of the right
+    layout). Returns False, leaving the copies to the caller, when a field is
+    not FP64."""
+    if any(t.dtype != torch.float64 for t in list(src) + list(dst)):
+        return False
+    n = len(src)
+    ps = (ctypes.c_void_p * n)(*(t.data_ptr() for t in src))
+    pd = (ctypes.c_void_p * n)(*(t.data_ptr() for t in dst))
+    lib = _capi.load()
+    fn = lib.vg_layout_to_canonical_f64 if to_canonical else lib.vg_layout_from_canonical_f64
+    _capi.check(fn(dev.domain(), n, ps, pd, stream), "layout conversion")
+    return True
+
+
+def _convert(dev, to_canonical, src, dst, stream):
+    """The FP64 pairs in one conversion launch, the others (FP32 tendencies
+    of the split form) by torch copies."""
+    pairs = list(zip(src, dst))
+    f64 = [(a, b) for a, b in pairs if a.dtype == torch.float64 and b.dtype == torch.float64]
+    if f64:
+        convert_layout(dev, to_canonical, [a for a, _ in f64], [b for _, b in f64], stream)
+    for a, b in pairs:
+        if not (a.dtype == torch.float64 and b.dtype == torch.float64):
+            b.copy_(a)
+
+
+def _to_canonical(dev, stage, levels, stream):
+    _convert(dev, True, list(stage), levels, stream)
+
+
+def _from_canonical(dev, fields, stage, stream):
+    _convert(dev, False, fields, list(stage), stream)
 
 
 class HostPipeline:
@@ -167,18 +204,15 @@ class HostPipeline:
             uploaded = torch.cuda.Event()
             uploaded.record(self.h2d)
         compute.wait_event(uploaded)
-        v.temp[..., v.tau].copy_(stage_in[0])
-        v.salt[..., v.tau].copy_(stage_in[1])
+        _to_canonical(self.st.dev, stage_in, [v.temp[..., v.tau], v.salt[..., v.tau]], compute.cuda_stream)
         self.in_free[b] = torch.cuda.Event()
         self.in_free[b].record(compute)
         self.st.step(1)
         if self.out_free[b] is not None:
             compute.wait_event(self.out_free[b])
         new = v.tau
-        stage_out[0].copy_(v.temp[..., new])
-        stage_out[1].copy_(v.salt[..., new])
-        stage_out[2].copy_(v.dtemp_iso)
-        stage_out[3].copy_(v.dsalt_iso)
+        _from_canonical(self.st.dev, [v.temp[..., new], v.salt[..., new], v.dtemp_iso, v.dsalt_iso], stage_out,
+                        compute.cuda_stream)
         ready = torch.cuda.Event()
         ready.record(compute)
         with torch.cuda.stream(self.d2h):
