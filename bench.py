@@ -262,8 +262,8 @@ def _reference_kernel_ab_line():
     torch.cuda.set_device(device)
     try:
         return reference_kernel_ab(device)
-    except RuntimeError as e:
-        return {"unavailable": str(e).splitlines()[0]}
+    except (RuntimeError, OSError) as e:
+        return {"unavailable": (str(e).splitlines() or ["error"])[0]}
 
 
 def run_ensemble(device, steps=20):
