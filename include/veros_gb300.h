@@ -290,9 +290,10 @@ int vg_layout_from_canonical_f64(const VgDomain *dom, int nfields, const double 
  * rotations). The energy branch is not batched (VG_ERR_UNSUPPORTED). */
 typedef struct VgEnsembleTuning {
   int pre_rows;       /* columns per CTA / 32 of the slope kernel: 4 or 8 */
-  int pre_kchunk;     /* levels per CTA of the slope kernel, 0 = whole column */
+  int pre_kchunk;     /* levels per item of the slope kernel, 0 = whole column, -1 = equal shares of
+                         all members' tile-levels per resident CTA (static, no work counter) */
   int flux_rows;      /* columns per CTA / 32 of the flux kernel: 4 or 8 */
-  int flux_kchunk;    /* levels per CTA of the flux kernel, 0 = whole column */
+  int flux_kchunk;    /* levels per item of the flux kernel, as pre_kchunk */
   int solve_threads;  /* columns per CTA of the implicit solve: 32 or 64 */
 } VgEnsembleTuning;
 

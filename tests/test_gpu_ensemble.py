@@ -58,7 +58,10 @@ def test_every_tiling_gives_the_same_fields():
     ens = Ensemble(batched)
     tilings = [dict(pre_rows=4, pre_kchunk=16, flux_rows=4, flux_kchunk=0, solve_threads=32),
                dict(pre_rows=8, pre_kchunk=0, flux_rows=8, flux_kchunk=16, solve_threads=64),
-               dict(pre_rows=4, pre_kchunk=32, flux_rows=8, flux_kchunk=32, solve_threads=64)]
+               dict(pre_rows=4, pre_kchunk=32, flux_rows=8, flux_kchunk=32, solve_threads=64),
+               # equal shares of all members' tile-levels per resident CTA
+               dict(pre_rows=8, pre_kchunk=-1, flux_rows=8, flux_kchunk=-1, solve_threads=64),
+               dict(pre_rows=4, pre_kchunk=-1, flux_rows=4, flux_kchunk=-1, solve_threads=32)]
     for t in tilings:
         ens.tune(**t)
         ens.step(1)

@@ -23,7 +23,9 @@ using namespace detail;
 
 struct WorkItem {
   int member;
-  int a, b, c;  // tile x, tile y, k-chunk (pre/flux); column block (solve); level (prepare)
+  // tile x, tile y, k-chunk (pre/flux); with equal shares: tile, first level,
+  // end level (pre/flux); column block (solve); level (prepare)
+  int a, b, c;
 };
 
 template <typename F>
@@ -98,6 +100,23 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched(const MemberArgs<F> *_
   }
 }
 
+// Equal shares: CTA c runs the segments starts[c] .. starts[c+1]-1 (member,
+// tile, first level, end level) in order, with no work counter.
+template <typename F, int TY>
+__global__ void __launch_bounds__(32 * TY, 2) pre_batched_shares(const MemberArgs<F> *__restrict__ members,
+                                                                 const WorkItem *__restrict__ items,
+                                                                 const int *__restrict__ starts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ PreArgs<F> a;
+  for (int it = starts[blockIdx.x]; it < starts[blockIdx.x + 1]; ++it) {
+    const WorkItem w = items[it];
+    __syncthreads();  // the previous segment is done with `a` and shared memory
+    stage(&a, &members[w.member].pre);
+    const int nbx = (a.L.X - 3 + 31) / 32;
+    pre_tile_body<F, TY>(a, smem_raw, w.a % nbx, w.a / nbx, w.b, w.c);
+  }
+}
+
 template <typename F, int TY>
 __global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *__restrict__ members,
                                                            const WorkItem *__restrict__ items, int nitems,
@@ -111,6 +130,22 @@ __global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *
     if (threadIdx.x == 0) a[0].kchunk = a[1].kchunk = kchunk > 0 ? min(kchunk, a[0].L.Z) : a[0].L.Z;
     __syncthreads();
     flux_div_body<F, TY, 2>(a, zq_dzt, w.a, w.b, w.c * a[0].kchunk, min(a[0].L.Z, (w.c + 1) * a[0].kchunk));
+  }
+}
+
+template <typename F, int TY>
+__global__ void __launch_bounds__(32 * TY, 2) flux_batched_shares(const MemberArgs<F> *__restrict__ members,
+                                                                  const WorkItem *__restrict__ items,
+                                                                  const int *__restrict__ starts) {
+  extern __shared__ double zq_dzt[];
+  __shared__ DiffArgs<F> a[2];
+  for (int it = starts[blockIdx.x]; it < starts[blockIdx.x + 1]; ++it) {
+    const WorkItem w = items[it];
+    __syncthreads();
+    stage(&a[0], &members[w.member].dT);
+    stage(&a[1], &members[w.member].dS);
+    const int nbx = (a[0].L.X - 4 + 31) / 32;
+    flux_div_body<F, TY, 2>(a, zq_dzt, w.a % nbx, w.a / nbx, w.b, w.c);
   }
 }
 
@@ -146,6 +181,7 @@ struct Ensemble : EnsembleBase {
   const double **d_tau[3] = {nullptr, nullptr, nullptr};
   WorkItem *d_prep = nullptr, *d_pre = nullptr, *d_flux = nullptr, *d_solve = nullptr;
   int n_prep = 0, n_pre = 0, n_flux = 0, n_solve = 0;
+  int *d_pre_start = nullptr, *d_flux_start = nullptr;  // equal shares: first segment of each CTA
   int *d_counter = nullptr;
   Tuning tun{8, 0, 8, 0, 64};
   int grid_pre = 0, grid_flux = 0, grid_solve = 0, grid_prep = 0;
@@ -160,17 +196,50 @@ struct Ensemble : EnsembleBase {
     cudaFree(d_pre);
     cudaFree(d_flux);
     cudaFree(d_solve);
+    cudaFree(d_pre_start);
+    cudaFree(d_flux_start);
     cudaFree(d_counter);
   }
 
-  static int upload(WorkItem **dst, const std::vector<WorkItem> &v) {
+  template <typename T>
+  static int upload(T **dst, const std::vector<T> &v) {
     cudaFree(*dst);
     *dst = nullptr;
     if (v.empty()) return VG_OK;
-    cudaError_t e = cudaMalloc(dst, v.size() * sizeof(WorkItem));
-    if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(WorkItem), cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMalloc(dst, v.size() * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "ensemble work list: %s", cudaGetErrorString(e));
     return VG_OK;
+  }
+
+  // Equal shares: the members' tiles x levels, in list order, cut into ncta
+  // equal ranges of tile-levels; each range becomes the segments (tile, first
+  // level, end level) it covers. starts[c] is the first segment of CTA c.
+  static void equal_shares(const std::vector<int> &order, const std::vector<int> &tiles,
+                           const std::vector<Layout> &L, int ncta, std::vector<WorkItem> &seg,
+                           std::vector<int> &starts) {
+    long long W = 0;
+    for (int m : order) W += (long long)tiles[m] * L[m].Z;
+    starts.assign(ncta + 1, 0);
+    size_t oi = 0;
+    long long base = 0, p = 0;  // base: first tile-level of member order[oi]
+    for (int c = 0; c < ncta; ++c) {
+      starts[c] = (int)seg.size();
+      const long long end = W * (c + 1) / ncta;
+      while (p < end) {
+        while (p >= base + (long long)tiles[order[oi]] * L[order[oi]].Z) {
+          base += (long long)tiles[order[oi]] * L[order[oi]].Z;
+          ++oi;
+        }
+        const int m = order[oi], Z = L[m].Z;
+        const long long q = p - base;
+        const int t = (int)(q / Z), kb = (int)(q % Z);
+        const int ke = (int)std::min<long long>(Z, end - base - (long long)t * Z);
+        seg.push_back({m, t, kb, ke});
+        p = base + (long long)t * Z + ke;
+      }
+    }
+    starts[ncta] = (int)seg.size();
   }
 
   // Work lists: largest members first, so the persistent CTAs finish together.
@@ -181,27 +250,36 @@ struct Ensemble : EnsembleBase {
       return (long long)layouts[x].X * layouts[x].Y * layouts[x].Z > (long long)layouts[y].X * layouts[y].Y * layouts[y].Z;
     });
     std::vector<WorkItem> pre, flux, solve, prep;
+    std::vector<int> pre_tiles(n), flux_tiles(n);
     for (int m : order) {
       const Layout &L = layouts[m];
       const int kc_pre = tun.pre_kchunk > 0 ? std::min(tun.pre_kchunk, L.Z) : L.Z;
       const int kc_flux = tun.flux_kchunk > 0 ? std::min(tun.flux_kchunk, L.Z) : L.Z;
       const int pbx = (L.X - 3 + 31) / 32, pby = (L.Y - 3 + tun.pre_rows - 1) / tun.pre_rows;
       const int pbz = (L.Z + kc_pre - 1) / kc_pre;
-      for (int bz = 0; bz < pbz; ++bz)
-        for (int by = 0; by < pby; ++by)
-          for (int bx = 0; bx < pbx; ++bx) pre.push_back({m, bx, by, bz});
+      pre_tiles[m] = pbx * pby;
+      if (tun.pre_kchunk >= 0)
+        for (int bz = 0; bz < pbz; ++bz)
+          for (int by = 0; by < pby; ++by)
+            for (int bx = 0; bx < pbx; ++bx) pre.push_back({m, bx, by, bz});
       const int fbx = (L.X - 4 + 31) / 32, fby = (L.Y - 4 + tun.flux_rows - 1) / tun.flux_rows;
       const int fbz = (L.Z + kc_flux - 1) / kc_flux;
-      for (int bz = 0; bz < fbz; ++bz)  // temp and salt of a tile in one item
-        for (int by = 0; by < fby; ++by)
-          for (int bx = 0; bx < fbx; ++bx) flux.push_back({m, bx, by, bz});
+      flux_tiles[m] = fbx * fby;
+      if (tun.flux_kchunk >= 0)
+        for (int bz = 0; bz < fbz; ++bz)  // temp and salt of a tile in one item
+          for (int by = 0; by < fby; ++by)
+            for (int bx = 0; bx < fbx; ++bx) flux.push_back({m, bx, by, bz});
       const int ncols = (L.X - 4) * (L.Y - 4);
       for (int cb = 0; cb < (ncols + tun.solve_threads - 1) / tun.solve_threads; ++cb) solve.push_back({m, cb, 0, 0});
       for (int k = 0; k < L.Z; ++k) prep.push_back({m, 0, 0, k});
     }
+    std::vector<int> pre_start, flux_start;
+    if (tun.pre_kchunk < 0) equal_shares(order, pre_tiles, layouts, grid_pre, pre, pre_start);
+    if (tun.flux_kchunk < 0) equal_shares(order, flux_tiles, layouts, grid_flux, flux, flux_start);
     int st;
     if ((st = upload(&d_pre, pre)) || (st = upload(&d_flux, flux)) || (st = upload(&d_solve, solve)) ||
-        (st = upload(&d_prep, prep)))
+        (st = upload(&d_prep, prep)) || (st = upload(&d_pre_start, pre_start)) ||
+        (st = upload(&d_flux_start, flux_start)))
       return st;
     n_pre = (int)pre.size();
     n_flux = (int)flux.size();
@@ -227,26 +305,31 @@ struct Ensemble : EnsembleBase {
 
   int tune(const Tuning &t) override {
     if ((t.pre_rows != 4 && t.pre_rows != 8) || (t.flux_rows != 4 && t.flux_rows != 8) ||
-        (t.solve_threads != 32 && t.solve_threads != 64) || t.pre_kchunk < 0 || t.flux_kchunk < 0)
-      return fail(VG_ERR_ARG, "tuning: rows must be 4 or 8, solve_threads 32 or 64, k-chunks >= 0");
+        (t.solve_threads != 32 && t.solve_threads != 64) || t.pre_kchunk < -1 || t.flux_kchunk < -1)
+      return fail(VG_ERR_ARG, "tuning: rows must be 4 or 8, solve_threads 32 or 64, k-chunks >= -1");
     tun = t;
-    int st = build_lists();
-    if (st) return st;
+    int st;
     smem_pre = t.pre_rows == 4 ? pre_smem_bytes<F, 4>(maxZ) : pre_smem_bytes<F, 8>(maxZ);
     smem_flux = 2 * (size_t)maxZ * sizeof(double);
     smem_solve = (2 * (size_t)maxZ + 3 * (size_t)maxZ * t.solve_threads) * sizeof(double);
+    const bool ps = t.pre_kchunk < 0, fs = t.flux_kchunk < 0;
     if (t.pre_rows == 4)
-      st = occupancy_grid(pre_batched<F, 4>, 128, smem_pre, grid_pre);
+      st = ps ? occupancy_grid(pre_batched_shares<F, 4>, 128, smem_pre, grid_pre)
+              : occupancy_grid(pre_batched<F, 4>, 128, smem_pre, grid_pre);
     else
-      st = occupancy_grid(pre_batched<F, 8>, 256, smem_pre, grid_pre);
+      st = ps ? occupancy_grid(pre_batched_shares<F, 8>, 256, smem_pre, grid_pre)
+              : occupancy_grid(pre_batched<F, 8>, 256, smem_pre, grid_pre);
     if (st) return st;
     if (t.flux_rows == 4)
-      st = occupancy_grid(flux_batched<F, 4>, 128, smem_flux, grid_flux);
+      st = fs ? occupancy_grid(flux_batched_shares<F, 4>, 128, smem_flux, grid_flux)
+              : occupancy_grid(flux_batched<F, 4>, 128, smem_flux, grid_flux);
     else
-      st = occupancy_grid(flux_batched<F, 8>, 256, smem_flux, grid_flux);
+      st = fs ? occupancy_grid(flux_batched_shares<F, 8>, 256, smem_flux, grid_flux)
+              : occupancy_grid(flux_batched<F, 8>, 256, smem_flux, grid_flux);
     if (st) return st;
     if ((st = occupancy_grid(implicit_batched<F>, t.solve_threads, smem_solve, grid_solve))) return st;
-    return occupancy_grid(prepare_batched<F>, 256, 0, grid_prep);
+    if ((st = occupancy_grid(prepare_batched<F>, 256, 0, grid_prep))) return st;
+    return build_lists();  // the equal shares are cut for the CTA counts above
   }
 
   int step(int phase, cudaStream_t s) override {
@@ -257,19 +340,29 @@ struct Ensemble : EnsembleBase {
     int st;
     prepare_batched<F><<<std::min(grid_prep, n_prep), 256, 0, s>>>(args, d_tau[phase], d_prep, n_prep, d_counter);
     if ((st = check_launch("prepare_batched"))) return st;
-    if (tun.pre_rows == 4)
-      pre_batched<F, 4><<<std::min(grid_pre, n_pre), 128, smem_pre, s>>>(args, d_pre, n_pre, d_counter + 1,
-                                                                         tun.pre_kchunk);
-    else
-      pre_batched<F, 8><<<std::min(grid_pre, n_pre), 256, smem_pre, s>>>(args, d_pre, n_pre, d_counter + 1,
-                                                                         tun.pre_kchunk);
+    // equal shares: exactly the CTAs the shares were cut for
+    const int gp = std::min(grid_pre, n_pre), gf = std::min(grid_flux, n_flux);
+    if (d_pre_start) {
+      if (tun.pre_rows == 4)
+        pre_batched_shares<F, 4><<<grid_pre, 128, smem_pre, s>>>(args, d_pre, d_pre_start);
+      else
+        pre_batched_shares<F, 8><<<grid_pre, 256, smem_pre, s>>>(args, d_pre, d_pre_start);
+    } else if (tun.pre_rows == 4) {
+      pre_batched<F, 4><<<gp, 128, smem_pre, s>>>(args, d_pre, n_pre, d_counter + 1, tun.pre_kchunk);
+    } else {
+      pre_batched<F, 8><<<gp, 256, smem_pre, s>>>(args, d_pre, n_pre, d_counter + 1, tun.pre_kchunk);
+    }
     if ((st = check_launch("pre_batched"))) return st;
-    if (tun.flux_rows == 4)
-      flux_batched<F, 4><<<std::min(grid_flux, n_flux), 128, smem_flux, s>>>(args, d_flux, n_flux, d_counter + 2,
-                                                                             tun.flux_kchunk);
-    else
-      flux_batched<F, 8><<<std::min(grid_flux, n_flux), 256, smem_flux, s>>>(args, d_flux, n_flux, d_counter + 2,
-                                                                             tun.flux_kchunk);
+    if (d_flux_start) {
+      if (tun.flux_rows == 4)
+        flux_batched_shares<F, 4><<<grid_flux, 128, smem_flux, s>>>(args, d_flux, d_flux_start);
+      else
+        flux_batched_shares<F, 8><<<grid_flux, 256, smem_flux, s>>>(args, d_flux, d_flux_start);
+    } else if (tun.flux_rows == 4) {
+      flux_batched<F, 4><<<gf, 128, smem_flux, s>>>(args, d_flux, n_flux, d_counter + 2, tun.flux_kchunk);
+    } else {
+      flux_batched<F, 8><<<gf, 256, smem_flux, s>>>(args, d_flux, n_flux, d_counter + 2, tun.flux_kchunk);
+    }
     if ((st = check_launch("flux_batched"))) return st;
     implicit_batched<F><<<std::min(grid_solve, n_solve), tun.solve_threads, smem_solve, s>>>(args, d_solve, n_solve,
                                                                                            d_counter + 3);

@@ -141,7 +141,7 @@ class Ensemble:
     def signature(self):
         return (self.precision, tuple((s.X, s.Y, s.Z) for s in self.states))
 
-    def autotune(self, steps=2, kchunks=(0, 32, 16)):
+    def autotune(self, steps=2, kchunks=(0, 32, 16, -1)):
         """Pick the tiling by timing candidates on this ensemble; advances the
         members by the steps it times. Returns ``(tuning, {candidate: ms})``."""
         sig = self.signature()
