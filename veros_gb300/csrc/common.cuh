@@ -26,17 +26,23 @@ inline int check_launch(const char *what) {
 
 int validate_domain(const VgDomain *dom);
 
-// CTAs for a span kernel (an even share of W work units per CTA): every CTA
-// the device holds at once, but at least min_units units each. 0 on error.
+// CTAs for a span kernel over ntiles x Z tile-levels (an even share per
+// CTA). With at least four tiles per resident CTA slot, one CTA per tile: the
+// hardware then runs neighbouring tiles side by side (their halo reads meet
+// in L2) and its tail is short against the many waves. Otherwise every CTA
+// the device holds at once, each with an equal share (at least min_levels
+// tile-levels), so that no SM idles through a partial last wave. 0 on error.
 template <typename K>
-inline int span_ctas(K kernel, int threads, size_t smem, long long W, int min_units) {
+inline int span_ctas(K kernel, int threads, size_t smem, int ntiles, int Z, int min_levels) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1)
     return 0;
-  const long long by_units = (W + min_units - 1) / min_units;
-  return (int)std::max(1LL, std::min((long long)sms * per, by_units));
+  const long long slots = (long long)sms * per;
+  if (ntiles >= 4 * slots) return ntiles;
+  const long long by_units = ((long long)ntiles * Z + min_levels - 1) / min_levels;
+  return (int)std::max(1LL, std::min(slots, by_units));
 }
 
 struct Layout {

@@ -13,15 +13,14 @@ namespace vg {
 namespace {
 
 // NTR = 2: temp and salt in one pass over the tensor (b: salt); NTR = 1: a alone
-// Tiles of 32 x 8 columns; every resident CTA takes an equal share of the
-// tile-levels (flux_span_kernel), at least 8 levels each.
+// Tiles of 32 x 8 columns (flux_span_kernel): one CTA per tile on large
+// domains, else every resident CTA with an equal share of the tile-levels.
 template <typename F, int NTR>
 int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
   constexpr int TY = 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
   const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
-  const long long W = (long long)nbx * nby * a.L.Z;
-  const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, W, 8);
+  const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, nbx * nby, a.L.Z, 8);
   if (nc < 1) return fail(VG_ERR_LAUNCH, "flux_span_kernel: occupancy query failed");
   a.kchunk = b.kchunk = a.L.Z;
   flux_span_kernel<F, TY, NTR><<<nc, TX * TY, smem, s>>>(a, b, nbx, nbx * nby);

@@ -44,15 +44,15 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   a.sr = out->ai_stride_r;
   a.slopes = slopes;
   a.slope_field = (long long)a.L.plane * a.L.Z;
-  // tiles of 32 x 8 columns; every resident CTA (two per SM) takes an equal
-  // share of the tile-levels, at least 8 levels each
+  // tiles of 32 x 8 columns; one CTA per tile on large domains, else every
+  // resident CTA (two per SM) with an equal share of the tile-levels
   constexpr int TY = 8, TX = 32;
   const int nbx = (a.L.X - 3 + TX - 1) / TX, nby = (a.L.Y - 3 + TY - 1) / TY;
   const size_t smem = pre_smem_bytes<F, TY>(a.L.Z);
   cudaError_t e =
       cudaFuncSetAttribute(pre_span_kernel<F, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_span_kernel smem %zu: %s", smem, cudaGetErrorString(e));
-  const int nc = span_ctas(pre_span_kernel<F, TY>, TX * TY, smem, (long long)nbx * nby * a.L.Z, 8);
+  const int nc = span_ctas(pre_span_kernel<F, TY>, TX * TY, smem, nbx * nby, a.L.Z, 8);
   if (nc < 1) return fail(VG_ERR_LAUNCH, "pre_span_kernel: occupancy query failed");
   a.kchunk = a.L.Z;
   pre_span_kernel<F, TY><<<nc, TX * TY, smem, as_stream(stream)>>>(a, nbx, nbx * nby);
