@@ -456,7 +456,7 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
 
   // Loads run PF levels ahead of the serial chain (software pipelining): the
   // chain itself only waits for FP64 latency, not for global memory.
-  constexpr int PF = 4;
+  constexpr int PF = 8;
   double qK[PF], qT[PF][NRHS];
 #pragma unroll
   for (int u = 0; u < PF; ++u) {

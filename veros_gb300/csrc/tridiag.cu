@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
 
   // Loads run PF levels ahead of the elimination's serial chain (software
   // pipelining); the arithmetic is dgtsv's, operation for operation.
-  constexpr int PF = 4;
+  constexpr int PF = 8;
   double qa[PF], qb[PF], qc[PF], qd[PF];
 #pragma unroll
   for (int u = 0; u < PF; ++u) {

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kVmixThreads) vertmix_kernel(VmixArgs a) {
   }
   if (ks < 0 || ks >= Z) return;
 
-  constexpr int PF = 4;
+  constexpr int PF = 8;
   double qK[PF], qT[PF][2];
 #pragma unroll
   for (int u = 0; u < PF; ++u) {
