@@ -445,7 +445,7 @@ __device__ __forceinline__ F cvt_f(double x) {
 
 template <typename F, int NRHS>
 __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const DiffArgs<F> &b2, const double *dtdzw,
-                                                const double *inv_dzt, double *cps, double *dps, int t, int nb,
+                                                const double *inv_dzt, double *cps, int cs, double *dps, int ds,
                                                 int i, int j, int ks) {
   const Layout &L = a.L;
   const int Z = L.Z;
@@ -494,11 +494,11 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
         const double ck = pm(-delta, idzt);                                      // c_tri (0 on the top level)
         const double den = recip_newton(pfma(-ak, cp, bk));  // pivot >= the diagonal's excess over 1
         cp = pm(ck, den);
-        cps[(size_t)k * nb + t] = cp;
+        cps[(size_t)k * cs] = cp;
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
           dp[r] = pm(pfma(-ak, dp[r], tr1[r]), den);
-          dps[((size_t)r * Z + k) * nb + t] = dp[r];
+          dps[((size_t)r * Z + k) * ds] = dp[r];
         }
         delta_prev = delta;
       }
@@ -528,10 +528,10 @@ __device__ __forceinline__ void implicit_column(const DiffArgs<F> &a, const Diff
       const int k = Z - 1 - (m0 + u);
       if (k >= ks) {
         const long long o = base + (long long)k * L.plane;
-        const double c = cps[(size_t)k * nb + t];
+        const double c = cps[(size_t)k * cs];
 #pragma unroll
         for (int r = 0; r < NRHS; ++r) {
-          x[r] = pfma(-c, x[r], dps[((size_t)r * Z + k) * nb + t]);
+          x[r] = pfma(-c, x[r], dps[((size_t)r * Z + k) * ds]);
           trp[r][o] = x[r];
           dtr[r][o] = cvt_f<F>(pfma(x[r] - t1[u][r], inv_dt, d1[u][r]));  // diffusion.py:204
         }
@@ -564,7 +564,7 @@ __device__ __forceinline__ void implicit_body(const DiffArgs<F> &a, const DiffAr
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
   const int ks = (unsigned)col < (unsigned)ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
-  if (ks >= 0 && ks < Z) implicit_column<F, NRHS>(a, b2, dtdzw, inv_dzt, cps, dps, t, nb, i, j, ks);
+  if (ks >= 0 && ks < Z) implicit_column<F, NRHS>(a, b2, dtdzw, inv_dzt, cps + t, nb, dps + t, nb, i, j, ks);
   __syncthreads();  // dtdzw is refilled by the next block of columns a persistent CTA takes
 }
 
@@ -572,6 +572,36 @@ template <typename F, int NRHS>
 __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs<F> a, DiffArgs<F> b2) {
   extern __shared__ double smem[];
   implicit_body<F, NRHS>(a, b2, smem, blockIdx.x);
+}
+
+// Temp and salt of a column on two neighbouring threads (lane 2c: a, lane
+// 2c+1: b2): both form the shared factorisation (they write the same c'
+// values to the column's slot) and each eliminates its own tracer, so twice
+// as many warps hide the recurrence's latency for the same shared memory
+// per column. The arithmetic of each tracer is that of implicit_kernel<F, 2>.
+template <typename F>
+__global__ void __launch_bounds__(128) implicit_pair_kernel(DiffArgs<F> a, DiffArgs<F> b2) {
+  extern __shared__ double smem[];
+  const Layout &L = a.L;
+  const int Z = L.Z;
+  const int ncols_x = L.X - 4, ncols = ncols_x * (L.Y - 4);
+  const int t = threadIdx.x, nb = blockDim.x, nc = nb / 2, c = t >> 1, r = t & 1;
+  double *dtdzw = smem;
+  double *inv_dzt = smem + Z;
+  double *cps = smem + 2 * Z;             // [k][column]
+  double *dps = cps + (size_t)Z * nc;     // [k][thread]
+  for (int k = t; k < Z; k += nb) {
+    dtdzw[k] = rdiv(a.dt, a.g.dzw[k]);
+    inv_dzt[k] = 1.0 / a.g.dzt[k];
+  }
+  __syncthreads();
+  const int slot = blockIdx.x * nc + c;
+  const int col = a.col_order ? (slot < ncols ? __ldg(a.col_order + slot) : ncols) : slot;
+  const int i = 2 + col % ncols_x;
+  const int j = 2 + col / ncols_x;
+  const int ks = (unsigned)col < (unsigned)ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
+  const DiffArgs<F> &own = r ? b2 : a;
+  if (ks >= 0 && ks < Z) implicit_column<F, 1>(own, own, dtdzw, inv_dzt, cps + c, nc, dps + t, nb, i, j, ks);
 }
 
 // Energy branch (veros/core/isoneutral/diffusion.py:234-281 with

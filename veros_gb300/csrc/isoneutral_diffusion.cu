@@ -30,6 +30,18 @@ int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
 template <typename F, int NRHS>
 int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) {
   const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
+  if (NRHS == 2) {  // temp and salt of a column on two threads, 64 columns per CTA
+    const int nb = 128, nc = 64;
+    const size_t smem = (2 * (size_t)a.L.Z + (size_t)a.L.Z * (nc + nb)) * sizeof(double);
+    if (smem > 48 * 1024) {
+      cudaError_t e =
+          cudaFuncSetAttribute(implicit_pair_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess)
+        return fail(VG_ERR_LAUNCH, "implicit_pair_kernel smem %zu: %s", smem, cudaGetErrorString(e));
+    }
+    implicit_pair_kernel<F><<<(ncols + nc - 1) / nc, nb, smem, s>>>(a, b);
+    return check_launch("implicit_pair_kernel");
+  }
   const int nb = 64;
   const size_t smem = (2 * (size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
   if (smem > 48 * 1024) {
