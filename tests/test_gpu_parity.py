@@ -400,6 +400,35 @@ def test_drop_in_signatures_on_device_state():
     _check_state(dev, vs, ("temp", "salt", "dtemp_iso", "dsalt_iso", "P_diss_iso", "K_33"), host.settings, vs.tau)
 
 
+def test_deep_columns_step_and_drop_in_vs_oracle():
+    """200 levels (the implicit solves then take fewer columns per CTA to fit
+    their shared memory): one fused step and the per-tracer drop-in calls
+    against the oracle."""
+    import veros_gb300 as vg
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+
+    host = synthetic.make_state(24, 20, 200, seed=4, eq_of_state_type=3, dz_bottom=100.0)
+    _teacher_forced_rollout(host, 1)
+    dev = DeviceState.from_host(host)
+    v = dev.variables
+    v.temp[..., v.taup1] = v.temp[..., v.tau] * v.maskT
+    v.salt[..., v.taup1] = v.salt[..., v.tau] * v.maskT
+    v.update(vg.isoneutral_diffusion_pre(dev))
+    vg.isoneutral_diffusion(dev, v.temp, True)
+    vg.isoneutral_diffusion(dev, v.salt, False)
+    torch.cuda.synchronize()
+    vs = orc.OracleState({k: a.copy() for k, a in host.arrays.items()})
+    for name in ("temp", "salt"):
+        tr = getattr(vs, name)
+        tr[..., vs.taup1] = tr[..., vs.tau] * vs.maskT
+    vs.__dict__.update(orc.isoneutral_diffusion_pre(vs, host.settings))
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, host.settings, True))
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, host.settings, False))
+    _check_state(dev, vs, ("temp", "salt", "dtemp_iso", "dsalt_iso", "K_33"), host.settings, vs.tau)
+
+
 @pytest.mark.parametrize("precision", ["f64", "f32split"])
 def test_energy_branch_per_tracer_calls_match_fused_step(precision):
     """P_diss_iso from the per-tracer drop-in calls (one energy launch each)

@@ -30,9 +30,14 @@ int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
 template <typename F, int NRHS>
 int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) {
   const int ncols_x = a.L.X - 4, ncols = ncols_x * (a.L.Y - 4);
-  if (NRHS == 2) {  // temp and salt of a column on two threads, 64 columns per CTA
-    const int nb = 128, nc = 64;
-    const size_t smem = (2 * (size_t)a.L.Z + (size_t)a.L.Z * (nc + nb)) * sizeof(double);
+  // shared memory per CTA: the two per-level tables plus c' per column and d'
+  // per thread; deep columns take fewer columns per CTA
+  constexpr size_t kMaxSmem = 200 * 1024;
+  if (NRHS == 2) {  // temp and salt of a column on two threads, up to 64 columns per CTA
+    int nc = 64;
+    while (nc > 8 && (2 + 3 * (size_t)nc) * a.L.Z * sizeof(double) > kMaxSmem) nc /= 2;
+    const int nb = 2 * nc;
+    const size_t smem = (2 + 3 * (size_t)nc) * a.L.Z * sizeof(double);
     if (smem > 48 * 1024) {
       cudaError_t e =
           cudaFuncSetAttribute(implicit_pair_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -42,7 +47,8 @@ int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) 
     implicit_pair_kernel<F><<<(ncols + nc - 1) / nc, nb, smem, s>>>(a, b);
     return check_launch("implicit_pair_kernel");
   }
-  const int nb = 64;
+  int nb = 64;
+  while (nb > 8 && (2 + (1 + NRHS) * (size_t)nb) * a.L.Z * sizeof(double) > kMaxSmem) nb /= 2;
   const size_t smem = (2 * (size_t)a.L.Z + (1 + NRHS) * (size_t)a.L.Z * nb) * sizeof(double);
   if (smem > 48 * 1024) {
     cudaError_t e =
