@@ -305,14 +305,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           rT = to_F<F>(Tc) * to_F<F>(eos_c1) + to_F<F>(zeos[lev]);  // (isoneutral.py:40, get_rho.py:93-112)
           rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
         }
+        // horizontal differences; their metric factors are applied in F below
         if ((mk & VG_MASK_U) && i < L.X - 1) {
-          const double f = sm.inv_dxu_cost[p];
-          dTx = (__ldg(a.T + o + 1) - Tc) * f;
-          dSx = (__ldg(a.S + o + 1) - Sc) * f;
+          dTx = __ldg(a.T + o + 1) - Tc;
+          dSx = __ldg(a.S + o + 1) - Sc;
         }
         if ((mk & VG_MASK_V) && j < L.Y - 1) {
-          dTy = (__ldg(a.T + o + L.pitch) - Tc) * sm.inv_dyu[pj];
-          dSy = (__ldg(a.S + o + L.pitch) - Sc) * sm.inv_dyu[pj];
+          dTy = __ldg(a.T + o + L.pitch) - Tc;
+          dSy = __ldg(a.S + o + L.pitch) - Sc;
         }
         if ((mk & VG_MASK_W) && lev < Z - 1) {
           dTz = (__ldg(a.T + o + L.plane) - Tc) * zinv_dzw[lev];
@@ -328,10 +328,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         F(*q)[NP] = sm.q[buf];
         q[Q_RT][p] = rT;
         q[Q_RS][p] = rS;
-        q[Q_TX][p] = to_F<F>(dTx);
-        q[Q_SX][p] = to_F<F>(dSx);
-        q[Q_TY][p] = to_F<F>(dTy);
-        q[Q_SY][p] = to_F<F>(dSy);
+        // face gradients (isoneutral.py:64-95): the FP64 difference times
+        // 1/(dxu cost) or 1/dyu, the product in F (FP32 in the split form)
+        const F fx = to_F<F>(sm.inv_dxu_cost[p]), fy = to_F<F>(sm.inv_dyu[pj]);
+        q[Q_TX][p] = to_F<F>(dTx) * fx;
+        q[Q_SX][p] = to_F<F>(dSx) * fx;
+        q[Q_TY][p] = to_F<F>(dTy) * fy;
+        q[Q_SY][p] = to_F<F>(dSy) * fy;
         q[Q_R0][p] = to_F<F>(recip_neg(clamp_eps(G0)));
         q[Q_R1][p] = to_F<F>(recip_neg(clamp_eps(G1)));
         sm.qm[buf][p] = (uint8_t)(mk | (carryW[s] ? kMaskWBelow : 0u));
