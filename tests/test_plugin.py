@@ -1,0 +1,53 @@
+"""plugin.install() against stand-in Veros modules (no GPU, no Veros import):
+every attribute the reference's callers look up is rebound to this library's
+drop-in and uninstall() restores the originals."""
+
+import sys
+import types
+
+import pytest
+
+
+@pytest.fixture
+def fake_veros(monkeypatch):
+    from veros_gb300 import plugin
+
+    originals = {}
+    for modname, attr, _ in plugin._TARGETS:
+        parts = modname.split(".")
+        for n in range(1, len(parts) + 1):
+            name = ".".join(parts[:n])
+            if name not in sys.modules or not getattr(sys.modules[name], "_vg_fake", False):
+                mod = types.ModuleType(name)
+                mod._vg_fake = True
+                monkeypatch.setitem(sys.modules, name, mod)
+        mod = sys.modules[modname]
+        sentinel = object()
+        setattr(mod, attr, sentinel)
+        originals[(modname, attr)] = sentinel
+    return originals
+
+
+def test_install_rebinds_every_call_site_and_uninstall_restores(fake_veros):
+    from veros_gb300 import plugin
+
+    handle = plugin.install()
+    for modname, attr, fn in plugin._TARGETS:
+        assert getattr(sys.modules[modname], attr) is fn, (modname, attr)
+    handle.uninstall()
+    for (modname, attr), orig in fake_veros.items():
+        assert getattr(sys.modules[modname], attr) is orig, (modname, attr)
+
+
+def test_the_reference_call_sites_are_covered():
+    """The names the reference's callers resolve at call time
+    (veros/core/thermodynamics.py:430-432, veros/core/utilities.py:4)."""
+    from veros_gb300 import plugin
+
+    targets = {(m, a) for m, a, _ in plugin._TARGETS}
+    for need in (("veros.core.isoneutral", "isoneutral_diffusion_pre"),
+                 ("veros.core.isoneutral", "isoneutral_diffusion"),
+                 ("veros.core.utilities", "solve_implicit"),
+                 ("veros.core.utilities", "solve_tridiagonal"),
+                 ("veros.core.operators", "solve_tridiagonal")):
+        assert need in targets, need
