@@ -51,3 +51,30 @@ def test_the_reference_call_sites_are_covered():
                  ("veros.core.utilities", "solve_tridiagonal"),
                  ("veros.core.operators", "solve_tridiagonal")):
         assert need in targets, need
+
+
+def test_install_on_the_reference_modules_when_present():
+    """With the reference checkout at hand (not on GPU machines), every target
+    module and attribute exists in the real Veros and is rebound."""
+    import importlib
+    import os
+
+    ref = os.environ.get("REF_ROOT", os.path.join(os.sep, "root", "reference"))
+    if not os.path.isdir(os.path.join(ref, "veros")):
+        pytest.skip("reference checkout not present")
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    try:
+        import make_golden
+    finally:
+        sys.path.pop(0)
+    make_golden._import_reference(ref)
+    from veros_gb300 import plugin
+
+    for modname, attr, _ in plugin._TARGETS:
+        assert hasattr(importlib.import_module(modname), attr), (modname, attr)
+    handle = plugin.install()
+    try:
+        for modname, attr, fn in plugin._TARGETS:
+            assert getattr(importlib.import_module(modname), attr) is fn
+    finally:
+        handle.uninstall()
