@@ -225,17 +225,22 @@ def make_grid_case():
 
 
 def main():
+    """make_golden.py [reference_root] [case ...]: writes the named cases (all by default)."""
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    only = set(sys.argv[2:])
     _import_reference(ref)
-    cases = {
-        "iso_random_energy": make_random_case(12, 10, 8, True),
-        "iso_random_noenergy": make_random_case(10, 9, 7, False),
-        "iso_synth_eq1": make_synth_case(0, 1, False, None),
-        "iso_synth_eq3": make_synth_case(1, 3, True, 0.3),
-        "tridiag": make_tridiag_case(),
-        "vertmix_random": make_vertmix_case(12, 10, 9, 17),
-        "grid_topo": make_grid_case(),
+    makers = {
+        "iso_random_energy": lambda: make_random_case(12, 10, 8, True),
+        "iso_random_noenergy": lambda: make_random_case(10, 9, 7, False),
+        "iso_synth_eq1": lambda: make_synth_case(0, 1, False, None),
+        "iso_synth_eq2": lambda: make_synth_case(2, 2, True, None),
+        "iso_synth_eq3": lambda: make_synth_case(1, 3, True, 0.3),
+        "iso_synth_eq4": lambda: make_synth_case(3, 4, False, 0.3),
+        "tridiag": make_tridiag_case,
+        "vertmix_random": lambda: make_vertmix_case(12, 10, 9, 17),
+        "grid_topo": make_grid_case,
     }
+    cases = {name: make() for name, make in makers.items() if not only or name in only}
     for name, blob in cases.items():
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **blob)

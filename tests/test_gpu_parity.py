@@ -59,7 +59,8 @@ def _written(name, shape):
     return w
 
 
-@pytest.mark.parametrize("case", ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq3"])
+@pytest.mark.parametrize("case", ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq2",
+                                  "iso_synth_eq3", "iso_synth_eq4"])
 def test_pre_vs_reference_golden(case):
     from veros_gb300.isoneutral import run_pre
 
@@ -74,7 +75,8 @@ def test_pre_vs_reference_golden(case):
         assert np.array_equal(got[untouched], before[untouched]), f"{name}: untouched cells changed"
 
 
-@pytest.mark.parametrize("case", ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq3"])
+@pytest.mark.parametrize("case", ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq2",
+                                  "iso_synth_eq3", "iso_synth_eq4"])
 def test_diffusion_chain_vs_reference_golden(case):
     from veros_gb300.isoneutral import run_diffusion, run_pre
 

@@ -6,7 +6,8 @@ import pytest
 from conftest import load_golden
 from oracle import isoneutral_oracle as orc
 
-ISO_CASES = ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq3"]
+ISO_CASES = ["iso_random_energy", "iso_random_noenergy", "iso_synth_eq1", "iso_synth_eq2", "iso_synth_eq3",
+             "iso_synth_eq4"]
 
 
 def _state_and_settings(g):
