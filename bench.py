@@ -423,6 +423,54 @@ def run_quarter_degree(device, steps=100):
     return out
 
 
+def run_dropin_host(device, steps=3, warmup=1):
+    """The drop-in as a plugin-installed NumPy Veros calls it: the tracer part
+    of thermodynamics (veros/core/thermodynamics.py:425-432: zeroed
+    tendencies, isoneutral_diffusion_pre, isoneutral_diffusion of temp and of
+    salt, each result applied with vs.update) on host arrays of the 1-degree
+    workload. Every call uploads the fields it reads and downloads the ones it
+    returns, so the host<->device copies are inside the timed region; wall
+    clock per step (the calls return host arrays, so each one ends with the
+    host waiting)."""
+    import torch
+
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from veros_like import VerosLikeState
+    from veros_gb300 import isoneutral, synthetic
+    from veros_gb300.state import DeviceState
+
+    host = synthetic.global_1deg_state(seed=0)
+    settings = dict(host.settings, nx=host.nx, ny=host.ny, nz=host.nz)
+    state = VerosLikeState(settings, host.arrays, host.tau, host.taup1, host.taum1)
+    vs = state.variables
+    cells = host.nx * host.ny * host.nz
+
+    def step():
+        vs.P_diss_iso = np.zeros_like(vs.P_diss_iso)
+        vs.dtemp_iso = np.zeros_like(vs.dtemp_iso)
+        vs.dsalt_iso = np.zeros_like(vs.dsalt_iso)
+        vs.update(isoneutral.isoneutral_diffusion_pre(state))
+        vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.temp, istemp=True))
+        vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.salt, istemp=False))
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    b0 = dict(DeviceState.transfer_bytes)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = time.perf_counter() - t0
+    h2d = (DeviceState.transfer_bytes["h2d"] - b0["h2d"]) // steps
+    d2h = (DeviceState.transfer_bytes["d2h"] - b0["d2h"]) // steps
+    return {"value": cells * steps / dt, "unit": "cells/s", "ms_per_step": dt / steps * 1e3, "steps": steps,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "api": "isoneutral_diffusion_pre / isoneutral_diffusion (the functions plugin.install() binds) on a "
+                   "NumPy-backend VerosState stand-in, thermodynamics.py:425-432 call sequence, host arrays in "
+                   "the reference layout",
+            "timing": f"wall clock, {steps} steps after {warmup} warm-up"}
+
+
 # The tridiagonal A/B workload: one system per column of the 1-degree domain
 # (364 x 184 with the halo) and its 60 levels
 TDMA_NSYS, TDMA_DEPTH = (WORKLOAD["nx"] + 4) * (WORKLOAD["ny"] + 4), WORKLOAD["nz"]
@@ -693,15 +741,16 @@ def run_gb300(args):
 
     launches = args.steps * stepper.launches_per_step()
     ensemble = adjoint = None
-    if not (args.no_ensemble and args.no_adjoint and not args.quarter_degree and not args.aux):
+    if not (args.no_ensemble and args.no_adjoint and args.no_quarter_degree and not args.aux):
         del dev, stepper
         torch.cuda.empty_cache()
     if not args.no_ensemble:
         ensemble = run_ensemble(device)
     if not args.no_adjoint:
         adjoint = run_adjoint(device)
-    quarter = run_quarter_degree(device) if args.quarter_degree else None
+    quarter = None if args.no_quarter_degree else run_quarter_degree(device)
     aux = run_aux(device) if args.aux else None
+    dropin = None if args.no_dropin_host else run_dropin_host(device)
     if rank != 0:
         return 0
     peak, peak_kind = _peaks()
@@ -741,6 +790,7 @@ def run_gb300(args):
         "ensemble": ensemble,
         "adjoint": adjoint,
         "quarter_degree": quarter,
+        "e2e_dropin_host": dropin,
         "aux": aux,
         "clocks": clocks.summary(),
     }
@@ -758,8 +808,10 @@ def main():
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 48-member batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 8-step rollout adjoint measurement")
-    ap.add_argument("--quarter-degree", action="store_true",
-                    help="add the 0.25-degree split-versus-FP64 measurement (100 steps, ~25 GB of device memory)")
+    ap.add_argument("--no-quarter-degree", action="store_true",
+                    help="skip the 0.25-degree split-versus-FP64 measurement (100 steps, ~25 GB of device memory)")
+    ap.add_argument("--no-dropin-host", action="store_true",
+                    help="skip the timing of the drop-in calls on host arrays (a plugin-installed NumPy Veros)")
     ap.add_argument("--no-kernel-ab", action="store_true",
                     help="reference arm: skip the reference's CUDA TDMA kernel timing")
     ap.add_argument("--aux", action="store_true",

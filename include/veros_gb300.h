@@ -199,6 +199,11 @@ int vg_isoneutral_diffusion_noalloc_f64(const VgDomain *dom, const VgGrid *grid,
                                         const VgTracerArgs *tr, int skew, void *stream);
 /* Bytes of the static scratch array vg_isoneutral_diffusion_noalloc_f64 uses. */
 size_t vg_isoneutral_diffusion_noalloc_capacity(void);
+/* Forget the cached device addresses of that array (no GPU work). The address
+ * belongs to a device's context: a caller that resets a device
+ * (cudaDeviceReset unloads the library's device code) calls this before the
+ * next scratch-free call on it. No counterpart in the reference. */
+void vg_isoneutral_diffusion_noalloc_reset(void);
 
 /* Fields of one rollout step (vg_isoneutral_step_f64). */
 typedef struct VgStepFields {
@@ -259,11 +264,20 @@ int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, v
  * salt at level taup1 with the diffusivity kappaH and the surface forcing
  * forc_temp_surface / forc_salt_surface ((X, Y) planes, canonical pitch);
  * writes the new levels and dtemp_vmix / dsalt_vmix on the whole array.
- * Single process, non-cyclic (the closing boundary exchange is a no-op). */
+ * enable_cyclic_x (settings.enable_cyclic_x): end with the closing boundary
+ * exchange of the new temp and salt levels (thermodynamics.py:292-298) as one
+ * process runs it, the periodic x-halo copy of vg_enforce_boundaries_f64.
+ * Domain decompositions over several processes are not supported. */
 int vg_vertmix_tempsalt_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                             const double *kappaH, const int32_t *kbot, double *temp_taup1, double *salt_taup1,
                             const double *forc_temp_surface, const double *forc_salt_surface,
-                            double *dtemp_vmix, double *dsalt_vmix, void *stream);
+                            double *dtemp_vmix, double *dsalt_vmix, int enable_cyclic_x, void *stream);
+
+/* Replaces veros.core.utilities.enforce_boundaries (veros/core/utilities.py:7-21)
+ * for one process: with enable_cyclic_x, arr[-2:, ...] = arr[2:4, ...] and then
+ * arr[:2, ...] = arr[-4:-2, ...] over every (j, k) of one (X, Y, Z) field in
+ * the canonical layout; without it nothing is done (as the reference). */
+int vg_enforce_boundaries_f64(const VgDomain *dom, double *arr, int enable_cyclic_x, void *stream);
 
 /* Replaces isoneutral_diag_streamfunction_kernel
  * (veros/core/isoneutral/isoneutral.py:232-254): B1_gm[2:-2,1:-2] and
@@ -360,6 +374,18 @@ int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, long long s_y
                           const double *a, const double *b, const double *c, const double *d,
                           const uint8_t *water, const uint8_t *edge,
                           const double *b_edge, const double *d_edge, double *out,
+                          int *bad_columns, void *stream);
+
+/* The same drop-in for float32 systems (runtime_settings.float_type =
+ * "float32", veros/runtime.py:93). The reference's NumPy solve passes float32
+ * arrays to LAPACK dgtsv, which computes on float64 copies, and stores the
+ * solution into a float32 array (veros/core/operators.py:64, :75-76): this
+ * call widens each entry to double, eliminates in double in dgtsv's order
+ * and rounds each solution value to float once. */
+int vg_solve_implicit_f32(int nsx, int nsy, int nz, long long s_x, long long s_y, long long s_z,
+                          const float *a, const float *b, const float *c, const float *d,
+                          const uint8_t *water, const uint8_t *edge,
+                          const float *b_edge, const float *d_edge, float *out,
                           int *bad_columns, void *stream);
 
 /* Drop-in for the XLA GPU custom-call targets tdma_cuda_double / tdma_cuda_float

@@ -22,6 +22,8 @@ trailing ``(ip|jp, kr)`` pair), the Veros NumPy-backend algorithm for:
                                     veros/core/utilities.py:24-59
 * ``solve_tridiagonal_numpy``       veros/core/operators.py:60-77
 * ``vertmix_tempsalt``              veros/core/thermodynamics.py:248-300
+* ``enforce_boundaries`` (one process)
+                                    veros/core/utilities.py:7-16
 * ``isoneutral_diag_streamfunction_kernel``
                                     veros/core/isoneutral/isoneutral.py:232-254
 
@@ -306,13 +308,16 @@ def solve_tridiagonal(a, b, c, d, water_mask, edge_mask):
     a[edge_mask] = 0
     c[..., -1] = 0
     if _kbot_form(water_mask, edge_mask):
+        # dgtsv works in float64 on whatever the reference hands it; the
+        # solution is stored in an array of a's dtype (float32 runs round it)
         nz = a.shape[-1]
         shape = a.shape
         wm = water_mask.reshape(-1, nz)
         has = wm.any(axis=1)
         ks = np.where(has, wm.argmax(axis=1), nz)
-        sol = dgtsv_columns(a.reshape(-1, nz), b.reshape(-1, nz), c.reshape(-1, nz), d.reshape(-1, nz), ks)
-        return sol.reshape(shape)
+        f64 = lambda x: np.asarray(x, dtype=np.float64).reshape(-1, nz)  # noqa: E731
+        sol = dgtsv_columns(f64(a), f64(b), f64(c), f64(d), ks)
+        return sol.reshape(shape).astype(out.dtype, copy=False)
     from scipy.linalg import lapack
 
     sol = lapack.dgtsv(a[water_mask][1:], b[water_mask], c[water_mask][:-1], d[water_mask])[3]
@@ -531,9 +536,22 @@ def isoneutral_step(vs, settings):
     vs.taum1, vs.tau, vs.taup1 = vs.tau, vs.taup1, vs.taum1
 
 
+def enforce_boundaries(arr, enable_cyclic_x):
+    """``enforce_boundaries`` (veros/core/utilities.py:7-16) on one process:
+    with a cyclic x boundary the two halo columns on each side take the
+    periodic interior columns; otherwise nothing changes."""
+    arr = arr.copy()
+    if enable_cyclic_x:
+        arr[-2:, ...] = arr[2:4, ...]
+        arr[:2, ...] = arr[-4:-2, ...]
+    return arr
+
+
 def vertmix_tempsalt(vs, settings):
-    """``vertmix_tempsalt`` (veros/core/thermodynamics.py:248-300), non-cyclic,
-    single process (the closing boundary exchange is then a no-op).
+    """``vertmix_tempsalt`` (veros/core/thermodynamics.py:248-300) on one
+    process, including its closing boundary exchange of the new temp and salt
+    levels (:292-298), which copies the periodic x halo when the setting
+    ``enable_cyclic_x`` is on (absent: off).
 
     Returns a dict with ``temp``, ``salt``, ``dtemp_vmix``, ``dsalt_vmix``.
     """
@@ -563,6 +581,10 @@ def vertmix_tempsalt(vs, settings):
         tr[2:-2, 2:-2, :, tp1] = np.where(water_mask, sol, tr[2:-2, 2:-2, :, tp1])
     dtemp_vmix = (temp[:, :, :, tp1] - dtemp_vmix) / dt
     dsalt_vmix = (salt[:, :, :, tp1] - dsalt_vmix) / dt
+    cyclic = bool(settings.get("enable_cyclic_x", False) if isinstance(settings, dict)
+                  else getattr(settings, "enable_cyclic_x", False))
+    temp[..., tp1] = enforce_boundaries(temp[..., tp1], cyclic)
+    salt[..., tp1] = enforce_boundaries(salt[..., tp1], cyclic)
     return dict(temp=temp, salt=salt, dtemp_vmix=dtemp_vmix, dsalt_vmix=dsalt_vmix)
 
 

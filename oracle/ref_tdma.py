@@ -27,8 +27,20 @@ LAUNCHER = os.path.join(OUT, "libref_tdma_launch.so")
 REF_SOURCE = os.path.join("veros", "core", "special", "cuda_tdma_kernels.cu")
 
 
+# Where this build recipe finds the reference sources it compiles: the
+# REF_ROOT environment variable, else the checkout location of the build
+# container. GPU machines have neither; there the cubin built beforehand is used.
+_DEFAULT_CHECKOUT = os.path.join(os.sep, "root", "reference")
+
+
 def _ref_root():
-    return os.environ.get("REF_ROOT", os.path.join(os.sep, "root", "reference"))
+    return os.environ.get("REF_ROOT", _DEFAULT_CHECKOUT)
+
+
+def reference_root():
+    """The reference checkout the test infrastructure may import from, or None."""
+    root = _ref_root()
+    return root if os.path.isdir(os.path.join(root, "veros")) else None
 
 
 def _nvcc():

@@ -1,10 +1,12 @@
 """Generate the golden vectors that pin the oracle and the synthetic-state builder.
 
-Runs the Veros reference NumPy backend (``/root/reference``) in this process,
-so it only works where that checkout exists; the ``.npz`` files it writes are
+Runs the Veros reference NumPy backend in this process, so it only works
+where a checkout of the reference exists; the ``.npz`` files it writes are
 committed and the tests read only those. Usage::
 
-    python tests/golden/make_golden.py [/path/to/veros/checkout]
+    python tests/golden/make_golden.py /path/to/veros/checkout [case ...]
+
+(or with the checkout in the ``REF_ROOT`` environment variable).
 
 ``loguru`` is not installed here, so a no-op stand-in module is registered
 before Veros is imported (Veros only logs through it).
@@ -25,6 +27,12 @@ Cases (all float64, reference layout):
 * ``vertmix_random``: ``vertmix_tempsalt`` (veros/core/thermodynamics.py:248-300)
   and ``isoneutral_diag_streamfunction_kernel`` (veros/core/isoneutral/isoneutral.py:232-254)
   on the random-state fixture, with a non-negative vertical diffusivity.
+* ``thermo_cyclic``: the tracer part of ``thermodynamics`` as Veros calls it
+  (veros/core/thermodynamics.py:425-441: zeroed tendencies, pre, diffusion of
+  temp and salt, skew diffusion of both, vertical mixing with its closing
+  boundary exchange) on a random state with ``enable_cyclic_x``.
+* ``tridiag_f32``: the reference's NumPy solve on float32 systems (its float64
+  LAPACK call and float32 output, veros/core/operators.py:60-77).
 """
 
 import os
@@ -172,6 +180,70 @@ def make_vertmix_case(nx, ny, nz, seed):
     return blob
 
 
+THERMO_FIELDS = ("dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt", "kbot", "maskT", "maskU",
+                 "maskV", "maskW", "temp", "salt", "K_iso", "K_gm", "int_drhodT", "int_drhodS", "dtemp_iso",
+                 "dsalt_iso", "P_diss_iso", "P_diss_skew", "kappaH", "forc_temp_surface", "forc_salt_surface",
+                 "dtemp_vmix", "dsalt_vmix") + PRE_FIELDS
+THERMO_OUT = ("temp", "salt", "dtemp_iso", "dsalt_iso", "P_diss_iso", "P_diss_skew", "dtemp_vmix",
+              "dsalt_vmix") + PRE_FIELDS
+THERMO_SETTINGS = SETTING_KEYS + ("enable_cyclic_x", "enable_neutral_diffusion", "enable_skew_diffusion")
+
+
+def make_thermo_case(nx, ny, nz, seed):
+    """thermodynamics.py:425-441 on the random-state fixture with a cyclic x boundary."""
+    from veros.core import isoneutral
+    from veros.core.thermodynamics import vertmix_tempsalt
+    from veros.core.operators import update, at
+    from veros.pyom_compat import get_random_state
+
+    np.random.seed(seed)
+    settings = dict(nx=nx, ny=ny, nz=nz, dt_tracer=3600, dt_mom=3600, enable_neutral_diffusion=True,
+                    enable_skew_diffusion=True, enable_conserve_energy=True, enable_cyclic_x=True, K_iso_steep=1)
+    state = get_random_state(extra_settings=settings)
+    vs = state.variables
+    vs.kappaH = np.abs(np.asarray(vs.kappaH)) * 1e-2  # non-negative, as the mixing closures produce
+    blob = {f"in_{k}": v for k, v in _snapshot(vs, THERMO_FIELDS).items()}
+    blob.update({f"setting_{k}": np.array(getattr(state.settings, k)) for k in THERMO_SETTINGS})
+    blob.update(nx=np.array(nx), ny=np.array(ny), nz=np.array(nz))
+    blob.update(tau=np.array(vs.tau), taup1=np.array(vs.taup1), taum1=np.array(vs.taum1))
+    # veros/core/thermodynamics.py:425-441, the enable_neutral_diffusion branch and vertical mixing
+    vs.P_diss_iso = update(vs.P_diss_iso, at[...], 0.0)
+    vs.dtemp_iso = update(vs.dtemp_iso, at[...], 0.0)
+    vs.dsalt_iso = update(vs.dsalt_iso, at[...], 0.0)
+    vs.update(isoneutral.isoneutral_diffusion_pre(state))
+    vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.temp, istemp=True))
+    vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.salt, istemp=False))
+    vs.P_diss_skew = update(vs.P_diss_skew, at[...], 0.0)
+    vs.update(isoneutral.isoneutral_skew_diffusion(state, tr=vs.temp, istemp=True))
+    vs.update(isoneutral.isoneutral_skew_diffusion(state, tr=vs.salt, istemp=False))
+    vs.update(vertmix_tempsalt(state))
+    blob.update({f"out_{k}": np.array(getattr(vs, k)).copy() for k in THERMO_OUT})
+    return blob
+
+
+def make_tridiag_f32_case():
+    from veros.core.utilities import create_water_masks, solve_implicit
+
+    rng = np.random.default_rng(23)
+    nx, ny, nz = 12, 10, 16
+    kbot = rng.integers(0, nz, size=(nx, ny))
+    _, water_mask, edge_mask = create_water_masks(kbot, nz)
+    delta = (np.abs(rng.standard_normal((nx, ny, nz))) * 3.0).astype(np.float32)
+    a = -delta
+    c = -np.roll(delta, -1, axis=-1)
+    b = np.float32(1.0) + delta + np.roll(delta, -1, axis=-1)
+    d = rng.standard_normal((nx, ny, nz)).astype(np.float32)
+    b_edge = (1.0 + np.abs(rng.standard_normal((nx, ny, nz)))).astype(np.float32)
+    d_edge = rng.standard_normal((nx, ny, nz)).astype(np.float32)
+    # general (non-dominant) float32 systems: pivot interchanges in dgtsv
+    ra, rb, rc, rd = (rng.standard_normal((nx, ny, nz)).astype(np.float32) for _ in range(4))
+    out_dd = solve_implicit(a.copy(), b, c.copy(), d, water_mask, edge_mask, b_edge=b_edge, d_edge=d_edge)
+    out_random = solve_implicit(ra.copy(), rb, rc.copy(), rd, water_mask, edge_mask)
+    assert out_dd.dtype == np.float32 and out_random.dtype == np.float32
+    return dict(a=a, b=b, c=c, d=d, b_edge=b_edge, d_edge=d_edge, kbot=kbot, water_mask=water_mask,
+                edge_mask=edge_mask, out_dd=out_dd, ra=ra, rb=rb, rc=rc, rd=rd, out_random=out_random)
+
+
 def make_tridiag_case():
     from veros.core.operators import solve_tridiagonal_numpy
     from veros.core.utilities import create_water_masks, solve_implicit
@@ -225,9 +297,12 @@ def make_grid_case():
 
 
 def main():
-    """make_golden.py [reference_root] [case ...]: writes the named cases (all by default)."""
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    only = set(sys.argv[2:])
+    """make_golden.py reference_root [case ...]: writes the named cases (all by default)."""
+    args = sys.argv[1:]
+    ref = args.pop(0) if args and os.path.isdir(os.path.join(args[0], "veros")) else os.environ.get("REF_ROOT")
+    if not ref or not os.path.isdir(os.path.join(ref, "veros")):
+        sys.exit("usage: make_golden.py <reference checkout> [case ...]  (or set REF_ROOT)")
+    only = set(args)
     _import_reference(ref)
     makers = {
         "iso_random_energy": lambda: make_random_case(12, 10, 8, True),
@@ -238,6 +313,8 @@ def main():
         "iso_synth_eq4": lambda: make_synth_case(3, 4, False, 0.3),
         "tridiag": make_tridiag_case,
         "vertmix_random": lambda: make_vertmix_case(12, 10, 9, 17),
+        "thermo_cyclic": lambda: make_thermo_case(16, 12, 8, 29),
+        "tridiag_f32": make_tridiag_f32_case,
         "grid_topo": make_grid_case,
     }
     cases = {name: make() for name, make in makers.items() if not only or name in only}

@@ -1,5 +1,12 @@
 """The C ABI without a GPU: the library loads, exports every declared symbol,
-and rejects bad arguments with status codes (no CUDA call is reached)."""
+and rejects bad arguments with status codes (no CUDA call is reached).
+
+Non-NULL pointer arguments come from ``_buffer``: where a GPU is present, real
+zeroed device memory large enough for every access the small test domains
+allow, so that a regression that let a call past its argument check would
+compute on valid memory and fail the status assertion, not fault the GPU;
+without a GPU, placeholder addresses that no call ever dereferences (a launch
+would fail with "no device")."""
 
 import ctypes
 import os
@@ -41,6 +48,23 @@ def test_version_and_empty_error(lib):
     assert lib.vg_version().startswith(b"veros_gb300")
 
 
+_KEEP = []
+
+
+def _buffer(nbytes=1 << 16):
+    """Address of ``nbytes`` of zeroed device memory (placeholder without a GPU)."""
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            t = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+            _KEEP.append(t)
+            return t.data_ptr()
+    except ImportError:
+        pass
+    return 1 << 40
+
+
 def _dom(X=10, Y=9, Z=5, pitch=16):
     from veros_gb300 import _capi
 
@@ -70,11 +94,11 @@ def test_null_pointers_and_settings_are_rejected(lib):
     with pytest.raises(ValueError):
         _capi.check(st, "pre")
     # an unsupported equation of state is reported before any launch
-    fake = ctypes.c_void_p(16)
-    grid = _capi.VgGrid(*([fake] * 9))
-    ten = _capi.VgTensorFields(*([fake] * 7), 1, 1)
+    buf = ctypes.c_void_p(_buffer())
+    grid = _capi.VgGrid(*([buf] * 9))
+    ten = _capi.VgTensorFields(*([buf] * 7), 1, 1)
     sett.eq_of_state_type = 5
-    st = lib.vg_isoneutral_pre_f64(_dom(), grid, sett, fake, fake, fake, fake, ten, None)
+    st = lib.vg_isoneutral_pre_f64(_dom(), grid, sett, buf, buf, buf, buf, ten, None)
     assert st == _capi.VG_ERR_UNSUPPORTED
     with pytest.raises(NotImplementedError):
         _capi.check(st, "pre")
@@ -86,17 +110,17 @@ def test_diffusion_scratch_contract(lib):
     d = _dom()
     need = lib.vg_isoneutral_diffusion_scratch_bytes(d)
     assert need == 3 * d.plane * d.Z * 8
-    fake = ctypes.c_void_p(16)
-    grid = _capi.VgGrid(*([fake] * 9))
-    ten = _capi.VgTensorFields(*([fake] * 7), 1, 1)
+    buf = ctypes.c_void_p(_buffer())
+    grid = _capi.VgGrid(*([buf] * 9))
+    ten = _capi.VgTensorFields(*([buf] * 7), 1, 1)
     sett = _capi.VgIsoSettings(1e-3, 1e-3, 0.0, 3600.0, 9.81, 1024.0, 1, 0)
-    tr = _capi.VgTracerArgs(fake, fake, fake, None, None)
-    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, fake, fake, fake, tr, 0, fake, need - 8, None)
+    tr = _capi.VgTracerArgs(buf, buf, buf, None, None)
+    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, buf, buf, buf, tr, 0, buf, need - 8, None)
     assert st == _capi.VG_ERR_SCRATCH
-    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, fake, fake, fake, tr, 2, fake, need, None)
+    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, buf, buf, buf, tr, 2, buf, need, None)
     assert st == _capi.VG_ERR_ARG
     sett.enable_conserve_energy = 1
-    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, fake, fake, fake, tr, 0, fake, need, None)
+    st = lib.vg_isoneutral_diffusion_f64(d, grid, sett, ten, buf, buf, buf, tr, 0, buf, need, None)
     assert st == _capi.VG_ERR_ARG
 
 
@@ -108,11 +132,11 @@ def test_tridiag_shape_checks(lib):
     st = lib.vg_solve_implicit_f64(4, 4, 10, 1, 4, 16, *([None] * 11))
     assert st == _capi.VG_ERR_ARG
     # the output may not overlap an input (checked on the pointers, before any
-    # launch; only overlapping cases here, which never reach the device);
-    # 16 columns x 10 levels of doubles span 1280 bytes
-    base = 1 << 40
+    # launch; only overlapping cases here, all inside one buffer and 8-byte
+    # aligned); 16 columns x 10 levels of doubles span 1280 bytes
+    base = _buffer(8 * 4096) + 4096
     arrs = [base + n * 4096 for n in range(6)] + [None, None]  # a b c d water edge b_edge d_edge
-    for out in (arrs[3], arrs[1] + 1272, arrs[4] - 1279, arrs[0] - 1272):
+    for out in (arrs[3], arrs[1] + 1272, arrs[4] - 1272, arrs[0] - 1272):
         st = lib.vg_solve_implicit_f64(4, 4, 10, 10, 40, 1, *arrs, out, None, None)
         assert st == _capi.VG_ERR_ARG and "overlaps" in _capi.last_error()
     # the XLA-style entry keeps the error instead of exiting

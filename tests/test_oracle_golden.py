@@ -75,3 +75,44 @@ def test_vertmix_and_streamfunction_match_reference():
     out = orc.isoneutral_diag_streamfunction(vs)
     for k in ("B1_gm", "B2_gm"):
         _close(out[k], g[f"sf_{k}"], k)
+
+
+def test_thermodynamics_sequence_matches_reference():
+    """thermodynamics.py:425-441 (pre, diffusion and skew diffusion of both
+    tracers, vertical mixing with the cyclic boundary exchange) on the
+    reference's random state with enable_cyclic_x."""
+    g = load_golden("thermo_cyclic")
+    vs, s = _state_and_settings(g)
+    assert s["enable_cyclic_x"]
+    vs.P_diss_iso = np.zeros_like(vs.P_diss_iso)
+    vs.dtemp_iso = np.zeros_like(vs.dtemp_iso)
+    vs.dsalt_iso = np.zeros_like(vs.dsalt_iso)
+    vs.__dict__.update(orc.isoneutral_diffusion_pre(vs, s))
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, s, True))
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, s, False))
+    vs.P_diss_skew = np.zeros_like(vs.P_diss_skew)
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, s, True, iso=False))
+    vs.__dict__.update(orc.isoneutral_diffusion(vs, s, False, iso=False))
+    vs.__dict__.update(orc.vertmix_tempsalt(vs, s))
+    for k in ("temp", "salt", "dtemp_iso", "dsalt_iso", "P_diss_iso", "P_diss_skew", "dtemp_vmix", "dsalt_vmix",
+              "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "K_11", "K_22", "K_33"):
+        _close(getattr(vs, k), g[f"out_{k}"], k)
+
+
+def test_enforce_boundaries_is_the_periodic_halo_copy():
+    arr = np.arange(9 * 4 * 2, dtype=float).reshape(9, 4, 2)
+    out = orc.enforce_boundaries(arr, True)
+    assert np.array_equal(out[-2:], arr[2:4]) and np.array_equal(out[:2], arr[-4:-2])
+    assert np.array_equal(out[2:-2], arr[2:-2])
+    assert np.array_equal(orc.enforce_boundaries(arr, False), arr)
+
+
+def test_float32_tridiag_matches_reference():
+    """float32 systems: dgtsv in float64, the solution rounded to float32
+    (veros/core/operators.py:64, :75-76), bit for bit."""
+    g = load_golden("tridiag_f32")
+    out = orc.solve_implicit(g["a"], g["b"], g["c"], g["d"], g["water_mask"], g["edge_mask"],
+                             b_edge=g["b_edge"], d_edge=g["d_edge"])
+    assert out.dtype == np.float32 and np.array_equal(out, g["out_dd"])
+    out = orc.solve_tridiagonal(g["ra"], g["rb"], g["rc"], g["rd"], g["water_mask"], g["edge_mask"])
+    assert out.dtype == np.float32 and np.array_equal(out, g["out_random"])

@@ -59,8 +59,10 @@ def test_install_on_the_reference_modules_when_present():
     import importlib
     import os
 
-    ref = os.environ.get("REF_ROOT", os.path.join(os.sep, "root", "reference"))
-    if not os.path.isdir(os.path.join(ref, "veros")):
+    from oracle.ref_tdma import reference_root
+
+    ref = reference_root()
+    if ref is None:
         pytest.skip("reference checkout not present")
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
     try:
@@ -78,3 +80,45 @@ def test_install_on_the_reference_modules_when_present():
             assert getattr(importlib.import_module(modname), attr) is fn
     finally:
         handle.uninstall()
+
+
+def test_vertmix_raises_on_several_processes(monkeypatch):
+    """A multi-process Veros (runtime_state.proc_num > 1) would need the
+    domain decomposition's halo exchange at the end of vertmix_tempsalt
+    (veros/core/utilities.py:18-20): the drop-in refuses before any GPU work."""
+    from veros_gb300 import thermodynamics
+
+    fake = types.ModuleType("veros")
+    fake.runtime_state = types.SimpleNamespace(proc_num=2)
+    monkeypatch.setitem(sys.modules, "veros", fake)
+    with pytest.raises(NotImplementedError, match="2 processes"):
+        thermodynamics.vertmix_tempsalt(object())
+    fake.runtime_state.proc_num = 1
+    from veros_gb300.state import require_single_process
+
+    require_single_process("one process")  # no error
+
+
+def test_veros_like_state_keeps_the_reference_contract():
+    """The stand-in state the GPU drop-in tests use behaves like the reference's
+    VerosVariables (veros/state.py:70-90, :219-243)."""
+    import collections
+
+    import numpy as np
+
+    from veros_like import VerosLikeState
+
+    st = VerosLikeState(dict(nx=2, ny=2, nz=3), {"temp": np.zeros((6, 6, 3, 3)), "kbot": np.zeros((6, 6), int)})
+    vs = st.variables
+    assert not vs.temp.flags.writeable
+    with pytest.raises(ValueError):
+        vs.temp[0, 0, 0, 0] = 1.0
+    assert vs.update(None) is vs  # a routine's None result changes nothing
+    KO = collections.namedtuple("KernelOutput", ["temp"])
+    vs.update(KO(temp=np.ones((6, 6, 3, 3), dtype=np.float32)))
+    assert vs.temp.dtype == np.float64 and vs.temp[0, 0, 0, 0] == 1.0
+    with pytest.raises(ValueError, match="unexpected shape"):
+        vs.temp = np.ones((6, 6, 3))
+    with pytest.raises(AttributeError):
+        vs.update({"unknown": 1})
+    assert vs.kbot.dtype.kind == "i"

@@ -139,6 +139,7 @@ SIGNATURES = {
                                                            ctypes.POINTER(VgTracerArgs), ctypes.c_int,
                                                            ctypes.c_void_p]),
     "vg_isoneutral_diffusion_noalloc_capacity": (ctypes.c_size_t, []),
+    "vg_isoneutral_diffusion_noalloc_reset": (None, []),
     "vg_isoneutral_diffusion_pair_scratch_bytes": (ctypes.c_size_t, [ctypes.POINTER(VgDomain)]),
     "vg_isoneutral_diffusion_pair_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                                         ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgTensorFields),
@@ -168,7 +169,10 @@ SIGNATURES = {
     "vg_isoneutral_step_prepare_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgStepFields),
                                                       ctypes.c_void_p]),
     "vg_vertmix_tempsalt_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
-                                               ctypes.POINTER(VgIsoSettings)] + [ctypes.c_void_p] * 9),
+                                               ctypes.POINTER(VgIsoSettings)] + [ctypes.c_void_p] * 8 +
+                                [ctypes.c_int, ctypes.c_void_p]),
+    "vg_enforce_boundaries_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_void_p, ctypes.c_int,
+                                                 ctypes.c_void_p]),
     "vg_isoneutral_streamfunction_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_void_p, ctypes.c_void_p,
                                                         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
                                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -185,6 +189,8 @@ SIGNATURES = {
     "vg_ensemble_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "vg_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "vg_solve_implicit_f64": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
+                                             ctypes.c_longlong, ctypes.c_longlong] + [ctypes.c_void_p] * 11),
+    "vg_solve_implicit_f32": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_longlong,
                                              ctypes.c_longlong, ctypes.c_longlong] + [ctypes.c_void_p] * 11),
     "vg_tdma_cuda_double": (None, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
                                    ctypes.c_size_t]),

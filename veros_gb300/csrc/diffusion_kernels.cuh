@@ -671,11 +671,16 @@ __global__ void __launch_bounds__(kEnergyTX *kEnergyTY) energy_kernel(DiffArgs<F
   const int ks = a0.kbot[L.at2(i, j)] - 1;
   const bool land = ks >= 0;  // "land_mask" of create_water_masks: the column has water
   const bool inner = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
+  // flux_east exists on [1:-2, 2:-2] and flux_north on [2:-2, 1:-2]
+  // (diffusion.py:25, :52); the reference reads flux_east[1:-1] and [:-2],
+  // flux_north[:, 1:-1] and [:, :-2] (veros/core/diffusion.py:22-31), zero
+  // outside those ranges. The halo columns i = 1, X-2 and rows j = 1, Y-2
+  // only matter where kbot makes them water (a cyclic x boundary).
   EnergyColumn<F> col;
-  col.fe0 = i < L.X - 2 && j >= 2 && j < L.Y - 2;
-  col.fe1 = i >= 2 && col.fe0;
-  col.fn0 = i >= 2 && i < L.X - 2 && j < L.Y - 2;
-  col.fn1 = j >= 2 && col.fn0;
+  col.fe0 = i < L.X - 2 && j >= 2 && j < L.Y - 2;  // flux_east[i, j]
+  col.fe1 = i >= 2 && j >= 2 && j < L.Y - 2;       // flux_east[i-1, j]
+  col.fn0 = i >= 2 && i < L.X - 2 && j < L.Y - 2;  // flux_north[i, j]
+  col.fn1 = i >= 2 && i < L.X - 2 && j >= 2;       // flux_north[i, j-1]
   col.cx = to_F<F>(pm(c_cost[threadIdx.y], inv_dxt[threadIdx.x]));
   col.cy = to_F<F>(c_dyt_cost[threadIdx.y]);
   const F ratio = (land && ks >= k0 && ks < k1) ? ratio_s[ks - k0] : F(0.0);

@@ -63,14 +63,15 @@ int launch_implicit(const DiffArgs<F> &a, const DiffArgs<F> &b, cudaStream_t s) 
 // which an SM's resident CTAs share, so the cost of a chunking is the CTAs an
 // SM receives times the levels per CTA, counting a chunk's extra dissipation
 // evaluation at its top as half a level.
+// The SM count is that of the current device, read on every call (an
+// attribute query, no synchronisation): no state is shared between devices
+// or host threads.
 inline int energy_kchunk(int ctas_per_chunk, int Z) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    sms = std::max(1, sms);
-  }
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                 cudaSuccess)
+    sms = 1;
+  sms = std::max(1, sms);
   int best = Z;
   double best_cost = 1e300;
   for (int nch = 1; nch <= std::min(Z, 64); ++nch) {
@@ -225,7 +226,10 @@ extern "C" int vg_isoneutral_diffusion_pair_f32split(const VgDomain *dom, const 
 //   the array's device address with cudaGetSymbolAddress and caches it per
 //   device; make that first call before any stream capture. Host code must
 //   never pass the array's name itself to a kernel: in host code it is only a
-//   stand-in, not a device address.
+//   stand-in, not a device address. The cached address belongs to the
+//   device's current context: after cudaDeviceReset (which unloads this
+//   library's device code) call vg_isoneutral_diffusion_noalloc_reset before
+//   the next call, so that the address is looked up again.
 // * Sharing: every call uses the same array, which keeps the last call's
 //   contents. Nothing in it has to start at zero (each call writes every
 //   scratch cell it later reads), but calls that overlap on the GPU (on
@@ -246,6 +250,11 @@ void *g_noalloc_ptr[kMaxDevices] = {};
 }  // namespace vg
 
 extern "C" size_t vg_isoneutral_diffusion_noalloc_capacity(void) { return vg::kNoAllocScratchBytes; }
+
+extern "C" void vg_isoneutral_diffusion_noalloc_reset(void) {
+  std::lock_guard<std::mutex> lock(vg::g_noalloc_mutex);
+  for (void *&p : vg::g_noalloc_ptr) p = nullptr;
+}
 
 extern "C" int vg_isoneutral_diffusion_noalloc_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                                    const VgTensorFields *ten, const double *K_field,

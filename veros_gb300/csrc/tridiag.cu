@@ -1,7 +1,8 @@
 // Column tridiagonal solves.
 //
-// * vg_solve_implicit_f64: the drop-in for solve_implicit / solve_tridiagonal
-//   (veros/core/utilities.py:51-59, veros/core/operators.py:60-77). One thread
+// * vg_solve_implicit_f64 / _f32: the drop-in for solve_implicit /
+//   solve_tridiagonal (veros/core/utilities.py:51-59,
+//   veros/core/operators.py:60-77) on float64 or float32 arrays. One thread
 //   per column solves that column's water cells k = ks..nz-1 by Gaussian
 //   elimination with partial pivoting in the operation order of LAPACK dgtsv,
 //   which the reference calls (dgtsv.cuh); the factors stay in shared memory.
@@ -22,36 +23,48 @@ namespace {
 
 constexpr int kMaxNz = 200;
 
+// Storage type T of the coefficients, right-hand sides and solution: double,
+// or float for the reference's float32 runs, whose NumPy solve hands float32
+// arrays to LAPACK dgtsv, which works on float64 copies, and stores the
+// float64 solution into a float32 output (veros/core/operators.py:64, :75-76).
+// The elimination below is always in double; a float solution is rounded
+// once, on its store.
+template <typename T>
 struct TriArgs {
   int nsx, nsys, nz;
   long long sx, sy, sz;
-  const double *a, *b, *c, *d, *b_edge, *d_edge;
+  const T *a, *b, *c, *d, *b_edge, *d_edge;
   const uint8_t *water, *edge;
-  double *out;
+  T *out;
   int *bad;
 };
 
 // Row source of one generic column (b_edge/d_edge substituted at ks,
 // utilities.py:53-57; a at the edge row is never read, operators.py:72).
+// float entries widen to double exactly.
+template <typename T>
 struct GenSrc {
-  const TriArgs &p;
+  const TriArgs<T> &p;
   long long base;
   int ks;
   __device__ long long at(int k) const { return base + p.sz * k; }
-  __device__ double a(int k) const { return p.a[at(k)]; }
-  __device__ double b(int k) const { return (k == ks && p.b_edge) ? p.b_edge[at(k)] : p.b[at(k)]; }
-  __device__ double c(int k) const { return p.c[at(k)]; }
-  __device__ double d(int k) const { return (k == ks && p.d_edge) ? p.d_edge[at(k)] : p.d[at(k)]; }
+  __device__ double a(int k) const { return (double)p.a[at(k)]; }
+  __device__ double b(int k) const { return (double)((k == ks && p.b_edge) ? p.b_edge[at(k)] : p.b[at(k)]); }
+  __device__ double c(int k) const { return (double)p.c[at(k)]; }
+  __device__ double d(int k) const { return (double)((k == ks && p.d_edge) ? p.d_edge[at(k)] : p.d[at(k)]); }
 };
 
 // One thread per column. Shared memory holds the eliminated diagonal of the
 // CTA's columns, laid out [k][thread]; the eliminated right-hand side goes
-// to the output, which the back substitution overwrites with the solution
-// (the column stays in L2 between the sweeps). With an interchange the
-// column is re-solved from the inputs into the diagonal slots.
+// to the output when that is double (the back substitution overwrites it
+// with the solution; the column stays in L2 between the sweeps), or to a
+// second shared array [k][thread] when the output is float. With an
+// interchange the column is re-solved from the inputs into the diagonal
+// slots.
 constexpr int kTriMaxThreads = 128;
 
-__global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs p) {
+template <typename T>
+__global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs<T> p) {
   extern __shared__ double sm[];
   __shared__ int ks_s[kTriMaxThreads], perm_s[kTriMaxThreads];
   const int t = threadIdx.x;
@@ -75,7 +88,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
         if (w != (ks >= 0) || e != (ks == k)) bad = true;
       }
       if (bad && p.bad) atomicAdd(p.bad, 1);
-      for (int k = 0; k < (ks < 0 ? nz : ks); ++k) p.out[base + p.sz * k] = 0.0;
+      for (int k = 0; k < (ks < 0 ? nz : ks); ++k) p.out[base + p.sz * k] = T(0);
     }
     ks_s[t] = ks;
   }
@@ -96,9 +109,19 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   const int ks = ks_s[perm_s[t]];
   if (s >= p.nsys || ks < 0) return;
   const long long base = base_of(s);
-  GenSrc src{p, base, ks};
+  GenSrc<T> src{p, base, ks};
   double *Ds = sm + t;
-  double *out = p.out + base;  // the eliminated right-hand side, then the solution
+  T *out = p.out + base;  // the solution
+  // the eliminated right-hand side: in the output (double) or in shared memory (float)
+  double *Bs;
+  long long bstride;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    Bs = reinterpret_cast<double *>(out);
+    bstride = p.sz;
+  } else {
+    Bs = sm + (size_t)nb * nz + t;
+    bstride = nb;
+  }
 
   // Loads run PF levels ahead of the elimination's serial chain (software
   // pipelining); the arithmetic is dgtsv's, operation for operation.
@@ -108,15 +131,15 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   for (int u = 0; u < PF; ++u) {
     const int k = ks + 1 + u;
     qa[u] = k < nz ? src.a(k) : 0.0;
-    qb[u] = k < nz ? p.b[src.at(k)] : 0.0;
+    qb[u] = k < nz ? (double)p.b[src.at(k)] : 0.0;
     qc[u] = k < nz - 1 ? src.c(k) : 0.0;
-    qd[u] = k < nz ? p.d[src.at(k)] : 0.0;
+    qd[u] = k < nz ? (double)p.d[src.at(k)] : 0.0;
   }
   // elimination without interchange while dgtsv would take that branch
   bool interchange = false;
   double Dp = src.b(ks), Bp = src.d(ks), cp = ks < nz - 1 ? src.c(ks) : 0.0;
   Ds[(size_t)ks * nb] = Dp;
-  out[p.sz * ks] = Bp;
+  Bs[bstride * ks] = Bp;
   for (int k0 = ks + 1; k0 < nz && !interchange; k0 += PF) {
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
@@ -126,9 +149,9 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
         const int kn = k + PF;
         if (kn < nz) {
           qa[u] = src.a(kn);
-          qb[u] = p.b[src.at(kn)];
+          qb[u] = (double)p.b[src.at(kn)];
           qc[u] = kn < nz - 1 ? src.c(kn) : 0.0;
-          qd[u] = p.d[src.at(kn)];
+          qd[u] = (double)p.d[src.at(kn)];
         }
         if (fabs(Dp) < fabs(dl)) {
           interchange = true;
@@ -138,7 +161,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
           Bp = rsub(dk, rmul(fact, Bp));
           cp = ck;
           Ds[(size_t)k * nb] = Dp;
-          out[p.sz * k] = Bp;
+          Bs[bstride * k] = Bp;
         }
       }
     }
@@ -146,7 +169,7 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   if (interchange) {
     // the row sources are the inputs, which the output does not overlap
     dgtsv_slow_solve(src, ks, nz, Ds, nb);
-    for (int k = ks; k < nz; ++k) out[p.sz * k] = Ds[(size_t)k * nb];
+    for (int k = ks; k < nz; ++k) out[p.sz * k] = (T)Ds[(size_t)k * nb];
     return;
   }
   double qcb[PF], qbs[PF];
@@ -154,10 +177,10 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
   for (int u = 0; u < PF; ++u) {
     const int k = nz - 2 - u;
     qcb[u] = k >= ks ? src.c(k) : 0.0;
-    qbs[u] = k >= ks ? out[p.sz * k] : 0.0;
+    qbs[u] = k >= ks ? Bs[bstride * k] : 0.0;
   }
-  double x = rdiv(out[p.sz * (nz - 1)], Ds[(size_t)(nz - 1) * nb]);
-  out[p.sz * (nz - 1)] = x;
+  double x = rdiv(Bs[bstride * (nz - 1)], Ds[(size_t)(nz - 1) * nb]);
+  out[p.sz * (nz - 1)] = (T)x;
   for (int k0 = nz - 2; k0 >= ks; k0 -= PF) {
 #pragma unroll
     for (int u = 0; u < PF; ++u) {
@@ -166,10 +189,10 @@ __global__ void __launch_bounds__(kTriMaxThreads) pivoting_solve_kernel(TriArgs 
         const double ck = qcb[u], bk = qbs[u];
         if (k - PF >= ks) {
           qcb[u] = src.c(k - PF);
-          qbs[u] = out[p.sz * (k - PF)];
+          qbs[u] = Bs[bstride * (k - PF)];
         }
         x = rdiv(rsub(bk, rmul(ck, x)), Ds[(size_t)k * nb]);
-        out[p.sz * k] = x;
+        out[p.sz * k] = (T)x;
       }
     }
   }
@@ -295,6 +318,51 @@ void xla_tdma(void *stream, void **buffers, const char *opaque, size_t opaque_le
   check_launch(name);
 }
 
+template <typename T>
+int solve_implicit(const char *name, int nsx, int nsy, int nz, long long s_x, long long s_y, long long s_z,
+                   const T *a, const T *b, const T *c, const T *d, const uint8_t *water, const uint8_t *edge,
+                   const T *b_edge, const T *d_edge, T *out, int *bad_columns, void *stream) {
+  clear_error();
+  if (nsx < 0 || nsy < 0 || nz < 1 || nz > kMaxNz)
+    return fail(VG_ERR_SHAPE, "%s: nsx=%d nsy=%d nz=%d (1 <= nz <= %d)", name, nsx, nsy, nz, kMaxNz);
+  if (!a || !b || !c || !d || !water || !edge || !out) return fail(VG_ERR_ARG, "%s: NULL pointer", name);
+  const long long nsys = (long long)nsx * nsy;
+  if (nsys == 0) return VG_OK;
+  if (nsys > 0x7fffffffLL) return fail(VG_ERR_SHAPE, "%s: too many columns", name);
+  {
+    // the output holds intermediate values while the inputs are still read:
+    // it may not overlap them (element offsets span [lo, hi] in every array)
+    long long lo = 0, hi = 0;
+    for (const long long span : {s_x * (nsx - 1), s_y * (nsy - 1), s_z * (nz - 1)}) (span < 0 ? lo : hi) += span;
+    const long long es = (long long)sizeof(T);
+    const char *o0 = reinterpret_cast<const char *>(out) + lo * es;
+    const char *o1 = reinterpret_cast<const char *>(out) + (hi + 1) * es;
+    auto overlaps = [&](const void *q, long long elem) {
+      if (!q) return false;
+      const char *q0 = static_cast<const char *>(q) + lo * elem;
+      const char *q1 = static_cast<const char *>(q) + (hi + 1) * elem;
+      return q0 < o1 && o0 < q1;
+    };
+    if (overlaps(a, es) || overlaps(b, es) || overlaps(c, es) || overlaps(d, es) || overlaps(b_edge, es) ||
+        overlaps(d_edge, es) || overlaps(water, 1) || overlaps(edge, 1))
+      return fail(VG_ERR_ARG, "%s: out overlaps an input", name);
+  }
+  TriArgs<T> p{nsx, (int)nsys, nz, s_x, s_y, s_z, a, b, c, d, b_edge, d_edge, water, edge, out, bad_columns};
+  // shared doubles per column and level: the eliminated diagonal, and for a
+  // float output also the eliminated right-hand side
+  const size_t per = sizeof(T) == sizeof(double) ? 1 : 2;
+  int nb = kTriMaxThreads;
+  while (nb > 32 && (size_t)nb * nz * per * sizeof(double) > 100 * 1024) nb /= 2;
+  const size_t smem = (size_t)nb * nz * per * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e =
+        cudaFuncSetAttribute(pivoting_solve_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "%s: pivoting_solve_kernel smem: %s", name, cudaGetErrorString(e));
+  }
+  pivoting_solve_kernel<T><<<(unsigned)((nsys + nb - 1) / nb), nb, smem, as_stream(stream)>>>(p);
+  return check_launch("pivoting_solve_kernel");
+}
+
 }  // namespace
 
 }  // namespace vg
@@ -305,39 +373,16 @@ extern "C" int vg_solve_implicit_f64(int nsx, int nsy, int nz, long long s_x, lo
                                      const double *a, const double *b, const double *c, const double *d,
                                      const uint8_t *water, const uint8_t *edge, const double *b_edge,
                                      const double *d_edge, double *out, int *bad_columns, void *stream) {
-  clear_error();
-  if (nsx < 0 || nsy < 0 || nz < 1 || nz > kMaxNz)
-    return fail(VG_ERR_SHAPE, "vg_solve_implicit_f64: nsx=%d nsy=%d nz=%d (1 <= nz <= %d)", nsx, nsy, nz, kMaxNz);
-  if (!a || !b || !c || !d || !water || !edge || !out) return fail(VG_ERR_ARG, "vg_solve_implicit_f64: NULL pointer");
-  const long long nsys = (long long)nsx * nsy;
-  if (nsys == 0) return VG_OK;
-  if (nsys > 0x7fffffffLL) return fail(VG_ERR_SHAPE, "too many columns");
-  {
-    // the output holds intermediate values while the inputs are still read:
-    // it may not overlap them (element offsets span [lo, hi] in every array)
-    long long lo = 0, hi = 0;
-    for (const long long span : {s_x * (nsx - 1), s_y * (nsy - 1), s_z * (nz - 1)}) (span < 0 ? lo : hi) += span;
-    const char *o0 = reinterpret_cast<const char *>(out + lo), *o1 = reinterpret_cast<const char *>(out + hi + 1);
-    auto overlaps = [&](const void *q, size_t elem) {
-      if (!q) return false;
-      const char *q0 = static_cast<const char *>(q) + lo * (long long)elem;
-      const char *q1 = static_cast<const char *>(q) + (hi + 1) * (long long)elem;
-      return q0 < o1 && o0 < q1;
-    };
-    if (overlaps(a, 8) || overlaps(b, 8) || overlaps(c, 8) || overlaps(d, 8) || overlaps(b_edge, 8) ||
-        overlaps(d_edge, 8) || overlaps(water, 1) || overlaps(edge, 1))
-      return fail(VG_ERR_ARG, "vg_solve_implicit_f64: out overlaps an input");
-  }
-  TriArgs p{nsx, (int)nsys, nz, s_x, s_y, s_z, a, b, c, d, b_edge, d_edge, water, edge, out, bad_columns};
-  int nb = kTriMaxThreads;
-  while (nb > 32 && (size_t)nb * nz * sizeof(double) > 100 * 1024) nb /= 2;
-  const size_t smem = (size_t)nb * nz * sizeof(double);
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(pivoting_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pivoting_solve_kernel smem: %s", cudaGetErrorString(e));
-  }
-  pivoting_solve_kernel<<<(unsigned)((nsys + nb - 1) / nb), nb, smem, as_stream(stream)>>>(p);
-  return check_launch("pivoting_solve_kernel");
+  return solve_implicit<double>("vg_solve_implicit_f64", nsx, nsy, nz, s_x, s_y, s_z, a, b, c, d, water, edge,
+                                b_edge, d_edge, out, bad_columns, stream);
+}
+
+extern "C" int vg_solve_implicit_f32(int nsx, int nsy, int nz, long long s_x, long long s_y, long long s_z,
+                                     const float *a, const float *b, const float *c, const float *d,
+                                     const uint8_t *water, const uint8_t *edge, const float *b_edge,
+                                     const float *d_edge, float *out, int *bad_columns, void *stream) {
+  return solve_implicit<float>("vg_solve_implicit_f32", nsx, nsy, nz, s_x, s_y, s_z, a, b, c, d, water, edge,
+                               b_edge, d_edge, out, bad_columns, stream);
 }
 
 extern "C" void vg_tdma_cuda_double(void *stream, void **buffers, const char *opaque, size_t opaque_len) {

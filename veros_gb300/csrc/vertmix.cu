@@ -7,8 +7,11 @@
 //   isoneutral implicit part with kappaH for K_33, diffusion.py:154-164); the
 //   surface forcing enters the top row's right-hand side. dtemp_vmix and
 //   dsalt_vmix are written on the whole array ((new - old)/dt, zero outside
-//   the water columns). Single-process, non-cyclic: the closing boundary
-//   exchange (thermodynamics.py:292-298) is then a no-op.
+//   the water columns). With enable_cyclic_x the call ends with the
+//   reference's closing boundary exchange of the new levels
+//   (thermodynamics.py:292-298) in its single-process form: the periodic
+//   copy of the x halo columns (veros/core/utilities.py:7-16).
+// * vg_enforce_boundaries_f64: that copy on its own for one field.
 // * vg_isoneutral_streamfunction_f64: the GM streamfunction diagnostics B1_gm
 //   and B2_gm (veros/core/isoneutral/isoneutral.py:232-254), elementwise.
 #include "common.cuh"
@@ -184,6 +187,35 @@ __global__ void __launch_bounds__(kVmixThreads) vertmix_kernel(VmixArgs a) {
   }
 }
 
+// enforce_boundaries (veros/core/utilities.py:7-16) on one process:
+// arr[-2:] = arr[2:4], then arr[:2] = arr[-4:-2], for every (j, k) row of up
+// to two fields. One thread per row reads its four source cells before it
+// writes, which is what NumPy's overlap-safe assignment gives for the
+// narrowest domain (X = 5), where the sources and destinations meet; for
+// X >= 6 the two copies touch disjoint cells.
+__global__ void __launch_bounds__(256) cyclic_x_kernel(Layout L, double *f0, double *f1) {
+  const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= (long long)L.Y * L.Z) return;
+  const int j = (int)(row % L.Y), k = (int)(row / L.Y);
+  const int X = L.X;
+  for (int f = 0; f < 2; ++f) {
+    double *p = f == 0 ? f0 : f1;
+    if (!p) continue;
+    double *r = p + L.at(0, j, k);
+    const double s2 = r[2], s3 = r[3], t0 = r[X - 4], t1 = r[X - 3];
+    r[X - 2] = s2;
+    r[X - 1] = s3;
+    r[0] = t0;
+    r[1] = t1;
+  }
+}
+
+int launch_cyclic_x(const Layout &L, double *f0, double *f1, cudaStream_t s) {
+  const long long rows = (long long)L.Y * L.Z;
+  cyclic_x_kernel<<<(unsigned)((rows + 255) / 256), 256, 0, s>>>(L, f0, f1);
+  return check_launch("cyclic_x_kernel");
+}
+
 struct SfArgs {
   Layout L;
   const double *__restrict__ Kgm;
@@ -239,7 +271,7 @@ extern "C" int vg_vertmix_tempsalt_f64(const VgDomain *dom, const VgGrid *grid, 
                                        const double *kappaH, const int32_t *kbot, double *temp_taup1,
                                        double *salt_taup1, const double *forc_temp_surface,
                                        const double *forc_salt_surface, double *dtemp_vmix, double *dsalt_vmix,
-                                       void *stream) {
+                                       int enable_cyclic_x, void *stream) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -272,7 +304,20 @@ extern "C" int vg_vertmix_tempsalt_f64(const VgDomain *dom, const VgGrid *grid, 
   }
   const int ncols = a.L.X * a.L.Y;
   vertmix_kernel<<<(ncols + nb - 1) / nb, nb, smem, as_stream(stream)>>>(a);
-  return check_launch("vertmix_kernel");
+  st = check_launch("vertmix_kernel");
+  if (st || !enable_cyclic_x) return st;
+  // thermodynamics.py:292-298: after dtemp_vmix / dsalt_vmix, so the
+  // tendencies keep the halo columns' (new - old) / dt of the solve
+  return launch_cyclic_x(a.L, temp_taup1, salt_taup1, as_stream(stream));
+}
+
+extern "C" int vg_enforce_boundaries_f64(const VgDomain *dom, double *arr, int enable_cyclic_x, void *stream) {
+  clear_error();
+  int st = validate_domain(dom);
+  if (st) return st;
+  if (!arr) return fail(VG_ERR_ARG, "vg_enforce_boundaries_f64: NULL pointer argument");
+  if (!enable_cyclic_x) return VG_OK;
+  return launch_cyclic_x(layout_of(dom), arr, nullptr, as_stream(stream));
 }
 
 extern "C" int vg_isoneutral_streamfunction_f64(const VgDomain *dom, const double *K_gm, const double *Ai_ez,

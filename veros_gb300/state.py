@@ -11,6 +11,7 @@ element size, as the tensor-memory-access engine requires). Time levels and
 tensor components are whole x-y-z blocks.
 """
 
+import warnings
 from collections import namedtuple
 
 import numpy as np
@@ -33,7 +34,23 @@ FIELDS_Z = ("dzt", "dzw", "zt")
 
 SETTING_NAMES = ("iso_slopec", "iso_dslope", "K_iso_steep", "dt_tracer", "grav", "rho_0",
                  "eq_of_state_type", "enable_conserve_energy", "enable_skew_diffusion",
-                 "enable_neutral_diffusion")
+                 "enable_neutral_diffusion", "enable_cyclic_x")
+
+
+def require_single_process(what):
+    """Raise ``NotImplementedError`` when an imported Veros runs on several
+    processes (``runtime_state.proc_num > 1``, veros/runtime.py:183): ``what``
+    would need the domain decomposition's halo exchange
+    (veros/core/utilities.py:18-20), which this one-GPU library does not
+    perform. Without an importable Veros there is one process."""
+    try:
+        from veros import runtime_state
+
+        nproc = int(runtime_state.proc_num)
+    except Exception:
+        return
+    if nproc > 1:
+        raise NotImplementedError(f"{what}: {nproc} processes; the GPU drop-in runs one process per domain")
 
 
 def KernelOutput(**kwargs):
@@ -224,18 +241,26 @@ class DeviceState:
             st.upload(n, np.asarray(arr))
         return st
 
+    # bytes moved by upload() / download() in this process (host <-> device)
+    transfer_bytes = {"h2d": 0, "d2h": 0}
+
     def upload(self, name, arr):
         dst = getattr(self.variables, name)
-        src = torch.from_numpy(np.ascontiguousarray(arr))
+        src = np.ascontiguousarray(arr)
+        with warnings.catch_warnings():  # read-only host arrays (the NumPy backend's) are only read here
+            warnings.simplefilter("ignore", UserWarning)
+            src = torch.from_numpy(src)
         if src.dtype != dst.dtype:
             src = src.to(dst.dtype)
         dst.copy_(src, non_blocking=False)
+        DeviceState.transfer_bytes["h2d"] += src.numel() * src.element_size()
         if name in FIELDS_MASK:
             self._mask_version = None
 
     def download(self, name):
         t = getattr(self.variables, name)
         if isinstance(t, torch.Tensor):
+            DeviceState.transfer_bytes["d2h"] += t.numel() * t.element_size()
             return t.detach().cpu().contiguous().numpy()
         return t
 

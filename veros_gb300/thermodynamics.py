@@ -3,12 +3,21 @@
 follows the isoneutral step: returns ``KernelOutput(dtemp_vmix, temp,
 dsalt_vmix, salt)`` like the reference kernel. ``state`` is a
 :class:`DeviceState` (in place on the GPU) or a NumPy ``VerosState``.
+
+The reference ends with ``enforce_boundaries`` of the new temp and salt
+levels (thermodynamics.py:292-298): on one process, with
+``settings.enable_cyclic_x``, the periodic copy of the x halo columns
+(veros/core/utilities.py:7-16), which the CUDA call performs; across several
+processes it is the halo exchange of the domain decomposition
+(utilities.py:18-20), which this single-GPU library does not do, so a
+multi-process run raises ``NotImplementedError`` instead of returning stale
+halos.
 """
 
 import torch
 
 from . import _capi
-from .state import DeviceState, KernelOutput
+from .state import DeviceState, KernelOutput, require_single_process
 
 
 def run_vertmix(dev):
@@ -25,11 +34,13 @@ def run_vertmix(dev):
                                      v.kbot.data_ptr(), v.temp[..., v.taup1].data_ptr(),
                                      v.salt[..., v.taup1].data_ptr(), v.forc_temp_surface.data_ptr(),
                                      v.forc_salt_surface.data_ptr(), v.dtemp_vmix.data_ptr(), v.dsalt_vmix.data_ptr(),
+                                     int(bool(dev.settings.get("enable_cyclic_x", False))),
                                      torch.cuda.current_stream(dev.device).cuda_stream)
     _capi.check(st, "vertmix_tempsalt")
 
 
 def vertmix_tempsalt(state):
+    require_single_process("vertmix_tempsalt (its closing halo exchange)")
     names = ("dtemp_vmix", "temp", "dsalt_vmix", "salt")
     if isinstance(state, DeviceState):
         run_vertmix(state)
