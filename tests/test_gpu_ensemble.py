@@ -90,3 +90,36 @@ def test_graph_replay_matches_eager_and_autotune_runs():
     _assert_same(batched, eager)
     e1.close()
     e2.close()
+
+
+def test_members_against_the_oracle_at_their_own_shapes():
+    """Each member of an uneven ensemble against one oracle step (the reference
+    algorithm) from the same state, at its own extents: the smallest shapes of
+    the benchmark's member distribution (nx = ny = 32 with 15 levels), a
+    60-level member, and odd extents. Relative max-norm 1e-12 per field, as
+    for the single-domain drop-in; land cells exactly zero."""
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300 import synthetic
+    from veros_gb300.ensemble import Ensemble
+    from veros_gb300.state import DeviceState
+
+    from conftest import assert_field_close
+
+    shapes = [(32, 32, 15), (41, 33, 60), (70, 37, 30), (32, 45, 45)]
+    hosts = [synthetic.make_state(nx, ny, nz, seed=40 + m, eq_of_state_type=3, land_fraction=0.3, dz_bottom=250.0)
+             for m, (nx, ny, nz) in enumerate(shapes)]
+    devs = [DeviceState.from_host(h) for h in hosts]
+    ens = Ensemble(devs)
+    ens.step(1)
+    torch.cuda.synchronize()
+    for h, dev in zip(hosts, devs):
+        vs = orc.OracleState({k: v.copy() for k, v in h.arrays.items()})
+        orc.isoneutral_step(vs, h.settings)
+        dt = h.settings["dt_tracer"]
+        for n in FIELDS:
+            ref = getattr(vs, n)
+            tracer = vs.temp if n == "dtemp_iso" else vs.salt if n == "dsalt_iso" else None
+            assert_field_close(n, dev.download(n), ref, tracer=tracer, dt=dt)
+        land = ~h.arrays["maskT"].astype(bool)
+        assert np.all(dev.download("dtemp_iso")[land] == 0.0)
+    ens.close()

@@ -559,3 +559,37 @@ def test_vertmix_on_synthetic_state_vs_oracle():
     for n, tr in (("temp", None), ("salt", None), ("dtemp_vmix", "temp"), ("dsalt_vmix", "salt")):
         name = {"dtemp_vmix": "dtemp_iso", "dsalt_vmix": "dsalt_iso"}.get(n, n)
         assert_field_close(name, dev.download(n), out[n], tracer=None if tr is None else out[tr], dt=dt)
+
+
+@pytest.mark.parametrize("case", ["iso_random_energy", "iso_random_noenergy"])
+def test_diffusion_with_tensors_not_written_by_pre(case):
+    """The diffusion on the reference's random state without pre first: the
+    tensor fields are random on every face, dry ones included, as a caller
+    may pass them. The flux kernel orders its columns by their first wet level
+    and skips the FP64 work of dry faces only where their coefficients are
+    zero, so fluxes through dry faces with non-zero coefficients must still
+    enter the neighbouring wet cells as in the reference (which multiplies the
+    divergence by maskT, not the fluxes by the face masks)."""
+    from oracle import isoneutral_oracle as orc
+    from veros_gb300.isoneutral import run_diffusion
+
+    g = load_golden(case)
+    dev = _golden_device_state(g)
+    arrays = {k[3:]: v.copy() for k, v in g.items() if k.startswith("in_")}
+    settings = {k[8:]: v.item() for k, v in g.items() if k.startswith("setting_")}
+    vs = orc.OracleState(arrays, tau=int(g["tau"]), taup1=int(g["taup1"]), taum1=int(g["taum1"]))
+    # dry faces really carry non-zero coefficients here
+    dry_u = ~arrays["maskU"][1:-2, 2:-2]
+    assert np.any(arrays["Ai_ez"][1:-2, 2:-2][dry_u] != 0.0)
+    dt = float(settings["dt_tracer"])
+    for istemp, name in ((True, "temp"), (False, "salt")):
+        run_diffusion(dev, istemp)
+        torch.cuda.synchronize()
+        out = orc.isoneutral_diffusion(vs, settings, istemp)
+        vs.__dict__.update(out)
+        dname = "dtemp_iso" if istemp else "dsalt_iso"
+        for n in (name, dname):
+            assert_field_close(n, dev.download(n), out[n], tracer=out[name], dt=dt)
+        if "P_diss_iso" in out:
+            pf = p_diss_floor({**arrays, "temp": vs.temp, "salt": vs.salt}, settings, int(g["tau"]))
+            assert_field_close("P_diss_iso", dev.download("P_diss_iso"), out["P_diss_iso"], floor=pf)

@@ -45,6 +45,27 @@ inline int span_ctas(K kernel, int threads, size_t smem, int ntiles, int Z, int 
   return (int)std::max(1LL, std::min(slots, by_units));
 }
 
+// Index of this thread's "virtual" warp for kernels that hand their work to
+// warps in a priority order (the busiest entries to virtual warp 0). Warp
+// slot w of an SM issues on sub-partition w % 4, so co-resident CTAs whose
+// busy warps have the same index would share the sub-partitions' FP64 pipes
+// while others idle; the CTA's warp-slot base (%warpid of its warp 0, shared
+// by the caller through shared memory) rotates the order so that the CTA in
+// slot group g starts on sub-partition g * nw / 4. Only a performance
+// choice: any permutation of the work over the warps gives the same results.
+__device__ __forceinline__ unsigned hw_warp_slot() {
+  unsigned w;
+  asm volatile("mov.u32 %0, %%warpid;" : "=r"(w));
+  return w;
+}
+__device__ __forceinline__ int virtual_warp(int warp, int nw, unsigned slot0) {
+  // virtual warp v runs on physical warp p = v + c (mod nw), whose
+  // sub-partition (slot0 + p) % 4 is then (v + g * nw / 4) % 4
+  const int g = (int)(slot0 / (unsigned)nw);
+  const int c = ((g * (nw / 4) - (int)(slot0 % 4u)) % nw + nw) % nw;
+  return (warp - c + nw) % nw;
+}
+
 struct Layout {
   int X, Y, Z;
   long long pitch, plane;

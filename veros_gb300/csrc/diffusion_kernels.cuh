@@ -200,26 +200,133 @@ __device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long lo
                        __ldg(tr + o + P) - tc, __ldg(tr + o + P + Q) - tcu);
 }
 
+// Dynamic shared memory of flux_div_body: 1/(4 dzt) and 1/dzt per level, then
+// a (Z + 1)-entry int table for the wet-point ordering.
+inline size_t flux_smem_bytes(int Z) { return 2 * (size_t)Z * sizeof(double) + ((size_t)Z + 1) * sizeof(int); }
+
+// True if any of n values loaded at p + off[m] is non-zero (either sign of
+// zero counts as zero), by integer operations on the bit patterns.
+template <typename F>
+__device__ __forceinline__ bool any_nonzero(const F *p, long long o, const long long *off, int n) {
+  unsigned long long acc = 0;
+  for (int m = 0; m < n; ++m) {
+    const F v = ld(p, o + off[m]);
+    if constexpr (sizeof(F) == 8)
+      acc |= (unsigned long long)__double_as_longlong((double)v) << 1;
+    else
+      acc |= (unsigned long long)(__float_as_uint((float)v) << 1);
+  }
+  return acc != 0;
+}
+
 // One tile (bx, by) and levels [kb, ke) of NTR tracers of one domain; the whole CTA
 // (32 x TY threads) takes part. A[0..NTR-1] differ only in their tracer
 // fields; geometry, tensor and masks come from A[0]. zq_dzt: dynamic shared
-// memory of 2 Z doubles.
+// memory of flux_smem_bytes(Z).
+//
+// Wet-point ordering. An FP64 warp instruction holds the FP64 pipe for its
+// whole warp however few lanes are active, and on random topography most
+// warps have a few wet and many dry columns on most levels. So the threads
+// take the tile's columns in the order of their first level in [kb, ke) with
+// a mask bit set (stable, one warp's counting sort): on each level the
+// columns with a mask bit so far form a prefix of the order, and whole warps
+// of dry columns skip the FP64 work. A column runs the full computation from
+// its first wet level on (its carried values start there as at a segment
+// start). Before it, the divergence is zero (maskT multiplies it), and the
+// fluxes through its east, north and top faces are zero wherever their
+// tensor coefficients are, as isoneutral_diffusion_pre writes them for a
+// face whose mask is zero; a dry column checks that on the bit patterns of
+// the coefficients and computes any face whose coefficients are not zero
+// from freshly loaded tracers, so the result is the reference's for any
+// tensor. The arithmetic of every face and cell is the same in all paths.
+// Only the FP64 form orders its columns: the split form's fluxes are FP32,
+// whose pipe the dry lanes hardly load, and the ordering would cost it more
+// than it saves (measured 0.13 ms slower per step at 1 degree).
 template <typename F, int TY, int NTR>
 __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_dzt, int bx, int by, int kb, int ke) {
   constexpr int NT = TX * TY;
   __shared__ F fe_s[2][NTR][TY][TX + 1];  // east faces i0-1 .. i0+TX-1
   __shared__ F fn_s[2][NTR][TY + 1][TX];  // north faces j0-1 .. j0+TY-1
+  __shared__ short okey[NT], olist[NT];
+  __shared__ unsigned slot0;  // %warpid of warp 0 (virtual_warp)
   const DiffArgs<F> &a = A[0];
   const Layout &L = a.L;
   const int Z = L.Z;
   double *zinv_dzt = zq_dzt + Z;  // 1/(4 dzt[k]) then 1/dzt[k]
-  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX, warp = tid / 32, lane = tid % 32;
+  int *hist = reinterpret_cast<int *>(zq_dzt + 2 * Z);
+  const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const int i0 = 2 + bx * TX, j0 = 2 + by * TY;
+  const int nkeys = ke - kb + 1;
   for (int k = tid; k < Z; k += NT) {
     zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
     zinv_dzt[k] = 1.0 / a.g.dzt[k];
   }
+  constexpr bool kOrder = sizeof(F) == sizeof(double);
+  if (kOrder) {
+    for (int n = tid; n < nkeys; n += NT) hist[n] = 0;
+    // fluxes of faces nobody computes on a level are zero
+    for (int n = tid; n < 2 * NTR * TY * (TX + 1); n += NT) (&fe_s[0][0][0][0])[n] = F(0);
+    for (int n = tid; n < 2 * NTR * (TY + 1) * TX; n += NT) (&fn_s[0][0][0][0])[n] = F(0);
+  }
+  if (kOrder) {
+    // the first level of [kb, ke) with a mask bit of the column (ke - kb if none)
+    const int ci = i0 + tid % TX, cj = j0 + tid / TX;
+    int f = ke;
+    if (ci < L.X - 2 && cj < L.Y - 2) {
+      const uint8_t *mp = a.m + L.at(ci, cj, 0);
+      for (int l0 = kb; l0 < ke && f >= ke; l0 += 8) {
+        unsigned v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = l0 + u < ke ? __ldg(mp + (long long)(l0 + u) * L.plane) : 0u;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (f >= ke && v[u]) f = l0 + u;
+      }
+    }
+    okey[tid] = (short)(f - kb);
+    __syncthreads();
+    atomicAdd(&hist[okey[tid]], 1);
+  } else {
+    okey[tid] = 0;  // every column from the segment's first level, in tile order
+    olist[tid] = (short)tid;
+  }
+  if (tid == 0) slot0 = hw_warp_slot();
   __syncthreads();
+  if (kOrder && warp == 0) {
+    // exclusive prefix sums of the key histogram, then the stable scatter
+    int run = 0;
+    for (int c0 = 0; c0 < nkeys; c0 += 32) {
+      const int v = c0 + lane < nkeys ? hist[c0 + lane] : 0;
+      int x = v;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+      }
+      if (c0 + lane < nkeys) hist[c0 + lane] = run + x - v;
+      run += __shfl_sync(0xffffffffu, x, 31);
+    }
+    __syncwarp();
+    for (int c0 = 0; c0 < NT; c0 += 32) {
+      const int idx = c0 + lane;
+      const int kk = okey[idx];
+      const unsigned grp = __match_any_sync(0xffffffffu, kk);
+      const int leader = __ffs(grp) - 1;
+      const int rank = __popc(grp & ((1u << lane) - 1u));
+      int base = lane == leader ? hist[kk] : 0;
+      base = __shfl_sync(0xffffffffu, base, leader);
+      olist[base + rank] = (short)idx;
+      __syncwarp();
+      if (lane == leader) hist[kk] = base + __popc(grp);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // the busiest columns go to virtual warp 0 (virtual_warp spreads co-resident CTAs' busy warps
+  // over the sub-partitions); the split form keeps the tile order
+  const int oe = kOrder ? olist[virtual_warp(warp, NT / 32, slot0) * 32 + lane] : olist[tid];
+  const int kact = kb + okey[oe];  // first level with a mask bit (ke: none)
+  const int tx = oe % TX, ty = oe / TX;
 
   const int i = i0 + tx, j = j0 + ty;
   const bool own = i < L.X - 2 && j < L.Y - 2;
@@ -249,7 +356,8 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   // differences t(k) - t(k-1) (0 at k = 0, edge padding), and the four
   // horizontal differences around the own point; each level loads the level
   // above once and forms its differences once. The K pair sums of the east
-  // and north faces are carried the same way.
+  // and north faces are carried the same way. They start on the column's
+  // first wet level (start_column), as on a segment's first level.
   const long long P = L.pitch, Q = L.plane;
   double vc[NTR], ve[NTR], vn[NTR];     // values at level k
   double dzc[NTR], dze[NTR], dzn[NTR];  // t(k) - t(k-1)
@@ -261,8 +369,8 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     ft_prev[r] = 0.0;
     vc[r] = ve[r] = vn[r] = dzc[r] = dze[r] = dzn[r] = hw[r] = hs[r] = he[r] = hn[r] = 0.0;
   }
-  if (own) {
-    const long long ob = L.at(i, j, kb);
+  auto start_column = [&](int k0) {
+    const long long ob = L.at(i, j, k0);
 #pragma unroll
     for (int r = 0; r < NTR; ++r) {
       const double *tr = A[r].tr;
@@ -273,14 +381,14 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       hs[r] = vc[r] - __ldg(tr + ob - P);
       he[r] = ve[r] - vc[r];
       hn[r] = vn[r] - vc[r];
-      if (kb > 0) {
+      if (k0 > 0) {
         dzc[r] = vc[r] - __ldg(tr + ob - Q);
         dze[r] = ve[r] - __ldg(tr + ob + 1 - Q);
         dzn[r] = vn[r] - __ldg(tr + ob + P - Q);
       }
     }
-    if (kb > 0) {
-      const long long op = L.at(i, j, kb - 1);
+    if (k0 > 0) {
+      const long long op = L.at(i, j, k0 - 1);
       const F kd = ld(a.K, op);
       pe_below = kd + ld(a.K, op + 1);
       pn_below = kd + ld(a.K, op + P);
@@ -289,7 +397,10 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
 #pragma unroll
       for (int r = 0; r < NTR; ++r) ft_prev[r] = top_flux(L, A[r].tr, op, ct);
     }
-  }
+  };
+  // offsets of a face's tensor coefficients: the four (p, r) components and the K_11 / K_22 factor
+  const long long ai_off[4] = {0, a.sp, a.sr, a.sp + a.sr};
+  const long long k_off[1] = {0};
 
   for (int k = kb; k < ke; ++k) {
     // double-buffered exchange: the barrier of level k+1 orders level k's
@@ -300,7 +411,8 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     F fe[NTR], fn[NTR], ft[NTR];
 #pragma unroll
     for (int r = 0; r < NTR; ++r) fe[r] = fn[r] = ft[r] = 0.0;
-    if (own) {
+    if (own && k >= kact) {
+      if (k == kact) start_column(k);
       const bool up = k < Z - 1;
       double uc[NTR], ue[NTR], un[NTR], uw[NTR], us[NTR];  // level k+1
 #pragma unroll
@@ -347,6 +459,35 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
         hs[r] = hs1;
         he[r] = he1;
         hn[r] = hn1;
+      }
+    } else if (own) {
+      // no mask bit on this column yet: faces with non-zero coefficients only
+      if (any_nonzero(a.Aez, o, ai_off, 4) || any_nonzero(a.K11, o, k_off, 1)) {
+        F ce[6];
+        const F pe = ld(a.K, o) + ld(a.K, o + 1);
+        const F peb = k >= 1 ? ld(a.K, o - Q) + ld(a.K, o + 1 - Q) : F(0);
+        east_coef(a, o, face_diffloc(pe, peb, k, a.s1), inv_cost_dxu, qz, ce);
+#pragma unroll
+        for (int r = 0; r < NTR; ++r) fe[r] = east_flux(L, A[r].tr, o, k, ce);
+      }
+      if (any_nonzero(a.Anz, o, ai_off, 4) || any_nonzero(a.K22, o, k_off, 1)) {
+        F cn[6];
+        const F pn = ld(a.K, o) + ld(a.K, o + P);
+        const F pnb = k >= 1 ? ld(a.K, o - Q) + ld(a.K, o + P - Q) : F(0);
+        north_coef(a, o, face_diffloc(pn, pnb, k, a.s1), inv_dyu, qz, cn);
+#pragma unroll
+        for (int r = 0; r < NTR; ++r) fn[r] = north_flux(L, A[r].tr, o, k, cn, cosu_c);
+      }
+      if (k < Z - 1 && (any_nonzero(a.Abx, o, ai_off, 4) || any_nonzero(a.Aby, o, ai_off, 4))) {
+        F ct[10];
+        top_coef(a, o, qx_cost, q_dyt_cost, cosu_s, cosu_c, ct);
+#pragma unroll
+        for (int r = 0; r < NTR; ++r) ft[r] = top_flux(L, A[r].tr, o, ct);
+      }
+    }
+    if (own) {
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
         fe_s[b][r][ty][tx + 1] = fe[r];
         fn_s[b][r][ty + 1][tx] = fn[r];
       }
@@ -370,7 +511,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce);
     }
     __syncthreads();
-    if (own && (__ldg(a.m + o) & VG_MASK_T)) {  // maskT multiplies the divergence (diffusion.py:123-137)
+    if (own && k >= kact && (__ldg(a.m + o) & VG_MASK_T)) {  // maskT multiplies the divergence (diffusion.py:123-137)
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
         const DiffArgs<F> &t = A[r];
@@ -579,9 +720,10 @@ __global__ void __launch_bounds__(64) implicit_kernel(DiffArgs<F> a, DiffArgs<F>
 // values to the column's slot) and each eliminates its own tracer, so twice
 // as many warps hide the recurrence's latency for the same shared memory
 // per column. The arithmetic of each tracer is that of implicit_kernel<F, 2>.
+// The body of one CTA of the pair solve: column block cb of blockDim.x / 2
+// columns. Also run by the batched ensemble's persistent CTAs.
 template <typename F>
-__global__ void __launch_bounds__(128) implicit_pair_kernel(DiffArgs<F> a, DiffArgs<F> b2) {
-  extern __shared__ double smem[];
+__device__ __forceinline__ void implicit_pair_body(const DiffArgs<F> &a, const DiffArgs<F> &b2, double *smem, int cb) {
   const Layout &L = a.L;
   const int Z = L.Z;
   const int ncols_x = L.X - 4, ncols = ncols_x * (L.Y - 4);
@@ -595,13 +737,19 @@ __global__ void __launch_bounds__(128) implicit_pair_kernel(DiffArgs<F> a, DiffA
     inv_dzt[k] = 1.0 / a.g.dzt[k];
   }
   __syncthreads();
-  const int slot = blockIdx.x * nc + c;
+  const int slot = cb * nc + c;
   const int col = a.col_order ? (slot < ncols ? __ldg(a.col_order + slot) : ncols) : slot;
   const int i = 2 + col % ncols_x;
   const int j = 2 + col / ncols_x;
   const int ks = (unsigned)col < (unsigned)ncols ? a.kbot[L.at2(i, j)] - 1 : -1;  // create_water_masks (utilities.py:38-48)
   const DiffArgs<F> &own = r ? b2 : a;
   if (ks >= 0 && ks < Z) implicit_column<F, 1>(own, own, dtdzw, inv_dzt, cps + c, nc, dps + t, nb, i, j, ks);
+}
+
+template <typename F>
+__global__ void __launch_bounds__(128) implicit_pair_kernel(DiffArgs<F> a, DiffArgs<F> b2) {
+  extern __shared__ double smem[];
+  implicit_pair_body<F>(a, b2, smem, blockIdx.x);
 }
 
 // Energy branch (veros/core/isoneutral/diffusion.py:234-281 with

@@ -10,6 +10,15 @@
 // four launches plus one counter reset, so a rollout captures into a CUDA
 // graph. Tile height (columns per CTA), k-chunk and solver CTA size are
 // tuning parameters chosen by the caller (the Python autotuner).
+//
+// Why four launches and not one: every stage reads what the previous one
+// wrote around each tile (pre reads the new tracer level of the neighbouring
+// columns, the fluxes read the slopes and tensors of the tile's halo faces,
+// the solve the explicit update of its column), so one persistent launch
+// would need per-tile ready flags and spinning CTAs. Inside a CUDA graph a
+// stage boundary costs a few microseconds against a step of tens of
+// milliseconds, and each stage's work list is long enough (thousands of
+// items over the resident CTAs) that its tail is short.
 #include <algorithm>
 #include <vector>
 
@@ -149,17 +158,19 @@ __global__ void __launch_bounds__(32 * TY, 2) flux_batched_shares(const MemberAr
   }
 }
 
+// temp and salt of a column on two threads (implicit_pair_body): a CTA of
+// 2 x solve_threads threads solves one block of solve_threads columns per item
 template <typename F>
-__global__ void __launch_bounds__(64) implicit_batched(const MemberArgs<F> *__restrict__ members,
-                                                       const WorkItem *__restrict__ items, int nitems,
-                                                       int *counter) {
+__global__ void __launch_bounds__(128) implicit_batched(const MemberArgs<F> *__restrict__ members,
+                                                        const WorkItem *__restrict__ items, int nitems,
+                                                        int *counter) {
   extern __shared__ double smem[];
   __shared__ DiffArgs<F> t, s;
   WorkItem w;
   while (next_item(counter, nitems, items, w)) {
     stage(&t, &members[w.member].dT);
     stage(&s, &members[w.member].dS);
-    implicit_body<F, 2>(t, s, smem, w.a);
+    implicit_pair_body<F>(t, s, smem, w.a);
   }
 }
 
@@ -310,7 +321,7 @@ struct Ensemble : EnsembleBase {
     tun = t;
     int st;
     smem_pre = t.pre_rows == 4 ? pre_smem_bytes<F, 4>(maxZ) : pre_smem_bytes<F, 8>(maxZ);
-    smem_flux = 2 * (size_t)maxZ * sizeof(double);
+    smem_flux = flux_smem_bytes(maxZ);
     smem_solve = (2 * (size_t)maxZ + 3 * (size_t)maxZ * t.solve_threads) * sizeof(double);
     const bool ps = t.pre_kchunk < 0, fs = t.flux_kchunk < 0;
     if (t.pre_rows == 4)
@@ -327,7 +338,7 @@ struct Ensemble : EnsembleBase {
       st = fs ? occupancy_grid(flux_batched_shares<F, 8>, 256, smem_flux, grid_flux)
               : occupancy_grid(flux_batched<F, 8>, 256, smem_flux, grid_flux);
     if (st) return st;
-    if ((st = occupancy_grid(implicit_batched<F>, t.solve_threads, smem_solve, grid_solve))) return st;
+    if ((st = occupancy_grid(implicit_batched<F>, 2 * t.solve_threads, smem_solve, grid_solve))) return st;
     if ((st = occupancy_grid(prepare_batched<F>, 256, 0, grid_prep))) return st;
     return build_lists();  // the equal shares are cut for the CTA counts above
   }
@@ -364,8 +375,8 @@ struct Ensemble : EnsembleBase {
       flux_batched<F, 8><<<gf, 256, smem_flux, s>>>(args, d_flux, n_flux, d_counter + 2, tun.flux_kchunk);
     }
     if ((st = check_launch("flux_batched"))) return st;
-    implicit_batched<F><<<std::min(grid_solve, n_solve), tun.solve_threads, smem_solve, s>>>(args, d_solve, n_solve,
-                                                                                           d_counter + 3);
+    implicit_batched<F><<<std::min(grid_solve, n_solve), 2 * tun.solve_threads, smem_solve, s>>>(
+        args, d_solve, n_solve, d_counter + 3);
     return check_launch("implicit_batched");
   }
 };

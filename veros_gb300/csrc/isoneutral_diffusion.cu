@@ -19,7 +19,7 @@ template <typename F, int NTR>
 int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
   constexpr int TY = 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
-  const size_t smem = 2 * (size_t)a.L.Z * sizeof(double);
+  const size_t smem = flux_smem_bytes(a.L.Z);
   const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, nbx * nby, a.L.Z, 8);
   if (nc < 1) return fail(VG_ERR_LAUNCH, "flux_span_kernel: occupancy query failed");
   a.kchunk = b.kchunk = a.L.Z;

@@ -104,12 +104,58 @@ struct Smem {
   // cosu(j-1+jp) dyu(j-1+jp) / (4 dyt(j) cost(j)) by thread row
   double dqx[2][PX], dqy[2][PY];
   uint8_t qm[2][NP];
-  // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant
+  // wet-point ordering of the segment (see pre_tile_body): per plane point
+  // the key (first level with a mask bit, counted from the segment's first
+  // plane level), the plane points in key order, and the same for the own
+  // points, whose key also covers their west and south neighbours
+  short pkey[NP], plist[NP];
+  short ukey[NP], vkey[NP];  // per plane point: first level with its U / V mask bit
+  short okey[Tile<TY>::NT], olist[Tile<TY>::NT];
+  unsigned slot0;  // %warpid of warp 0 (virtual_warp)
+  // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant; then
+  // two (Z + 2)-entry int tables for the key histograms / running offsets
 };
 
 template <typename F, int TY>
 constexpr size_t pre_smem_bytes(int Z) {
-  return sizeof(Smem<F, TY>) + 4 * (size_t)Z * sizeof(double);
+  return sizeof(Smem<F, TY>) + 4 * (size_t)Z * sizeof(double) + 2 * ((size_t)Z + 2) * sizeof(int);
+}
+
+// Stable counting sort of n small keys (0 <= key < nkeys) by one warp:
+// list[] receives the indices 0..n-1 in key order, equal keys in index
+// order. off[] holds the exclusive prefix sums of the key histogram on entry
+// and is advanced as the indices are placed. Lanes sharing a key within a
+// chunk of 32 take consecutive slots after the group's running offset.
+__device__ __forceinline__ void warp_stable_scatter(const short *key, int n, int *off, short *list, int lane) {
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int idx = c0 + lane;
+    const int kk = idx < n ? key[idx] : -1;
+    const unsigned grp = __match_any_sync(0xffffffffu, kk);
+    const int leader = __ffs(grp) - 1;
+    const int rank = __popc(grp & ((1u << lane) - 1u));
+    int base = (lane == leader && kk >= 0) ? off[kk] : 0;
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (kk >= 0) list[base + rank] = (short)idx;
+    __syncwarp();
+    if (lane == leader && kk >= 0) off[kk] = base + __popc(grp);
+    __syncwarp();
+  }
+}
+
+// In-place exclusive prefix sum of h[0..n) by one warp.
+__device__ __forceinline__ void warp_exclusive_scan(int *h, int n, int lane) {
+  int run = 0;
+  for (int c0 = 0; c0 < n; c0 += 32) {
+    const int v = c0 + lane < n ? h[c0 + lane] : 0;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (c0 + lane < n) h[c0 + lane] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
 }
 
 template <typename F>
@@ -222,7 +268,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   double *zeos = zq_dzt + Z;
 
   const int tid = threadIdx.x;
-  const int tx = tid % TX, ty = tid / TX;
+  const int warp = tid / 32, lane = tid % 32;
   const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
 
   // ---- per-CTA grid tables ------------------------------------------------
@@ -276,7 +322,92 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   const double eos_c1 = a.eos_type == 3 ? -Eos::betaTs3 * Eos::rho0
                         : a.eos_type == 1 ? 0.0
                                           : -2.0 * Eos::betaTs24 * Eos::rho0;
+
+  // ---- wet-point ordering of the segment -----------------------------------
+  // An FP64 warp instruction holds the FP64 pipe for its whole warp, however
+  // few of its lanes are active, and on a dry level a point's work reduces to
+  // constants. So the threads take the points in the order of the level from
+  // which on they carry work: a point's key is its first level in [lo, hi]
+  // with a mask bit set (hi - lo + 1 if none); an own point's key is the least
+  // of its own key and the first levels with the U mask bit of its west
+  // neighbour and the V mask bit of its south neighbour (the faces it shares
+  // with them, through which they read its west and south slopes). With the
+  // masks of a Veros grid those faces are wet only where the point is, so an
+  // own point's key is its first wet level. From its key on a point runs the full
+  // computation on every level; before it, its plane quantities are those of
+  // a point without mask bits (the constants filled in here) and it has no
+  // faces to write but zeros. The arithmetic of every point is unchanged, so
+  // results do not depend on the order. On each level the active points are a
+  // prefix of the order, so whole warps of dry points skip the FP64 work.
+  const int lo = max(kb - 1, 0), hi = min(ke, Z - 1), nkeys = hi - lo + 2;
+  int *hist_p = reinterpret_cast<int *>(zeos + Z), *hist_o = hist_p + (Z + 2);
+  {
+    // plane quantities of a point without mask bits on this level and the one below
+    const F rdry = to_F<F>(recip_neg(clamp_eps(0.0)));
+    for (int n = tid; n < nkeys; n += NT) hist_p[n] = hist_o[n] = 0;
+    for (int p = tid; p < NP; p += NT) {
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        sm.q[b][Q_RT][p] = sm.q[b][Q_RS][p] = F(0);
+        sm.q[b][Q_TX][p] = sm.q[b][Q_SX][p] = sm.q[b][Q_TY][p] = sm.q[b][Q_SY][p] = F(0);
+        sm.q[b][Q_R0][p] = sm.q[b][Q_R1][p] = rdry;
+        sm.qm[b][p] = 0;
+      }
+      const int i = i0 - 1 + p % PX, j = j0 - 1 + p / PX;
+      int f = hi + 1, fu = hi + 1, fv = hi + 1;  // first level with any mask bit, with U, with V
+      if (i < L.X && j < L.Y) {
+        const uint8_t *mp = a.m + L.at(i, j, 0);
+        for (int l0 = lo; l0 <= hi; l0 += 16) {
+          unsigned v[16];
+#pragma unroll
+          for (int u = 0; u < 16; ++u) v[u] = l0 + u <= hi ? __ldg(mp + (long long)(l0 + u) * L.plane) : 0u;
+          int cf = hi + 1, cu = hi + 1, cv = hi + 1;  // first of this chunk of levels
+#pragma unroll
+          for (int u = 15; u >= 0; --u) {
+            if (v[u]) cf = l0 + u;
+            if (v[u] & VG_MASK_U) cu = l0 + u;
+            if (v[u] & VG_MASK_V) cv = l0 + u;
+          }
+          f = min(f, cf);
+          fu = min(fu, cu);
+          fv = min(fv, cv);
+          if (f <= hi && fu <= hi && fv <= hi) break;
+        }
+      }
+      sm.pkey[p] = (short)(f - lo);
+      sm.ukey[p] = (short)(fu - lo);
+      sm.vkey[p] = (short)(fv - lo);
+    }
+  }
   __syncthreads();
+  {
+    const int e = tid, pce = (e / TX + 1) * PX + e % TX + 1;
+    const short k = min(sm.pkey[pce], min(sm.ukey[pce - 1], sm.vkey[pce - PX]));
+    sm.okey[e] = k;
+    atomicAdd(&hist_o[k], 1);
+  }
+  for (int p = tid; p < NP; p += NT) atomicAdd(&hist_p[sm.pkey[p]], 1);
+  if (tid == 0) sm.slot0 = hw_warp_slot();
+  __syncthreads();
+  if (warp == 0) warp_exclusive_scan(hist_p, nkeys, lane);
+  else if (warp == 1) warp_exclusive_scan(hist_o, nkeys, lane);
+  __syncthreads();
+  if (warp == 0) warp_stable_scatter(sm.pkey, NP, hist_p, sm.plist, lane);
+  else if (warp == 1) warp_stable_scatter(sm.okey, NT, hist_o, sm.olist, lane);
+  __syncthreads();
+  // this thread's plane points (compute_plane) and own point (slopes, faces), with their keys;
+  // the busiest entries go to virtual warp 0 (virtual_warp spreads co-resident CTAs' busy
+  // warps over the sub-partitions)
+  const int vt = virtual_warp(warp, NT / 32, sm.slot0) * 32 + lane;
+  int pe[kPtSlots], pk[kPtSlots];
+#pragma unroll
+  for (int s = 0; s < kPtSlots; ++s) {
+    const int idx = vt + s * NT;
+    pe[s] = idx < NP ? sm.plist[idx] : -1;
+    pk[s] = idx < NP ? sm.pkey[pe[s]] : 0x7fff;
+  }
+  const int oe = sm.olist[vt], ok = sm.okey[oe];
+  const int tx = oe % TX, ty = oe / TX;
 
   // ---- per-point plane quantities ------------------------------------------
   double carryT[kPtSlots], carryS[kPtSlots];  // dT/dz, dS/dz of the previous level per point slot
@@ -290,8 +421,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   auto compute_plane = [&](int lev, int buf, bool store) {
 #pragma unroll
     for (int s = 0; s < kPtSlots; ++s) {
-      const int p = tid + s * NT;
-      if (p >= NP) break;
+      const int p = pe[s];
+      if (p < 0) break;
+      if (lev - lo < pk[s]) continue;  // dry so far: the prefilled constants, zero carries
       const int pi = p % PX, pj = p / PX;
       const int i = i0 - 1 + pi, j = j0 - 1 + pj;
       F rT = 0, rS = 0;
@@ -381,6 +513,22 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     const F(*q)[NP] = sm.q[b];
     const uint8_t *qm = sm.qm[b];
     F(*pb)[NP] = sm.pub[b];
+    if (lev - lo < ok) {
+      // no slope of the own point is needed yet, and no neighbour reads its published values
+#pragma unroll
+      for (int n = 0; n < NS; ++n) out[n] = Slope<F>{F(0), F(0)};
+      if (a.slopes && lev < ke && own_in) {
+        double *sl = a.slopes + L.at(i0 + tx, j0 + ty, lev);
+        const long long F_ = a.slope_field;
+#pragma unroll
+        for (int n = 0; n < NS; ++n) {
+          sl[(SLOPE_T + n) * F_] = 0.0;
+          sl[(SLOPE_S + n) * F_] = 0.0;
+        }
+        sl[SLOPE_R * F_] = (double)q[Q_R0][pc];
+        sl[(SLOPE_R + 1) * F_] = (double)q[Q_R1][pc];
+      }
+    } else {
     const unsigned m = qm[pc];
     const bool mH[4] = {(m & VG_MASK_U) != 0, (qm[pc - 1] & VG_MASK_U) != 0, (m & VG_MASK_V) != 0,
                         (qm[pc - PX] & VG_MASK_V) != 0};
@@ -409,6 +557,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       pb[PB_TS_XW0 + v][pc] = out[S_XW0 + v].t * F(out[S_XW0 + v].s);
       pb[PB_T_YS0 + v][pc] = out[S_YS0 + v].t;
       pb[PB_TS_YS0 + v][pc] = out[S_YS0 + v].t * F(out[S_YS0 + v].s);
+    }
     }
     if (pring >= 0) {
       const bool mHr = hring == 1 ? (qm[pring - 1] & VG_MASK_U) != 0 : (qm[pring - PX] & VG_MASK_V) != 0;
@@ -456,7 +605,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     const F dzwF[2] = {to_F<F>(zdzw[k > 0 ? k - 1 : 0]), to_F<F>(zdzw[k])}, qzF = to_F<F>(zq_dzt[k]);
     const F ksteepF = to_F<F>(a.ksteep);
     unsigned mk = 0;
-    if (east || north || top) mk = __ldg(a.m + o);
+    if ((east || north || top) && k - lo >= ok) mk = __ldg(a.m + o);  // before its key: no mask bit
 
     // east face: Ai_ez, K_11 (isoneutral.py:100-132); ip = 0 is this point, ip = 1 the east neighbour
     if (east) {
