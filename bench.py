@@ -700,14 +700,18 @@ def run_gb300(args):
     # same initial state; its tracers are compared with the FP64 run's
     split = DeviceState.from_host(host, device=device, precision="f32split")
     sstep = IsoneutralStepper(split)
-    sstep.step(args.warmup)
+    for _ in range(args.warmup):
+        sstep.step_stages()
     torch.cuda.synchronize()
+    sev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record()
-    sstep.step(args.steps)
+    for s in range(args.steps):
+        sstep.step_stages(sev[s])
     s1.record()
     torch.cuda.synchronize()
     split_ms = s0.elapsed_time(s1)
+    split_stage = np.array([[e[n].elapsed_time(e[n + 1]) for n in range(3)] for e in sev])
     split_err = {}
     for name in ("temp", "salt"):
         ref = getattr(dev.variables, name)
@@ -782,6 +786,8 @@ def run_gb300(args):
                 "api": "IsoneutralStepper.pipeline().submit per step: pinned host buffers in the reference layout, "
                        "uploads and downloads on their own streams overlapping the neighbouring steps' kernels"},
         "f32split": {"value": split_value, "unit": "cells/s", "ms_per_step": split_ms / args.steps,
+                     "stage_ms": {"prepare": float(split_stage[:, 0].mean()), "pre": float(split_stage[:, 1].mean()),
+                                  "diffusion_temp_and_salt": float(split_stage[:, 2].mean())},
                      "speedup_vs_f64": split_value / value,
                      "tracer_rel_maxnorm_err_vs_f64": split_err,
                      "precision": "FP64 tracers, gradients, slope denominators/slopes and implicit solve; "

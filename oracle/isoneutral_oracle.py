@@ -309,13 +309,16 @@ def solve_tridiagonal(a, b, c, d, water_mask, edge_mask):
     c[..., -1] = 0
     if _kbot_form(water_mask, edge_mask):
         # dgtsv works in float64 on whatever the reference hands it; the
-        # solution is stored in an array of a's dtype (float32 runs round it)
+        # solution is stored in an array of a's dtype (float32 runs round it).
+        # Wider types (np.longdouble, for extended-precision checks of this
+        # oracle) keep their precision.
         nz = a.shape[-1]
         shape = a.shape
         wm = water_mask.reshape(-1, nz)
         has = wm.any(axis=1)
         ks = np.where(has, wm.argmax(axis=1), nz)
-        f64 = lambda x: np.asarray(x, dtype=np.float64).reshape(-1, nz)  # noqa: E731
+        wt = np.result_type(a, b, c, d, np.float64)
+        f64 = lambda x: np.asarray(x, dtype=wt).reshape(-1, nz)  # noqa: E731
         sol = dgtsv_columns(f64(a), f64(b), f64(c), f64(d), ks)
         return sol.reshape(shape).astype(out.dtype, copy=False)
     from scipy.linalg import lapack

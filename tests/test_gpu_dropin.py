@@ -201,3 +201,59 @@ def test_solve_implicit_float32_vs_reference_golden():
                          d_edge=g["d_edge"])
     assert out.dtype == np.float32
     assert np.array_equal(out, g["out_dd"])
+
+
+def _thermo_sequence(isoneutral, thermodynamics, state):
+    """thermodynamics.py:425-441 on a NumPy state, as the first test runs it."""
+    vs = state.variables
+    vs.P_diss_iso = np.zeros_like(vs.P_diss_iso)
+    vs.dtemp_iso = np.zeros_like(vs.dtemp_iso)
+    vs.dsalt_iso = np.zeros_like(vs.dsalt_iso)
+    vs.update(isoneutral.isoneutral_diffusion_pre(state))
+    vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.temp, istemp=True))
+    vs.update(isoneutral.isoneutral_diffusion(state, tr=vs.salt, istemp=False))
+    vs.P_diss_skew = np.zeros_like(vs.P_diss_skew)
+    vs.update(isoneutral.isoneutral_skew_diffusion(state, tr=vs.temp, istemp=True))
+    vs.update(isoneutral.isoneutral_skew_diffusion(state, tr=vs.salt, istemp=False))
+    vs.update(thermodynamics.vertmix_tempsalt(state))
+    vs.taum1, vs.tau, vs.taup1 = vs.tau, vs.taup1, vs.taum1
+
+
+def test_host_mirror_uploads_only_changed_fields_and_changes_no_result(monkeypatch):
+    """Two steps of the installed sequence with the device mirror kept between
+    calls against the same steps with the mirror dropped before every call:
+    identical arrays; the second step uploads less than a full state; the
+    arrays the drop-ins return are read-only, as the NumPy backend's own."""
+    from veros_gb300.state import DeviceState, release_host_mirrors
+
+    g = load_golden("thermo_cyclic")
+    mods, handle = plugin_call_sites(monkeypatch)
+    try:
+        iso, thermo = mods["veros.core.isoneutral"], mods["veros.core.thermodynamics"]
+        kept, fresh = state_from_golden(g), state_from_golden(g)
+        release_host_mirrors()
+        uploads = []
+        for _ in range(2):
+            b0 = DeviceState.transfer_bytes["h2d"]
+            _thermo_sequence(iso, thermo, kept)
+            uploads.append(DeviceState.transfer_bytes["h2d"] - b0)
+        for _ in range(2):
+            # dropping the mirror before each call forces every field to be uploaded
+            class Releasing:
+                def __getattr__(self, n):
+                    fn = getattr(iso if hasattr(iso, n) else thermo, n)
+
+                    def call(*a, **k):
+                        release_host_mirrors()
+                        return fn(*a, **k)
+                    return call
+            r = Releasing()
+            _thermo_sequence(r, r, fresh)
+    finally:
+        handle.uninstall()
+        release_host_mirrors()
+    for n in OUT_FIELDS:
+        a, b = getattr(kept.variables, n), getattr(fresh.variables, n)
+        assert np.array_equal(a, b), n
+        assert not a.flags.writeable, n
+    assert uploads[1] < 0.5 * uploads[0], uploads

@@ -117,6 +117,9 @@ def test_veros_like_state_keeps_the_reference_contract():
     KO = collections.namedtuple("KernelOutput", ["temp"])
     vs.update(KO(temp=np.ones((6, 6, 3, 3), dtype=np.float32)))
     assert vs.temp.dtype == np.float64 and vs.temp[0, 0, 0, 0] == 1.0
+    same = np.zeros((6, 6, 3, 3))
+    vs.temp = same
+    assert vs.temp is same  # asarray keeps the object when the dtype matches
     with pytest.raises(ValueError, match="unexpected shape"):
         vs.temp = np.ones((6, 6, 3))
     with pytest.raises(AttributeError):

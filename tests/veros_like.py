@@ -5,11 +5,12 @@ one a ``plugin.install()``-ed Veros takes) is driven through this object. It
 keeps the parts of the reference's state contract that the drop-ins touch:
 
 * ``state.settings.<name>`` (``nx``, ``ny``, ``nz`` and the model settings);
-* ``state.variables.<field>`` as NumPy arrays that are read-only, as the
+* ``state.variables.<field>`` as NumPy arrays, allocated read-only as the
   NumPy backend allocates them (veros/variables.py:941), so a drop-in that
   tried to write a host array in place would fail here as it would there;
-* assignment coerces with ``asarray(val, dtype=...)`` and rejects a changed
-  shape with ``ValueError`` (veros/state.py:219-243);
+* assignment stores ``asarray(val, dtype=...)`` (the given object when its
+  dtype matches) and rejects a changed shape with ``ValueError``
+  (veros/state.py:219-243);
 * ``variables.update(other=None, **fields)`` takes a namedtuple
   (``KernelOutput``), a dict or nothing, and rejects unknown names with
   ``AttributeError`` (veros/state.py:70-90);
@@ -53,13 +54,12 @@ class VerosLikeVariables:
     def __setattr__(self, key, val):
         if key.startswith("_") or key not in self._names:
             return object.__setattr__(self, key, val)
+        # as the reference: asarray (the same object when the dtype already matches), shape check
         new = np.asarray(val, dtype=self._dtypes[key])
         old = getattr(self, key)
         if new.shape != old.shape:
             raise ValueError(f"Got unexpected shape for variable {key} (expected: {old.shape}, got: {new.shape})")
-        if new is val or np.shares_memory(new, old):
-            new = new.copy()
-        object.__setattr__(self, key, self._readonly(new))
+        object.__setattr__(self, key, new)
 
     def update(self, other=None, **new_fields):
         if other is not None:

@@ -66,6 +66,15 @@ __device__ __forceinline__ int virtual_warp(int warp, int nw, unsigned slot0) {
   return (warp - c + nw) % nw;
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async, bypassing L1):
+// both addresses 16-byte aligned. wait_all waits for all of this thread's
+// copies; other threads see them after a barrier.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 struct Layout {
   int X, Y, Z;
   long long pitch, plane;

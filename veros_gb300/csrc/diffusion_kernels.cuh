@@ -339,11 +339,14 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   const F inv_fy = F(1.0 / (cost * a.g.dyt[jc]));
   const F qx_cost = F(1.0 / (4.0 * a.g.dxt[ic] * cost));
   const F q_dyt_cost = F(1.0 / (4.0 * a.g.dyt[jc] * cost));
-  // halo faces: warp 0 the south row of north faces, warp 1 the west column of east faces
+  // halo faces: the last virtual warp the south row of north faces, the one before it the west
+  // column of east faces (in the FP64 form those warps hold the tile's driest columns, so the
+  // halo work does not lengthen the busiest warps' path to the level's barrier)
+  const int hwarp = kOrder ? virtual_warp(warp, NT / 32, slot0) : warp;
   const int hi_n = i0 + lane;  // north face (hi_n, j0-1)
-  const bool halo_n = warp == 0 && hi_n < L.X - 2 && j0 - 1 < L.Y - 2;
+  const bool halo_n = hwarp == NT / 32 - 1 && hi_n < L.X - 2 && j0 - 1 < L.Y - 2;
   const int hj_e = j0 + lane;  // east face (i0-1, hj_e)
-  const bool halo_e = warp == 1 && lane < TY && hj_e < L.Y - 2 && i0 - 1 < L.X - 2;
+  const bool halo_e = hwarp == NT / 32 - 2 && lane < TY && hj_e < L.Y - 2 && i0 - 1 < L.X - 2;
   F h_cosu = 0, h_inv_dyu = 0, h_inv_cost_dxu = 0;
   if (halo_n) {
     h_cosu = F(a.g.cosu[j0 - 1]);

@@ -106,6 +106,7 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched(const MemberArgs<F> *_
     if (threadIdx.x == 0) a.kchunk = kchunk > 0 ? min(kchunk, a.L.Z) : a.L.Z;
     __syncthreads();
     pre_tile_body<F, TY>(a, smem_raw, w.a, w.b, w.c * a.kchunk, min(a.L.Z, (w.c + 1) * a.kchunk));
+    cp_async_wait_all();  // the staged planes of this item are complete before the next reuses them
   }
 }
 
@@ -123,6 +124,7 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched_shares(const MemberArg
     stage(&a, &members[w.member].pre);
     const int nbx = (a.L.X - 3 + 31) / 32;
     pre_tile_body<F, TY>(a, smem_raw, w.a % nbx, w.a / nbx, w.b, w.c);
+    cp_async_wait_all();
   }
 }
 
@@ -421,6 +423,7 @@ int member_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *se
     a.kchunk = dom->Z;
     a.slopes = nullptr;
     a.slope_field = 0;
+    a.stage_ok = pre_stage_ok(a);
     Tr trT{f.temp_tau, f.temp_taup1, f.dtemp_iso, nullptr, nullptr};
     Tr trS{f.salt_tau, f.salt_taup1, f.dsalt_iso, nullptr, nullptr};
     // the diffusion argument builder of diffusion_kernels.cuh; no scratch without the energy branch

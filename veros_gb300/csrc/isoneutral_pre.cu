@@ -44,6 +44,7 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   a.sr = out->ai_stride_r;
   a.slopes = slopes;
   a.slope_field = (long long)a.L.plane * a.L.Z;
+  a.stage_ok = pre_stage_ok(a);
   // tiles of 32 x 8 columns; one CTA per tile on large domains, else every
   // resident CTA (two per SM) with an equal share of the tile-levels
   constexpr int TY = 8, TX = 32;

@@ -84,7 +84,18 @@ struct PreArgs {
   // slope_field doubles apart, for the adjoint
   double *slopes;
   long long slope_field;
+  // 1 if T, S and the mask bytes allow 16-byte copies of their rows (aligned
+  // bases, pitch and plane multiples of 16 elements): the split form then
+  // stages its T/S/mask planes in shared memory (PreStage)
+  int stage_ok;
 };
+
+// Whether the pre arguments allow the 16-byte row copies of the staged planes.
+template <typename F>
+inline int pre_stage_ok(const PreArgs<F> &a) {
+  auto al = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+  return al(a.T) && al(a.S) && al(a.m) && a.L.pitch % 16 == 0 && a.L.plane % 16 == 0;
+}
 enum { SLOPE_T = 0, SLOPE_S = 8, SLOPE_R = 16, SLOPE_FIELDS = 18 };
 
 // slope index h * 2 + v: h = east, west, north, south face; v = face below, above
@@ -93,9 +104,27 @@ enum { S_XE0, S_XE1, S_XW0, S_XW1, S_YN0, S_YN1, S_YS0, S_YS1, NS };
 enum { PB_T_XW0, PB_T_XW1, PB_T_YS0, PB_T_YS1, PB_TS_XW0, PB_TS_XW1, PB_TS_YS0, PB_TS_YS1, NPB };
 constexpr unsigned kMaskWBelow = 0x10;  // in the plane mask byte: W mask of the level below
 
+// Staged planes of the split form: T, S (FP64) and the mask bytes of four
+// consecutive levels (a ring, level l in slot l & 3) over rows j0-1 .. j0+PY-1
+// and columns i0-1 .. i0+PX+1 (the plane points and their east / north
+// neighbours), filled by cp.async two levels ahead of their use, so that a
+// level's plane quantities read shared memory instead of waiting on global
+// loads. The FP64 form has no shared memory to spare for it at two CTAs per SM.
+template <bool kOn, int TY>
+struct PreStage {};
+template <int TY>
+struct PreStage<true, TY> {
+  static constexpr int ROWS = Tile<TY>::PY + 1, DW = 36, MW = 48;  // doubles / bytes per staged row
+  double T[4][ROWS][DW];
+  double S[4][ROWS][DW];
+  unsigned char M[4][ROWS][MW];
+};
+
 template <typename F, int TY>
 struct Smem {
   static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
+  static constexpr bool kStage = sizeof(F) == sizeof(float);
+  __align__(16) PreStage<kStage, TY> st;
   F q[2][NQ][NP];  // per-point quantities; the split form keeps them FP32 (R computed in FP64)
   F pub[2][NPB][NP];
   double inv_dxu[PX], inv_dyu[PY], inv_cost[PY];
@@ -270,6 +299,38 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   const int tid = threadIdx.x;
   const int warp = tid / 32, lane = tid % 32;
   const int i0 = 1 + bx * TX, j0 = 1 + by * TY;
+  constexpr bool kStage = Sm::kStage;
+  const bool stage = kStage && a.stage_ok;
+  // the last plane compute_plane reads (its level + 1 below the top)
+  const int pmax = min(min(ke, Z - 1) + 1, Z - 1);
+  // cp.async of one level's T, S and mask rows into its ring slot (split form)
+  auto issue_plane = [&](int lev) {
+    if constexpr (kStage) {
+      using St = PreStage<true, TY>;
+      constexpr int ND = St::DW / 2, NM = St::MW / 16, PER_ROW = 2 * ND + NM;
+      const int slot = lev & 3, xs = i0 - 1;  // xs = 32 bx: 16-byte aligned rows
+      for (int c = tid; c < St::ROWS * PER_ROW; c += NT) {
+        const int r = c / PER_ROW, q = c % PER_ROW, j = j0 - 1 + r;
+        if (j >= L.Y) continue;
+        if (q < 2 * ND) {
+          const int x = xs + 2 * (q % ND);
+          if (x + 1 >= L.pitch) continue;  // pitch is even: a pair never straddles it
+          const double *src = (q < ND ? a.T : a.S) + L.at(x, j, lev);
+          double *dst = q < ND ? &sm.st.T[slot][r][2 * (q % ND)] : &sm.st.S[slot][r][2 * (q % ND)];
+          cp_async16(dst, src);
+        } else {
+          const int x = xs + 16 * (q - 2 * ND);
+          if (x + 15 >= L.pitch) continue;  // pitch is a multiple of 16
+          cp_async16(&sm.st.M[slot][r][16 * (q - 2 * ND)], a.m + L.at(x, j, lev));
+        }
+      }
+    }
+  };
+
+  // the staged planes the prologue's compute_plane calls and the first loop level read
+  const int lo_stage = max(kb - 1, 0);
+  if (stage)
+    for (int l = lo_stage; l <= min(kb + 2, pmax); ++l) issue_plane(l);
 
   // ---- per-CTA grid tables ------------------------------------------------
   for (int p = tid; p < PX; p += NT) {
@@ -394,6 +455,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   __syncthreads();
   if (warp == 0) warp_stable_scatter(sm.pkey, NP, hist_p, sm.plist, lane);
   else if (warp == 1) warp_stable_scatter(sm.okey, NT, hist_o, sm.olist, lane);
+  if (stage) cp_async_wait_all();  // the prologue's planes, visible after this barrier
   __syncthreads();
   // this thread's plane points (compute_plane) and own point (slopes, faces), with their keys;
   // the busiest entries go to virtual warp 0 (virtual_warp spreads co-resident CTAs' busy
@@ -431,24 +493,39 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       unsigned mk = 0;
       if (i < L.X && j < L.Y) {
         const long long o = L.at(i, j, lev);
-        mk = __ldg(a.m + o);
-        const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
+        // T/S at the point, its east and north neighbours and the point above:
+        // from the staged ring (split form, rows aligned) or global memory
+        auto trc = [&](int which, int di, int dj, int dl) -> double {
+          if constexpr (kStage) {
+            if (stage) {
+              const int sl = (lev + dl) & 3;
+              return which ? sm.st.S[sl][pj + dj][pi + di] : sm.st.T[sl][pj + dj][pi + di];
+            }
+          }
+          return __ldg((which ? a.S : a.T) + o + di + dj * L.pitch + dl * L.plane);
+        };
+        if constexpr (kStage) {
+          mk = stage ? (unsigned)sm.st.M[lev & 3][pj][pi] : (unsigned)__ldg(a.m + o);
+        } else {
+          mk = __ldg(a.m + o);
+        }
+        const double Tc = trc(0, 0, 0, 0), Sc = trc(1, 0, 0, 0);
         if (mk & VG_MASK_T) {
           rT = to_F<F>(Tc) * to_F<F>(eos_c1) + to_F<F>(zeos[lev]);  // (isoneutral.py:40, get_rho.py:93-112)
           rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
         }
         // horizontal differences; their metric factors are applied in F below
         if ((mk & VG_MASK_U) && i < L.X - 1) {
-          dTx = __ldg(a.T + o + 1) - Tc;
-          dSx = __ldg(a.S + o + 1) - Sc;
+          dTx = trc(0, 1, 0, 0) - Tc;
+          dSx = trc(1, 1, 0, 0) - Sc;
         }
         if ((mk & VG_MASK_V) && j < L.Y - 1) {
-          dTy = __ldg(a.T + o + L.pitch) - Tc;
-          dSy = __ldg(a.S + o + L.pitch) - Sc;
+          dTy = trc(0, 0, 1, 0) - Tc;
+          dSy = trc(1, 0, 1, 0) - Sc;
         }
         if ((mk & VG_MASK_W) && lev < Z - 1) {
-          dTz = (__ldg(a.T + o + L.plane) - Tc) * zinv_dzw[lev];
-          dSz = (__ldg(a.S + o + L.plane) - Sc) * zinv_dzw[lev];
+          dTz = (trc(0, 0, 0, 1) - Tc) * zinv_dzw[lev];
+          dSz = (trc(1, 0, 0, 1) - Sc) * zinv_dzw[lev];
         }
         if (lev >= Z - 1) mk &= ~(unsigned)VG_MASK_W;  // no face above the top level
       }
@@ -492,14 +569,19 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   };
 
   const int pc = (ty + 1) * PX + (tx + 1);  // own point in the plane arrays
-  // ring point whose west (east ring column) or south (north ring row) slopes this thread publishes
+  // ring point whose west (east ring column) or south (north ring row) slopes this thread publishes:
+  // the last TX + TY virtual threads, whose own points are the tile's driest, so that a level's
+  // ring work does not lengthen the busiest warps' path to the barrier
   int pring = -1, hring = 0;
-  if (tid < TX) {
-    pring = (TY + 1) * PX + tid + 1;
-    hring = 3;
-  } else if (tid < TX + TY) {
-    pring = (tid - TX + 1) * PX + TX + 1;
-    hring = 1;
+  {
+    const int rt = vt - (NT - TX - TY);
+    if (rt >= 0 && rt < TX) {
+      pring = (TY + 1) * PX + rt + 1;
+      hring = 3;
+    } else if (rt >= TX) {
+      pring = (rt - TX + 1) * PX + TX + 1;
+      hring = 1;
+    }
   }
 
   // the slopes of the ring points no tile owns (the last tile column / row of the domain)
@@ -582,6 +664,8 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   if (kb > 0) compute_plane(kb - 1, (kb - 1) & 1, false);  // only the carries
   compute_plane(kb, kb & 1, true);
   __syncthreads();
+  // staged ring: plane kb+3 into the slot of plane kb-1, which nobody reads any more
+  if (stage && kb + 3 <= pmax) issue_plane(kb + 3);
   Slope<F> cur[NS], nxt[NS];
 #pragma unroll
   for (int n = 0; n < NS; ++n) nxt[n] = Slope<F>{F(0), F(0)};
@@ -595,8 +679,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 
   for (int k = kb; k < ke; ++k) {
     if (k + 1 < Z) compute_plane(k + 1, (k + 1) & 1, true);
-    // plane k+1 complete; the slopes of level k published; nobody still reads the buffers rewritten next
+    // this thread's copies of plane k+3 (issued one level ago) have landed
+    if (stage) cp_async_wait_all();
+    // plane k+1 complete; the slopes of level k published; nobody still reads the buffers rewritten next;
+    // the staged plane k+3 visible
     __syncthreads();
+    // staged ring: plane k+4 into the slot of plane k, last read by compute_plane(k) and (k-1)
+    if (stage && k + 4 <= pmax) issue_plane(k + 4);
     if (k + 1 < Z) slopes_level(k + 1, (k + 1) & 1, nxt);
     const F(*pb)[NP] = sm.pub[k & 1];
     const F(*pbn)[NP] = sm.pub[(k + 1) & 1];  // level k+1 (written only when k + 1 < Z; read only then)
@@ -729,7 +818,8 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_span_kernel(PreArgs<F> a, int 
     const int t = (int)(p / Z), kb = (int)(p % Z);
     const int ke = (int)min((long long)Z, end - (long long)t * Z);
     pre_tile_body<F, TY>(a, smem_raw, t % ntx, t / ntx, kb, ke);
-    __syncthreads();  // shared memory is rebuilt by the next segment
+    cp_async_wait_all();  // no staged copy of this segment may land in the next one's buffers
+    __syncthreads();      // shared memory is rebuilt by the next segment
     p = (long long)t * Z + ke;
   }
 }

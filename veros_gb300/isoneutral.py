@@ -11,15 +11,18 @@ Same call signatures as the reference:
 
 ``state`` is either a :class:`veros_gb300.state.DeviceState` (fields stay on
 the GPU, all work is enqueued on torch's current stream, nothing synchronises)
-or a NumPy-backend ``VerosState``, whose fields are uploaded, processed and
-written back (the reference's ``vs.update`` contract: pre returns the new
-arrays, the diffusion routines mutate ``state.variables``).
+or a NumPy-backend ``VerosState``, whose fields are mirrored on the device,
+processed and written back (the reference's ``vs.update`` contract: pre
+returns the new arrays, the diffusion routines mutate ``state.variables``).
+Arrays returned to a NumPy state are read-only, as the NumPy backend's own
+are, and a field is uploaded only when the state holds another array than the
+one last transferred for it (``state.host_mirror``).
 """
 
 import torch
 
 from . import _capi
-from .state import DeviceState, KernelOutput, FIELDS_MASK
+from .state import DeviceState, KernelOutput, FIELDS_MASK, host_mirror, mirror_download, mirror_written
 
 PRE_OUT = ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "K_11", "K_22", "K_33")
 
@@ -96,9 +99,10 @@ def isoneutral_diffusion_pre(state):
         return KernelOutput(**{n: getattr(v, n) for n in PRE_OUT})
     names = ("temp", "salt", "K_iso", "dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt",
              *FIELDS_MASK, *PRE_OUT)
-    dev = DeviceState.from_host(state, fields=names)
+    dev = host_mirror(state, names)
+    mirror_written(dev, PRE_OUT)
     run_pre(dev)
-    return KernelOutput(**{n: dev.download(n) for n in PRE_OUT})
+    return KernelOutput(**{n: mirror_download(dev, n) for n in PRE_OUT})
 
 
 def _diffusion_entry(state, tr, istemp, skew):
@@ -113,19 +117,20 @@ def _diffusion_entry(state, tr, istemp, skew):
         run_diffusion(state, istemp, skew=skew)
         return None
     energy = bool(state.settings.enable_conserve_energy)
-    names = [name, dname, "K_iso", "K_gm", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "kbot",
+    names = [name, dname, "K_gm" if skew else "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by", "kbot",
              "dxt", "dxu", "dyt", "dyu", "cost", "cosu", "dzt", "dzw", "zt", *FIELDS_MASK]
     if energy:
         names += ["int_drhodT" if istemp else "int_drhodS", pname]
-    dev = DeviceState.from_host(state, fields=names)
-    if tr is not None:
-        dev.upload(name, tr)
-    run_diffusion(dev, istemp, skew=skew)
     vs = state.variables
-    out = {name: dev.download(name), dname: dev.download(dname)}
-    if energy:
-        out[pname] = dev.download(pname)
-    vs.update(out)
+    if tr is not None and tr is not getattr(vs, name):
+        names = [n for n in names if n != name]
+    dev = host_mirror(state, names)
+    if tr is not None and tr is not getattr(vs, name):
+        dev.upload(name, tr)  # the reference diffuses the tr it is given (by value)
+    written = [name, dname] + ([pname] if energy else [])
+    mirror_written(dev, written)
+    run_diffusion(dev, istemp, skew=skew)
+    vs.update({n: mirror_download(dev, n) for n in written})
     return None
 
 
@@ -143,9 +148,10 @@ def isoneutral_diag_streamfunction_kernel(state):
     """GM streamfunction diagnostics (veros/core/isoneutral/isoneutral.py:232-254):
     ``KernelOutput(B1_gm, B2_gm)``."""
     if not _is_device_state(state):
-        dev = DeviceState.from_host(state, fields=("K_gm", "Ai_ez", "Ai_nz", "B1_gm", "B2_gm"))
+        dev = host_mirror(state, ("K_gm", "Ai_ez", "Ai_nz", "B1_gm", "B2_gm"))
+        mirror_written(dev, ("B1_gm", "B2_gm"))
         _run_streamfunction(dev)
-        return KernelOutput(B1_gm=dev.download("B1_gm"), B2_gm=dev.download("B2_gm"))
+        return KernelOutput(B1_gm=mirror_download(dev, "B1_gm"), B2_gm=mirror_download(dev, "B2_gm"))
     _run_streamfunction(state)
     v = state.variables
     return KernelOutput(B1_gm=v.B1_gm, B2_gm=v.B2_gm)

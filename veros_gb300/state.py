@@ -12,6 +12,7 @@ tensor components are whole x-y-z blocks.
 """
 
 import warnings
+import weakref
 from collections import namedtuple
 
 import numpy as np
@@ -261,7 +262,8 @@ class DeviceState:
         t = getattr(self.variables, name)
         if isinstance(t, torch.Tensor):
             DeviceState.transfer_bytes["d2h"] += t.numel() * t.element_size()
-            return t.detach().cpu().contiguous().numpy()
+            # the reference layout (C order of the logical shape) formed on the device, then one copy
+            return t.detach().contiguous().cpu().numpy()
         return t
 
     # ---- derived device views --------------------------------------------
@@ -332,3 +334,78 @@ class DeviceState:
     def to_host_dict(self, names=None):
         names = names or self.variables.fields()
         return {n: self.download(n) for n in names}
+
+
+# ---- device mirrors for the drop-ins' host-array path ------------------------
+#
+# A plugin-installed NumPy-backend Veros hands the drop-ins a VerosState of
+# host arrays on every call. Uploading every field a call reads, every call,
+# would move the whole state over the host link each time, although most of
+# it has not changed since the previous call: the grid and masks never change,
+# and the tensors and tracers a call reads are usually the very arrays an
+# earlier drop-in call returned. The NumPy backend never modifies a state
+# array in place: its update() works on a copy (veros/core/operators.py:19-45)
+# and setattr stores the array it is given (veros/state.py:219-243). So a
+# device field can stand for a host array as long as that array object is
+# alive and read-only: the drop-ins return read-only arrays (as the NumPy
+# backend allocates its own, veros/variables.py:941) and remember them, and a
+# call uploads a field only when the state holds a different or writeable
+# array. One mirror per domain shape and device is kept for the process.
+
+_MIRRORS = {}
+
+
+def host_mirror(host, fields, precision="f64", device=None):
+    """The device mirror of a NumPy-backend VerosState with ``fields`` current.
+
+    Fields whose host array is the read-only array last transferred for them
+    are not uploaded again. The mirror's settings and time-level indices are
+    the state's."""
+    vs = host.variables
+    s = host.settings
+    nx, ny, nz = int(s.nx), int(s.ny), int(s.nz)
+    device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    key = (nx, ny, nz, precision, str(device))
+    dev = _MIRRORS.get(key)
+    settings = {n: getattr(s, n) for n in SETTING_NAMES if hasattr(s, n)}
+    if dev is None:
+        dev = DeviceState(nx, ny, nz, settings, device=device, precision=precision)
+        dev.alloc_fields()
+        dev._host_src = {}
+        _MIRRORS[key] = dev
+    dev.settings = Settings(**settings)
+    v = dev.variables
+    v.tau, v.taup1, v.taum1 = int(vs.tau), int(vs.taup1), int(vs.taum1)
+    for n in fields:
+        try:
+            arr = getattr(vs, n)
+        except (AttributeError, RuntimeError):  # absent, or inactive in this configuration
+            continue
+        if arr is None or n not in v.fields():
+            continue
+        ref = dev._host_src.get(n)
+        if ref is not None and ref() is arr and isinstance(arr, np.ndarray) and not arr.flags.writeable:
+            continue  # the device field holds this very array
+        dev.upload(n, np.asarray(arr))
+        keep = isinstance(arr, np.ndarray) and not arr.flags.writeable
+        dev._host_src[n] = weakref.ref(arr) if keep else None
+    return dev
+
+
+def mirror_written(dev, names):
+    """Fields a kernel wrote no longer stand for any host array."""
+    for n in names:
+        dev._host_src[n] = None
+
+
+def mirror_download(dev, name):
+    """A read-only host copy of a device field, remembered as its host array."""
+    arr = dev.download(name)
+    arr.flags.writeable = False
+    dev._host_src[name] = weakref.ref(arr)
+    return arr
+
+
+def release_host_mirrors():
+    """Free the device mirrors of the host-array path."""
+    _MIRRORS.clear()

@@ -17,7 +17,7 @@ halos.
 import torch
 
 from . import _capi
-from .state import DeviceState, KernelOutput, require_single_process
+from .state import DeviceState, KernelOutput, host_mirror, mirror_download, mirror_written, require_single_process
 
 
 def run_vertmix(dev):
@@ -48,6 +48,7 @@ def vertmix_tempsalt(state):
         return KernelOutput(**{n: getattr(v, n) for n in names})
     fields = ("temp", "salt", "kappaH", "kbot", "forc_temp_surface", "forc_salt_surface", "dxt", "dxu", "dyt", "dyu",
               "cost", "cosu", "dzt", "dzw", "zt", "maskT", "maskU", "maskV", "maskW")
-    dev = DeviceState.from_host(state, fields=fields)
+    dev = host_mirror(state, fields)
+    mirror_written(dev, names)
     run_vertmix(dev)
-    return KernelOutput(**{n: dev.download(n) for n in names})
+    return KernelOutput(**{n: mirror_download(dev, n) for n in names})
