@@ -255,9 +255,25 @@ int vg_isoneutral_step_f32split(const VgDomain *dom, const VgGrid *grid, const V
                                 const VgStepFieldsF32 *f, void *scratch, size_t scratch_bytes, void *stream);
 int vg_isoneutral_step_prepare_f32split(const VgDomain *dom, const VgStepFieldsF32 *f, void *stream);
 
-/* First stage of vg_isoneutral_step_f64 alone (new time level and zeroed
- * tendencies), for callers that time or interleave the stages. */
+/* The new time level and zeroed tendencies of a step on every cell, as a
+ * separate kernel (what vg_isoneutral_step_f64 fuses into its flux kernel).
+ * With vg_isoneutral_pre_f64 and vg_isoneutral_diffusion_pair_ordered_f64 it
+ * makes the unfused form of the step, with the same results bit for bit. */
 int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, void *stream);
+
+/* One stage of vg_isoneutral_step_f64, for callers that time or interleave
+ * the stages; stages 0, 1, 2 in order make one step. 0: the new time level
+ * and zeroed tendencies on the two-cell rim of every level; 1: pre; 2:
+ * diffusion of temp and salt, whose flux kernel also prepares the interior
+ * cells (each wet cell's new level and tendency written once, from tr[tau]
+ * and its flux divergence, instead of a separate preparation followed by a
+ * read-modify-write). */
+int vg_isoneutral_step_stage_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                 const VgStepFields *f, void *scratch, size_t scratch_bytes, int stage,
+                                 void *stream);
+int vg_isoneutral_step_stage_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
+                                      const VgStepFieldsF32 *f, void *scratch, size_t scratch_bytes, int stage,
+                                      void *stream);
 
 /* Replaces veros.core.thermodynamics.vertmix_tempsalt
  * (veros/core/thermodynamics.py:248-300): implicit vertical mixing of temp and

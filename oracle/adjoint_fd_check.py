@@ -44,6 +44,8 @@ sys.path.insert(0, REPO)
 NSTEPS = 8
 NDIR = {"T": 6, "S": 5, "K": 5}
 EPS_LD = {"T": (1e-11, 1e-12), "S": (1e-11, 1e-12), "K": (1e-7, 1e-8)}
+# kink-free steps: small enough that no slope of the rollout changes sign between x - h u and x + h u
+EPS_KF = {"T": (1e-13, 1e-14), "S": (1e-13, 1e-14), "K": (1e-10, 1e-11)}
 EPS_64 = {"T": (1e-11,), "S": (1e-11,), "K": (1e-7,)}
 
 
@@ -146,6 +148,79 @@ def _ld_loss(job):
     return idx, str(eps), sign, str(L), str(h)
 
 
+def _ld_cd(job):
+    """Central difference of the longdouble oracle along direction idx with
+    relative step eps, and the number of slopes (Ai components of every step)
+    whose sign differs between the two rollouts."""
+    idx, which, eps = job
+    host, T0, S0, K, target, wet = _ld_state()
+    which_d, u = directions(T0.shape)[idx]
+    assert which_d == which
+    x = {"T": T0, "S": S0, "K": K}[which]
+    h = np.longdouble(eps) * np.sqrt(np.sum(x * x))
+    from oracle import isoneutral_adjoint as A
+
+    out = []
+    for sign in (1, -1):
+        base = {"T": T0, "S": S0, "K": K}
+        base[which] = x + sign * h * u.astype(np.longdouble)
+        T, S, signs = base["T"], base["S"], []
+        for _ in range(NSTEPS):
+            T, S, vs = A.forward_step(host, T, S, base["K"])
+            signs.append(np.concatenate([np.sign(getattr(vs, n)).astype(np.int8).ravel()
+                                         for n in ("Ai_ez", "Ai_nz", "Ai_bx", "Ai_by")]))
+        out.append((np.sum(wet * (T - target) ** 2), np.concatenate(signs)))
+    (Lp, sp), (Lm, sm) = out
+    return idx, str(eps), str((Lp - Lm) / (2 * h)), int(np.count_nonzero(sp != sm))
+
+
+def _ld_adjoint(_):
+    """The NumPy adjoint of the rollout, evaluated in longdouble."""
+    from oracle import isoneutral_adjoint as A
+
+    host, T0, S0, K, target, wet = _ld_state()
+    L, gT, gS, gK = A.rollout_grad(host, T0, S0, K, target, NSTEPS)
+    return [str(float(np.sum(g * u.astype(np.longdouble))))
+            for (w, u), g in ((d, {"T": gT, "S": gS, "K": gK}[d[0]]) for d in directions(T0.shape))]
+
+
+def run_cpu_kinkfree(path, procs):
+    """Kink-free central differences and the longdouble adjoint, added to the CPU file."""
+    import multiprocessing as mp
+
+    with open(path) as f:
+        data = json.load(f)
+    jobs = [(idx, row["which"], eps) for idx, row in enumerate(data["directions"]) for eps in EPS_KF[row["which"]]]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(procs) as pool:
+        adj = pool.map_async(_ld_adjoint, [0])
+        results = pool.map(_ld_cd, jobs)
+        ad_ld = adj.get()[0]
+    worst = {}
+    for idx, eps, fd, nflip in results:
+        row = data["directions"][idx]
+        row["ad_longdouble"] = float(ad_ld[idx])
+        fd = float(np.longdouble(fd))
+        sc = max(abs(row["ad_longdouble"]), row["scale"])
+        e_ld = abs(fd - row["ad_longdouble"]) / sc
+        row.setdefault("kink_free", {})[eps] = {"fd": fd, "slope_sign_changes": nflip,
+                                                "rel_err_longdouble_adjoint": e_ld,
+                                                "rel_err_numpy_adjoint": abs(fd - row["ad_numpy"]) / sc}
+        key = f"{row['which']} eps={eps}"
+        if nflip == 0:
+            worst[key] = max(worst.get(key, 0.0), e_ld)
+    for row in data["directions"]:
+        row["numpy_fp64_vs_longdouble_adjoint"] = abs(row["ad_numpy"] - row["ad_longdouble"]) / max(
+            abs(row["ad_longdouble"]), row["scale"])
+    data["kink_free"] = {"eps": EPS_KF, "worst_rel_err_longdouble_adjoint_no_sign_change": worst,
+                         "worst_numpy_fp64_vs_longdouble_adjoint": max(
+                             r["numpy_fp64_vs_longdouble_adjoint"] for r in data["directions"]),
+                         "seconds": time.perf_counter() - t0}
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1)
+    print(json.dumps(data["kink_free"], indent=1))
+
+
 def run_cpu(path, procs):
     import multiprocessing as mp
 
@@ -213,5 +288,7 @@ if __name__ == "__main__":
         run_gpu(sys.argv[2])
     elif mode == "cpu":
         run_cpu(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else (os.cpu_count() or 1))
+    elif mode == "kinkfree":
+        run_cpu_kinkfree(sys.argv[2], int(sys.argv[3]) if len(sys.argv) > 3 else (os.cpu_count() or 1))
     else:
         compare(sys.argv[2], sys.argv[3])

@@ -381,6 +381,30 @@ def test_column_order_gives_identical_results():
     assert np.array_equal(np.sort(order), np.arange((a.X - 4) * (a.Y - 4)))
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32split"])
+@pytest.mark.parametrize("energy", [False, True])
+def test_fused_preparation_matches_separate_pass(precision, energy):
+    """The step with the preparation fused into the flux kernel (rim kernel,
+    pre, fused diffusion) equals a separate preparation of every cell, pre and
+    the unfused diffusion, bit for bit, over two steps, land and coast
+    columns included."""
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    host = synthetic.make_state(37, 26, 14, seed=9, eq_of_state_type=3, land_fraction=0.3,
+                                settings=dict(enable_conserve_energy=energy))
+    a = IsoneutralStepper(DeviceState.from_host(host, precision=precision))
+    b = IsoneutralStepper(DeviceState.from_host(host, precision=precision))
+    for _ in range(2):
+        a.step(1)
+        b.step_unfused()
+    torch.cuda.synchronize()
+    names = ("temp", "salt", "dtemp_iso", "dsalt_iso") + (("P_diss_iso",) if energy else ())
+    for n in names:
+        np.testing.assert_array_equal(a.dev.download(n), b.dev.download(n), err_msg=n)
+
+
 def test_drop_in_signatures_on_device_state():
     import veros_gb300 as vg
     from veros_gb300 import synthetic

@@ -168,6 +168,14 @@ SIGNATURES = {
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_isoneutral_step_prepare_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgStepFields),
                                                       ctypes.c_void_p]),
+    "vg_isoneutral_step_stage_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                    ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgStepFields),
+                                                    ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                                    ctypes.c_void_p]),
+    "vg_isoneutral_step_stage_f32split": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
+                                                         ctypes.POINTER(VgIsoSettings),
+                                                         ctypes.POINTER(VgStepFieldsF32), ctypes.c_void_p,
+                                                         ctypes.c_size_t, ctypes.c_int, ctypes.c_void_p]),
     "vg_vertmix_tempsalt_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                                ctypes.POINTER(VgIsoSettings)] + [ctypes.c_void_p] * 8 +
                                 [ctypes.c_int, ctypes.c_void_p]),

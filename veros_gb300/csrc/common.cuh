@@ -229,15 +229,19 @@ struct Eos {
 
 // The temp+salt diffusion of vg_isoneutral_diffusion_pair_* with the
 // implicit solve's columns taken in the order column_order (interior column
-// indices (i-2) + (j-2)*(X-4); NULL: natural order).
+// indices (i-2) + (j-2)*(X-4); NULL: natural order). fuse_prepare: the flux
+// kernel also does a step's preparation of the interior cells (the step's
+// rim is prepared separately), instead of updating what a separate
+// preparation wrote.
 int diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                const VgTensorFields *ten, const double *K_iso, const uint8_t *mask_bits,
                                const int32_t *kbot, const VgTracerArgs *temp, const VgTracerArgs *salt,
-                               const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream);
+                               const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream,
+                               int fuse_prepare = 0);
 int diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                     const VgTensorFieldsF32 *ten, const float *K_iso, const uint8_t *mask_bits,
                                     const int32_t *kbot, const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
                                     const int32_t *column_order, void *scratch, size_t scratch_bytes,
-                                    void *stream);
+                                    void *stream, int fuse_prepare = 0);
 
 }  // namespace vg

@@ -60,7 +60,19 @@ struct DiffArgs {
   F *P;
   F *fe, *fn, *ft;  // scratch fluxes (energy branch)
   int iso, save_fluxes, kchunk;
+  // 1 inside a whole step (vg_isoneutral_step_*): the kernel also does the
+  // step's preparation of its interior cells (tr[taup1] = tr[tau] * maskT,
+  // zero tendencies and P_diss) instead of updating what a separate pass
+  // wrote; the same values, bit for bit, without that pass
+  int fuse_prepare;
 };
+
+// x * 0.0 by integer operations for finite x (the zero of x's sign), the
+// product itself otherwise (inf and NaN give NaN)
+__device__ __forceinline__ double times_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return ((b >> 52) & 0x7FF) == 0x7FF ? x * 0.0 : __longlong_as_double(b & (long long)0x8000000000000000ULL);
+}
 
 template <typename F>
 __device__ __forceinline__ F ld(const F *p, long long o) { return __ldg(p + o); }
@@ -514,16 +526,31 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       for (int r = 0; r < NTR; ++r) fe_s[b][r][lane][0] = east_flux(L, A[r].tr, oh, k, ce);
     }
     __syncthreads();
-    if (own && k >= kact && (__ldg(a.m + o) & VG_MASK_T)) {  // maskT multiplies the divergence (diffusion.py:123-137)
+    const bool wetT = own && k >= kact && (__ldg(a.m + o) & VG_MASK_T);
+    if (wetT) {  // maskT multiplies the divergence (diffusion.py:123-137)
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
         const DiffArgs<F> &t = A[r];
         F e = pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy));
         e = pfma(ft[r] - ft_prev[r], to_F<F>(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
-        t.dtr_iso[o] = add_(t.dtr_iso[o], e);
-        t.trp[o] = fma(t.dt, to_D(e), t.trp[o]);  // tr[taup1] += dt * dtr (diffusion.py:192)
+        if (a.fuse_prepare) {
+          // tr[taup1] = tr[tau] * 1 and dtracer_iso = 0 (thermodynamics.py:226-241, :427-429), then
+          // the explicit update: the values the separate preparation and the update below give
+          t.dtr_iso[o] = add_(F(0), e);
+          t.trp[o] = fma(t.dt, to_D(e), __ldg(t.tr + o));
+        } else {
+          t.dtr_iso[o] = add_(t.dtr_iso[o], e);
+          t.trp[o] = fma(t.dt, to_D(e), t.trp[o]);  // tr[taup1] += dt * dtr (diffusion.py:192)
+        }
+      }
+    } else if (own && a.fuse_prepare) {  // no divergence: the prepared values (maskT = 0)
+#pragma unroll
+      for (int r = 0; r < NTR; ++r) {
+        A[r].dtr_iso[o] = F(0);
+        A[r].trp[o] = times_zero(__ldg(A[r].tr + o));
       }
     }
+    if (own && a.fuse_prepare && a.P) a.P[o] = F(0);
     if (own) {
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
@@ -553,7 +580,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
 // starting above level 0 pays the restart of a k-chunk); the body ends with a
 // barrier before its buffers are reused.
 template <typename F, int TY, int NTR>
-__global__ void __launch_bounds__(TX * TY, 2) flux_span_kernel(DiffArgs<F> a, DiffArgs<F> b, int ntx, int ntiles) {
+__global__ void __launch_bounds__(TX * TY, 16 / TY) flux_span_kernel(DiffArgs<F> a, DiffArgs<F> b, int ntx, int ntiles) {
   extern __shared__ double zq_dzt[];
   const DiffArgs<F> A[2] = {a, b};
   const int Z = a.L.Z;
@@ -919,6 +946,7 @@ inline int make_diff_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSe
   a.iso = skew ? 0 : 1;
   a.kchunk = 0;
   a.col_order = nullptr;
+  a.fuse_prepare = 0;
   return VG_OK;
 }
 

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) prepare_batched(const MemberArgs<F> *__re
 }
 
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) pre_batched(const MemberArgs<F> *__restrict__ members,
+__global__ void __launch_bounds__(32 * TY, 16 / TY) pre_batched(const MemberArgs<F> *__restrict__ members,
                                                           const WorkItem *__restrict__ items, int nitems,
                                                           int *counter, int kchunk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched(const MemberArgs<F> *_
 // Equal shares: CTA c runs the segments starts[c] .. starts[c+1]-1 (member,
 // tile, first level, end level) in order, with no work counter.
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) pre_batched_shares(const MemberArgs<F> *__restrict__ members,
+__global__ void __launch_bounds__(32 * TY, 16 / TY) pre_batched_shares(const MemberArgs<F> *__restrict__ members,
                                                                  const WorkItem *__restrict__ items,
                                                                  const int *__restrict__ starts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(32 * TY, 2) pre_batched_shares(const MemberArg
 }
 
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *__restrict__ members,
+__global__ void __launch_bounds__(32 * TY, 16 / TY) flux_batched(const MemberArgs<F> *__restrict__ members,
                                                            const WorkItem *__restrict__ items, int nitems,
                                                            int *counter, int kchunk) {
   extern __shared__ double zq_dzt[];
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(32 * TY, 2) flux_batched(const MemberArgs<F> *
 }
 
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) flux_batched_shares(const MemberArgs<F> *__restrict__ members,
+__global__ void __launch_bounds__(32 * TY, 16 / TY) flux_batched_shares(const MemberArgs<F> *__restrict__ members,
                                                                   const WorkItem *__restrict__ items,
                                                                   const int *__restrict__ starts) {
   extern __shared__ double zq_dzt[];

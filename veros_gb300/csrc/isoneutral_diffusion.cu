@@ -125,7 +125,8 @@ int diffusion_one(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *
 template <typename F, typename Ten, typename Tr>
 int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten,
                    const F *K_iso, const uint8_t *mask_bits, const int32_t *kbot, const Tr *temp, const Tr *salt,
-                   void *scratch, size_t scratch_bytes, void *stream, const int32_t *col_order = nullptr) {
+                   void *scratch, size_t scratch_bytes, void *stream, const int32_t *col_order = nullptr,
+                   int fuse_prepare = 0) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -138,6 +139,9 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
   if ((st = make_diff_args(dom, grid, set, ten, K_iso, mask_bits, kbot, salt, 0, sc + one / sizeof(double), aS)))
     return st;
   aT.col_order = aS.col_order = col_order;
+  aT.fuse_prepare = aS.fuse_prepare = fuse_prepare;
+  if (fuse_prepare && aT.P != aS.P)
+    return fail(VG_ERR_ARG, "step diffusion: temp and salt must share P_diss_iso");
   cudaStream_t s = as_stream(stream);
   if ((st = launch_flux_div<F, 2>(aT, aS, s))) return st;
   if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
@@ -150,18 +154,19 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
 int diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                const VgTensorFields *ten, const double *K_iso, const uint8_t *mask_bits,
                                const int32_t *kbot, const VgTracerArgs *temp, const VgTracerArgs *salt,
-                               const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream) {
+                               const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream,
+                               int fuse_prepare) {
   return diffusion_pair<double>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
-                                stream, column_order);
+                                stream, column_order, fuse_prepare);
 }
 
 int diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                     const VgTensorFieldsF32 *ten, const float *K_iso, const uint8_t *mask_bits,
                                     const int32_t *kbot, const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
                                     const int32_t *column_order, void *scratch, size_t scratch_bytes,
-                                    void *stream) {
+                                    void *stream, int fuse_prepare) {
   return diffusion_pair<float>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
-                               stream, column_order);
+                               stream, column_order, fuse_prepare);
 }
 
 }  // namespace vg

@@ -45,9 +45,11 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   a.slopes = slopes;
   a.slope_field = (long long)a.L.plane * a.L.Z;
   a.stage_ok = pre_stage_ok(a);
-  // tiles of 32 x 8 columns; one CTA per tile on large domains, else every
-  // resident CTA (two per SM) with an equal share of the tile-levels
-  constexpr int TY = 8, TX = 32;
+  // tiles of 32 x 8 columns (FP64: two CTAs of 8 warps per SM) or 32 x 4
+  // (split form: four CTAs of 4 warps, whose level barriers overlap); one CTA
+  // per tile on large domains, else every resident CTA with an equal share
+  // of the tile-levels
+  constexpr int TY = sizeof(F) == sizeof(double) ? 8 : 4, TX = 32;
   const int nbx = (a.L.X - 3 + TX - 1) / TX, nby = (a.L.Y - 3 + TY - 1) / TY;
   const size_t smem = pre_smem_bytes<F, TY>(a.L.Z);
   cudaError_t e =

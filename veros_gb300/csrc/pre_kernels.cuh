@@ -808,7 +808,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 // the restart of a k-chunk). With a whole number of tiles per SM rarely
 // available, equal shares keep every SM busy to the end of the launch.
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 2) pre_span_kernel(PreArgs<F> a, int ntx, int ntiles) {
+__global__ void __launch_bounds__(32 * TY, 16 / TY) pre_span_kernel(PreArgs<F> a, int ntx, int ntiles) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Z = a.L.Z;
   const long long W = (long long)ntiles * Z;

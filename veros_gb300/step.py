@@ -59,32 +59,48 @@ class IsoneutralStepper:
             self._rotate()
 
     def step_stages(self, events=None):
-        """One step as three C calls: prepare, pre, diffusion of temp and salt.
+        """One step as three C calls, the stages of ``vg_isoneutral_step_*``:
+        the rim's preparation, pre, and diffusion of temp and salt (with the
+        interior's preparation fused in). The same kernels as ``step``.
 
         ``events``: optional list of 4 ``torch.cuda.Event`` recorded on the
         current stream before, between and after the stages.
         """
-        dev, lib = self.dev, self.lib
+        dev = self.dev
         stream_obj = torch.cuda.current_stream(dev.device)
         stream = stream_obj.cuda_stream
         f = self._fields()
         dom, grid, sett = dev.domain(), dev.grid(), dev.settings.to_struct()
         nbytes = self.scratch.numel() * 8
-        rec = (lambda n: events[n].record(stream_obj)) if events else (lambda n: None)
-        rec(0)
+        fn = self._fn("vg_isoneutral_step_stage")
+        for stage in range(3):
+            if events:
+                events[stage].record(stream_obj)
+            _capi.check(fn(dom, grid, sett, f, self.scratch.data_ptr(), nbytes, stage, stream),
+                        ("step rim", "pre", "diffusion")[stage])
+        if events:
+            events[3].record(stream_obj)
+        self._rotate()
+
+    def step_unfused(self):
+        """One step as a separate preparation of every cell, pre and the
+        temp+salt diffusion (no fused preparation): the same results as
+        ``step``, bit for bit, at one extra pass over the tracer fields."""
+        dev = self.dev
+        stream = torch.cuda.current_stream(dev.device).cuda_stream
+        f = self._fields()
+        dom, grid, sett = dev.domain(), dev.grid(), dev.settings.to_struct()
         _capi.check(self._fn("vg_isoneutral_step_prepare")(dom, f, stream), "step prepare")
-        rec(1)
         _capi.check(self._fn("vg_isoneutral_pre")(dom, grid, sett, f.temp_tau, f.salt_tau, f.K_iso, f.mask_bits,
                                                   f.ten, stream), "pre")
-        rec(2)
         targs = _capi.VgTracerArgs if dev.precision == "f64" else _capi.VgTracerArgsF32
         trT = targs(f.temp_tau, f.temp_taup1, f.dtemp_iso, f.int_drhodT_tau, f.P_diss_iso)
         trS = targs(f.salt_tau, f.salt_taup1, f.dsalt_iso, f.int_drhodS_tau, f.P_diss_iso)
         _capi.check(self._fn("vg_isoneutral_diffusion_pair_ordered")(dom, grid, sett, f.ten, f.K_iso, f.mask_bits,
                                                                      f.kbot, trT, trS, f.column_order,
-                                                                     self.scratch.data_ptr(), nbytes, stream),
+                                                                     self.scratch.data_ptr(),
+                                                                     self.scratch.numel() * 8, stream),
                     "diffusion")
-        rec(3)
         self._rotate()
 
     def step_host(self, temp_tau, salt_tau, out_temp, out_salt, out_dtemp, out_dsalt, staging=None):
