@@ -369,6 +369,9 @@ typedef struct VgAdjointFields {
   const double *gtemp_new, *gsalt_new;
   double *gtemp, *gsalt;
   double *gK_iso;
+  /* optional (NULL: natural order): the interior columns in the order the
+   * transposed solve takes them, as VgStepFields.column_order */
+  const int32_t *column_order;
 } VgAdjointFields;
 
 size_t vg_isoneutral_step_adjoint_scratch_bytes(const VgDomain *dom);

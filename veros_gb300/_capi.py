@@ -86,7 +86,8 @@ class VgEnsembleMemberF32(ctypes.Structure):
 
 class VgAdjointFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp", "salt", "temp_new", "salt_new", "K_iso", "mask_bits", "kbot",
-                                                "gtemp_new", "gsalt_new", "gtemp", "gsalt", "gK_iso")]
+                                                "gtemp_new", "gsalt_new", "gtemp", "gsalt", "gK_iso",
+                                                "column_order")]
 
 
 # name -> (restype, argtypes); the exported C ABI

@@ -112,7 +112,8 @@ class IsoneutralAdjoint:
         dev = self.dev
         f = _capi.VgAdjointFields(T.data_ptr(), S.data_ptr(), T_new.data_ptr(), S_new.data_ptr(), K.data_ptr(),
                                   dev.mask_bits().data_ptr(), dev.variables.kbot.data_ptr(), gT_new.data_ptr(),
-                                  gS_new.data_ptr(), gT.data_ptr(), gS.data_ptr(), gK.data_ptr())
+                                  gS_new.data_ptr(), gT.data_ptr(), gS.data_ptr(), gK.data_ptr(),
+                                  dev.column_order().data_ptr())
         _capi.check(self.lib.vg_isoneutral_step_adjoint_f64(self._dom, self._grid, self._set, f, self._work.data_ptr(),
                                                             self._work.numel() * 8, self._stream()),
                     "isoneutral step adjoint")
@@ -131,8 +132,8 @@ class IsoneutralAdjoint:
         return T, S
 
     # launches per forward and backward step (for launch accounting)
-    forward_launches = 1 + 1 + 1 + 1  # prepare, pre, flux (temp and salt), implicit
-    backward_launches = 5
+    forward_launches = 1 + 1 + 1 + 1  # rim preparation, pre, flux (temp and salt), implicit
+    backward_launches = 6  # tables, pre, transposed solve, active list, slopes, gather
 
 
 class _IsoneutralStep(torch.autograd.Function):

@@ -21,17 +21,23 @@
 //   2. pre_span_kernel       the step's tensor K_11, K_22, K_33 (the forward kernel), and
 //                            per point its 8 tapers, 8 slopes and 2 clamped reciprocals
 //   3. adj_implicit_kernel   per water column: the transposed tridiagonal
-//                            system A^T y = dL/dx (one Thomas factorisation
-//                            for temp and salt) and dL/dK_33 from
+//                            system A^T y = dL/dx (temp and salt on two
+//                            threads sharing the Thomas factorisation, columns
+//                            deepest first) and dL/dK_33 from
 //                            dL/ddelta_k = (x_{k+1} - x_k)(y_k/dzt_k - y_{k+1}/dzt_{k+1})
-//   4. adj_slope_kernel      per point: the eight slope adjoints (from the stored
-//                            tapers and slopes), written as per-point partial
-//                            sums onto the point's faces
+//   4. adj_active_kernel     zero partial sums of the points whose faces carry no
+//                            term; the others listed
+//      adj_slope_kernel      per listed point: the eight slope adjoints (from the
+//                            stored tapers and slopes), written as per-point
+//                            partial sums onto the point's faces
 //   5. adj_gather_kernel     per point: sums the partials of the faces around
 //                            it into dL/dT_n, dL/dS_n and dL/dK_iso
 //
 // Every partial is written exactly once by the point that owns it and read
 // by its neighbours in the next launch: no atomics, results are deterministic.
+#include <algorithm>
+#include <climits>
+
 #include "common.cuh"
 #include "pre_kernels.cuh"
 
@@ -68,9 +74,13 @@ inline size_t table_doubles(const Layout &L) { return 3 * (size_t)L.X + 4 * (siz
 
 inline size_t field_doubles(const Layout &L) { return (size_t)L.plane * L.Z; }
 
+// doubles before the active-point list (fields, then the grid tables)
+inline size_t list_offset(const Layout &L) { return (size_t)kFields * field_doubles(L) + table_doubles(L); }
+
+// fields, tables, then the active-point list (one int32 per point) and its count
 inline size_t scratch_bytes(const Layout &L) {
-  size_t n = (size_t)kFields * field_doubles(L) + table_doubles(L);
-  return (n * sizeof(double) + 255) & ~(size_t)255;
+  size_t n = list_offset(L) * sizeof(double) + (field_doubles(L) + 1) * sizeof(int32_t);
+  return (n + 255) & ~(size_t)255;
 }
 
 GridInv tables_of(const Layout &L, const double *t) {
@@ -136,6 +146,7 @@ struct ImpArgs {
   double *gTp, *gSp, *gK33;  // dL/d(right-hand side), dL/dK_33
   double *nu;                // the scaled adjoint sources of the explicit part (F_NU)
   long long field;
+  const int32_t *__restrict__ col_order;  // interior columns, deepest first (optional)
 };
 
 // Row k of the forward matrix: a_k = -delta_{k-1}/dzt_k, c_k = -delta_k/dzt_k,
@@ -143,34 +154,58 @@ struct ImpArgs {
 // ks), delta_k = dt K_33/dzw_k (0 on the top level). The transposed system
 // has sub-diagonal c_{k-1} and super-diagonal a_{k+1}; A is row diagonally
 // dominant, so A^T is column diagonally dominant and needs no pivoting.
-__global__ void __launch_bounds__(64) adj_implicit_kernel(ImpArgs a) {
+// Temp and salt of a column on two neighbouring threads (lane 2c: temp,
+// 2c+1: salt), which both form the shared factorisation; the lane of temp
+// stores c'_k, each lane its own d'_k, so a CTA holds 1.5 Z doubles per
+// thread in shared memory and twice the warps hide the recurrence.
+__global__ void __launch_bounds__(128) adj_implicit_kernel(ImpArgs a) {
   extern __shared__ double smem[];
   const Layout &L = a.L;
-  const int Z = L.Z, nb = blockDim.x, t = threadIdx.x;
-  double *cps = smem;                   // [k][thread]
-  double *dps = smem + (size_t)Z * nb;  // [r][k][thread]
-  const int col = blockIdx.x * nb + t;
-  if (col >= L.X * L.Y) return;
-  const int i = col % L.X, j = col / L.X;
+  const int Z = L.Z, nb = blockDim.x, nc = nb / 2, t = threadIdx.x, c = t >> 1, r = t & 1;
+  const unsigned pair = 3u << ((t & 31) & ~1);
+  double *cps = smem;                   // [k][column]
+  double *dps = smem + (size_t)Z * nc;  // [k][thread]
+  // slots: the interior columns (in col_order: the lanes of a warp then walk
+  // columns of similar depth), then the two-column rim
+  const int slot = blockIdx.x * nc + c;
+  if (slot >= L.X * L.Y) return;
+  const int nx = L.X - 4, nint = nx * (L.Y - 4);
+  int i, j;
+  if (slot < nint) {
+    const int col = a.col_order ? __ldg(a.col_order + slot) : slot;
+    i = 2 + col % nx;
+    j = 2 + col / nx;
+  } else if (slot - nint < 4 * L.X) {
+    const int q = slot - nint, jr = q / L.X;
+    i = q % L.X;
+    j = jr < 2 ? jr : L.Y - 4 + jr;
+  } else {
+    const int q = slot - nint - 4 * L.X, cc = q % 4;
+    i = cc < 2 ? cc : L.X - 4 + cc;
+    j = 2 + q / 4;
+  }
   const long long base = L.at2(i, j);
   const bool interior = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
   const int ks = interior ? a.kbot[base] - 1 : -1;  // create_water_masks (utilities.py:38-48)
   const int kw = (ks >= 0 && ks < Z) ? ks : Z;
   const long long F = a.field;
+  const double *gn = r ? a.gSn : a.gTn;  // this lane's tracer
+  const double *xn = r ? a.xS : a.xT;
+  double *gp = r ? a.gSp : a.gTp;
+  double *nu = a.nu + 3 * r * F;
   // cells outside the solve pass their adjoint through; dry or halo cells have no explicit part
   for (int k = 0; k < kw; ++k) {
     const long long o = base + (long long)k * L.plane;
-    a.gTp[o] = a.gTn[o];
-    a.gSp[o] = a.gSn[o];
-    a.gK33[o] = 0.0;
+    gp[o] = gn[o];
+    if (r == 0) a.gK33[o] = 0.0;
 #pragma unroll
-    for (int n = 0; n < 6; ++n) a.nu[n * F + o] = 0.0;
+    for (int n = 0; n < 3; ++n) nu[n * F + o] = 0.0;
   }
   if (kw == Z) return;
   // the explicit tendency's metric factors (diffusion.py:116-139)
   const double fx = a.dt * a.gi.inv_dxt[i] * a.gi.inv_cost[j], fy = a.dt * a.gi.inv_dyt[j] * a.gi.inv_cost[j];
 
-  double cp = 0.0, dp0 = 0.0, dp1 = 0.0, delta_prev = 0.0;
+  double cp = 0.0, dp = 0.0, delta_prev = 0.0;
   for (int k = ks; k < Z; ++k) {
     const long long o = base + (long long)k * L.plane;
     const double delta = k < Z - 1 ? a.dt * a.gi.inv_dzw[k] * a.K33[o] : 0.0;
@@ -179,40 +214,27 @@ __global__ void __launch_bounds__(64) adj_implicit_kernel(ImpArgs a) {
     const double sup = k < Z - 1 ? -delta * a.gi.inv_dzt[k + 1] : 0.0;
     const double inv = 1.0 / (b - sub * cp);
     cp = sup * inv;
-    dp0 = (a.gTn[o] - sub * dp0) * inv;
-    dp1 = (a.gSn[o] - sub * dp1) * inv;
-    cps[(size_t)k * nb + t] = cp;
-    dps[(size_t)k * nb + t] = dp0;
-    dps[((size_t)Z + k) * nb + t] = dp1;
+    dp = (gn[o] - sub * dp) * inv;
+    if (r == 0) cps[(size_t)k * nc + c] = cp;
+    dps[(size_t)k * nb + t] = dp;
     delta_prev = delta;
   }
-  double y0 = 0.0, y1 = 0.0, xu0 = 0.0, xu1 = 0.0;  // values one level up
+  __syncwarp(pair);  // c'_k of the temp lane is visible to the salt lane
+  double y = 0.0, xu = 0.0;  // values one level up
   for (int k = Z - 1; k >= ks; --k) {
     const long long o = base + (long long)k * L.plane;
-    const double c = cps[(size_t)k * nb + t];
-    const double n0 = dps[(size_t)k * nb + t] - c * y0;
-    const double n1 = dps[((size_t)Z + k) * nb + t] - c * y1;
-    const double x0 = a.xT[o], x1 = a.xS[o];
-    double gk = 0.0;
-    if (k < Z - 1) {
-      const double r0 = a.gi.inv_dzt[k], r1 = a.gi.inv_dzt[k + 1];
-      const double ld = (xu0 - x0) * (n0 * r0 - y0 * r1) + (xu1 - x1) * (n1 * r0 - y1 * r1);
-      gk = ld * a.dt * a.gi.inv_dzw[k];
-    }
-    a.gTp[o] = n0;
-    a.gSp[o] = n1;
-    a.gK33[o] = gk;
-    const double fz = a.dt * a.gi.inv_dzt[k];
-    a.nu[o] = n0 * fx;
-    a.nu[F + o] = n0 * fy;
-    a.nu[2 * F + o] = n0 * fz;
-    a.nu[3 * F + o] = n1 * fx;
-    a.nu[4 * F + o] = n1 * fy;
-    a.nu[5 * F + o] = n1 * fz;
-    y0 = n0;
-    y1 = n1;
-    xu0 = x0;
-    xu1 = x1;
+    const double n = dps[(size_t)k * nb + t] - cps[(size_t)k * nc + c] * y;
+    const double x = xn[o];
+    // dL/ddelta_k = sum over the tracers of (x_{k+1} - x_k)(y_k/dzt_k - y_{k+1}/dzt_{k+1})
+    const double part = k < Z - 1 ? (xu - x) * (n * a.gi.inv_dzt[k] - y * a.gi.inv_dzt[k + 1]) : 0.0;
+    const double other = __shfl_xor_sync(pair, part, 1);
+    if (r == 0) a.gK33[o] = k < Z - 1 ? (part + other) * a.dt * a.gi.inv_dzw[k] : 0.0;
+    gp[o] = n;
+    nu[o] = n * fx;
+    nu[F + o] = n * fy;
+    nu[2 * F + o] = n * (a.dt * a.gi.inv_dzt[k]);
+    y = n;
+    xu = x;
   }
 }
 
@@ -238,12 +260,40 @@ struct SlopeArgs {
   long long field;
 };
 
-__global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
+// Which faces of point (i, j, k) carry a term of the forward: face h (the
+// east/north terms, vE) and face v (the top terms, vT), from the masks and
+// the position alone. A point with none has all its partial sums zero.
+struct SlopeFaces {
+  bool mH[4], mWv[2], vE[4], vT[2];
+  __device__ __forceinline__ bool any() const { return vE[0] || vE[1] || vE[2] || vE[3] || vT[0] || vT[1]; }
+};
+
+__device__ __forceinline__ SlopeFaces slope_faces(const Layout &L, const uint8_t *m, int i, int j, int k) {
+  const int X = L.X, Y = L.Y, Z = L.Z;
+  const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane;
+  const unsigned mk = __ldg(m + o);
+  const bool hasE = i < X - 1, hasW = i > 0, hasN = j < Y - 1, hasS = j > 0, hasU = k < Z - 1, hasD = k > 0;
+  const bool inter = i >= 2 && i < X - 2 && j >= 2 && j < Y - 2;
+  const bool rowE = j >= 2 && j < Y - 2, colN = i >= 2 && i < X - 2;
+  SlopeFaces f;
+  f.mH[0] = hasE && (mk & VG_MASK_U);
+  f.mH[1] = hasW && (__ldg(m + o - 1) & VG_MASK_U);
+  f.mH[2] = hasN && (mk & VG_MASK_V);
+  f.mH[3] = hasS && (__ldg(m + o - PW) & VG_MASK_V);
+  f.mWv[0] = hasD && (__ldg(m + o - PL) & VG_MASK_W);
+  f.mWv[1] = hasU && (mk & VG_MASK_W);
+  f.vE[0] = rowE && i >= 1 && i < X - 2 && f.mH[0];
+  f.vE[1] = rowE && i >= 2 && i < X - 1 && f.mH[1];
+  f.vE[2] = colN && j >= 1 && j < Y - 2 && f.mH[2];
+  f.vE[3] = colN && j >= 2 && j < Y - 1 && f.mH[3];
+  f.vT[0] = inter && f.mWv[0];
+  f.vT[1] = inter && f.mWv[1];
+  return f;
+}
+
+// The slope adjoints of one point whose faces carry a term
+__device__ __forceinline__ void adj_slope_point(const SlopeArgs &a, const SlopeFaces &sf, int i, int j, int k) {
   const Layout &L = a.L;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (i >= L.X || j >= L.Y) return;
   const int X = L.X, Y = L.Y, Z = L.Z;
   const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane;
   const GridInv &gi = a.gi;
@@ -251,7 +301,6 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const unsigned mk = __ldg(m + o);
   const bool hasE = i < X - 1, hasW = i > 0, hasN = j < Y - 1, hasS = j > 0, hasU = k < Z - 1, hasD = k > 0;
   const bool inter = i >= 2 && i < X - 2 && j >= 2 && j < Y - 2;
-  const bool rowE = j >= 2 && j < Y - 2, colN = i >= 2 && i < X - 2;
   const double Tc = __ldg(a.T + o), Sc = __ldg(a.S + o);
   const long long F = a.field;
   // tracer differences across the faces (unmasked) and the face masks
@@ -268,9 +317,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   vdS[0] = hasD ? Sc - __ldg(a.S + o - PL) : 0.0;
   vdT[1] = hasU ? __ldg(a.T + o + PL) - Tc : 0.0;
   vdS[1] = hasU ? __ldg(a.S + o + PL) - Sc : 0.0;
-  const bool mH[4] = {hasE && (mk & VG_MASK_U), hasW && (__ldg(m + o - 1) & VG_MASK_U),
-                      hasN && (mk & VG_MASK_V), hasS && (__ldg(m + o - PW) & VG_MASK_V)};
-  const bool mWv[2] = {hasD && (__ldg(m + o - PL) & VG_MASK_W), hasU && (mk & VG_MASK_W)};
+  const bool *mH = sf.mH, *mWv = sf.mWv;
 
   // masked metric factors of the face gradients and the temperature gradients (isoneutral.py:46-95)
   const double icx = gi.inv_cost[j];
@@ -291,9 +338,7 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   const double R[2] = {__ldg(a.slopes + o + detail::SLOPE_R * F), __ldg(a.slopes + o + (detail::SLOPE_R + 1) * F)};
 
   // which faces carry a term: face h (east/north terms) and face v (top terms)
-  const bool vE[4] = {rowE && i >= 1 && i < X - 2 && mH[0], rowE && i >= 2 && i < X - 1 && mH[1],
-                      colN && j >= 1 && j < Y - 2 && mH[2], colN && j >= 2 && j < Y - 1 && mH[3]};
-  const bool vT[2] = {inter && mWv[0], inter && mWv[1]};
+  const bool *vE = sf.vE, *vT = sf.vT;
 
   // adjoints of the fluxes on the faces (diffusion.py:116-139) from the
   // scaled sources nu: lambda_fe(i) = nu_x(i) - nu_x(i+1), and so on
@@ -445,6 +490,49 @@ __global__ void __launch_bounds__(128) adj_slope_kernel(SlopeArgs a) {
   }
 }
 
+// Active-point list: a point whose faces carry no term has all its partial
+// sums zero, which this pass writes; the others are appended to the list
+// (one atomic per warp, the lanes of a warp in x order), so that the slope
+// pass runs whole warps of points with terms: an FP64 warp instruction costs
+// the same however few of its lanes are active, and most points of a warp
+// row are dry on most levels. Block (32, 4): a warp is one x row.
+__global__ void __launch_bounds__(128) adj_active_kernel(Layout L, const uint8_t *__restrict__ m, double *part,
+                                                         long long F, int32_t *list, int *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  const bool in = i < L.X && j < L.Y;
+  const bool act = in && slope_faces(L, m, i, j, k).any();
+  const long long o = in ? L.at(i, j, k) : 0;
+  if (in && !act) {
+#pragma unroll
+    for (int n = 0; n < P_N; ++n) part[n * F + o] = 0.0;
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, act);
+  if (!ball) return;
+  const int lane = threadIdx.x & 31, leader = __ffs(ball) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(count, __popc(ball));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (act) list[base + __popc(ball & ((1u << lane) - 1u))] = (int32_t)o;
+}
+
+// The slope pass over the active list: persistent threads, grid-stride.
+// Three CTAs per SM: 168 registers (14.8 against 15.0 ms for the 8-step
+// backward at 360 x 180 x 30 with the unbounded 184).
+__global__ void __launch_bounds__(128, 3) adj_slope_kernel(SlopeArgs a, const int32_t *__restrict__ list,
+                                                        const int *__restrict__ count) {
+  const int n = *count;
+  const Layout &L = a.L;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const long long o = __ldg(list + t);
+    const int k = (int)(o / L.plane);
+    const long long r = o - (long long)k * L.plane;
+    const int j = (int)(r / L.pitch), i = (int)(r - (long long)j * L.pitch);
+    adj_slope_point(a, slope_faces(L, a.m, i, j, k), i, j, k);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // 5. gather onto points
 // ---------------------------------------------------------------------------
@@ -554,6 +642,8 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   if (!scratch || scratch_bytes < need)
     return fail(VG_ERR_SCRATCH, "adjoint scratch of %zu bytes given, %zu needed", scratch_bytes, need);
   if (L.Z > 200) return fail(VG_ERR_SHAPE, "Z=%d above the 200 levels supported", L.Z);
+  if (adj::field_doubles(L) >= (size_t)INT_MAX)
+    return fail(VG_ERR_SHAPE, "%zu points per field: the active-point list indexes below 2^31", adj::field_doubles(L));
   cudaStream_t s = as_stream(stream);
   double *base = static_cast<double *>(scratch);
   const long long F = (long long)adj::field_doubles(L);
@@ -588,29 +678,40 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   // 3. implicit part
   {
     adj::ImpArgs a{L,   gi,  set->dt_tracer, f->kbot, ten.K_33, f->temp_new, f->salt_new, f->gtemp_new,
-                   f->gsalt_new, gTp, gSp, gK33, nu, F};
-    int nb = 64;
-    size_t smem = 3 * (size_t)L.Z * nb * sizeof(double);
-    if (smem > 160 * 1024) {
-      nb = 32;
-      smem /= 2;
-    }
+                   f->gsalt_new, gTp, gSp, gK33, nu, F, f->column_order};
+    // two threads per column, c' per column and d' per thread in shared memory
+    int nb = 128;
+    while (nb > 32 && 3 * (size_t)L.Z * (nb / 2) * sizeof(double) > 160 * 1024) nb /= 2;
+    const size_t smem = 3 * (size_t)L.Z * (nb / 2) * sizeof(double);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(adj::adj_implicit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
       if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "adj_implicit_kernel smem %zu: %s", smem, cudaGetErrorString(e));
     }
-    const int ncols = L.X * L.Y;
-    adj::adj_implicit_kernel<<<(ncols + nb - 1) / nb, nb, smem, s>>>(a);
+    const int ncols = L.X * L.Y, nc = nb / 2;
+    adj::adj_implicit_kernel<<<(ncols + nc - 1) / nc, nb, smem, s>>>(a);
     if ((st = check_launch("adj_implicit_kernel"))) return st;
   }
   const dim3 block(32, 4), grd((L.X + 31) / 32, (L.Y + 3) / 4, L.Z);
-  // 4. slope adjoints
+  // 4. slope adjoints: the points whose faces carry terms, listed, then the slope pass over the list
   {
+    int32_t *list = reinterpret_cast<int32_t *>(base + adj::list_offset(L));
+    int *count = list + F;
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
+    if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "adjoint list count: %s", cudaGetErrorString(e));
+    adj::adj_active_kernel<<<grd, block, 0, s>>>(L, f->mask_bits, part, F, list, count);
+    if ((st = check_launch("adj_active_kernel"))) return st;
     adj::SlopeArgs a{L,      g,    gi,       set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
                      set->K_iso_steep, f->temp, f->salt, f->K_iso, gK33, f->mask_bits, slopes, nu, ten.K_11,
                      ten.K_22, part, F};
-    adj::adj_slope_kernel<<<grd, block, 0, s>>>(a);
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, adj::adj_slope_kernel, 128, 0) != cudaSuccess || per < 1)
+      return fail(VG_ERR_LAUNCH, "adj_slope_kernel: occupancy query failed");
+    const long long want = ((long long)F + 127) / 128;
+    const int nblk = (int)std::min<long long>(want, (long long)sms * per);
+    adj::adj_slope_kernel<<<nblk, 128, 0, s>>>(a, list, count);
     if ((st = check_launch("adj_slope_kernel"))) return st;
   }
   // 5. gather

@@ -198,6 +198,14 @@ template <>
 __device__ __forceinline__ float to_F<float>(double x) {
   return d2f_int(x);
 }
+// D (FP64 or F) to F
+template <typename F, typename D>
+__device__ __forceinline__ F as_F(D x) {
+  if constexpr (sizeof(D) == sizeof(F))
+    return x;
+  else
+    return to_F<F>(x);
+}
 __device__ __forceinline__ double to_D(double x) { return x; }
 __device__ __forceinline__ double to_D(float x) { return f2d_int(x); }
 

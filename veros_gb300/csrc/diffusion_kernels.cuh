@@ -124,13 +124,14 @@ __device__ __forceinline__ void east_coef(const DiffArgs<F> &a, long long o, F d
 // flux of one tracer through a face from the face coefficients and the
 // tracer differences: the two lower and the two upper vertical differences
 // of the face's points, and the difference across the face
-template <typename F>
-__device__ __forceinline__ F face_flux(const F c[6], double z0m, double z1m, double z0p, double z1p, double h) {
-  F sumz = pm(c[0], to_F<F>(z0m));
-  sumz = pfma(c[1], to_F<F>(z1m), sumz);
-  sumz = pfma(c[2], to_F<F>(z0p), sumz);
-  sumz = pfma(c[3], to_F<F>(z1p), sumz);
-  return pfma(sumz, c[5], pm(to_F<F>(h), c[4]));
+// (differences in FP64 or already converted to F)
+template <typename F, typename D>
+__device__ __forceinline__ F face_flux(const F c[6], D z0m, D z1m, D z0p, D z1p, D h) {
+  F sumz = pm(c[0], as_F<F>(z0m));
+  sumz = pfma(c[1], as_F<F>(z1m), sumz);
+  sumz = pfma(c[2], as_F<F>(z0p), sumz);
+  sumz = pfma(c[3], as_F<F>(z1p), sumz);
+  return pfma(sumz, c[5], pm(as_F<F>(h), c[4]));
 }
 
 template <typename F>
@@ -189,17 +190,16 @@ __device__ __forceinline__ void top_coef(const DiffArgs<F> &a, long long o, F qx
 
 // top flux of one tracer from the west, east, south and north differences on
 // the face's lower (k) and upper (k+1) levels
-template <typename F>
-__device__ __forceinline__ F top_face_flux(const F c[10], double w0, double w1, double e0, double e1, double s0,
-                                           double s1, double n0, double n1) {
-  F sumx = pm(c[0], to_F<F>(w0));
-  sumx = pfma(c[1], to_F<F>(w1), sumx);
-  sumx = pfma(c[2], to_F<F>(e0), sumx);
-  sumx = pfma(c[3], to_F<F>(e1), sumx);
-  F sumy = pm(c[4], to_F<F>(s0));
-  sumy = pfma(c[5], to_F<F>(s1), sumy);
-  sumy = pfma(c[6], to_F<F>(n0), sumy);
-  sumy = pfma(c[7], to_F<F>(n1), sumy);
+template <typename F, typename D>
+__device__ __forceinline__ F top_face_flux(const F c[10], D w0, D w1, D e0, D e1, D s0, D s1, D n0, D n1) {
+  F sumx = pm(c[0], as_F<F>(w0));
+  sumx = pfma(c[1], as_F<F>(w1), sumx);
+  sumx = pfma(c[2], as_F<F>(e0), sumx);
+  sumx = pfma(c[3], as_F<F>(e1), sumx);
+  F sumy = pm(c[4], as_F<F>(s0));
+  sumy = pfma(c[5], as_F<F>(s1), sumy);
+  sumy = pfma(c[6], as_F<F>(n0), sumy);
+  sumy = pfma(c[7], as_F<F>(n1), sumy);
   return pfma(sumx, c[8], pm(sumy, c[9]));
 }
 
@@ -370,13 +370,14 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   // per tracer the values at the own, east and north columns, their vertical
   // differences t(k) - t(k-1) (0 at k = 0, edge padding), and the four
   // horizontal differences around the own point; each level loads the level
-  // above once and forms its differences once. The K pair sums of the east
+  // above once and forms its differences once, in FP64, converted to F once
+  // (each difference serves two levels' faces). The K pair sums of the east
   // and north faces are carried the same way. They start on the column's
   // first wet level (start_column), as on a segment's first level.
   const long long P = L.pitch, Q = L.plane;
   double vc[NTR], ve[NTR], vn[NTR];     // values at level k
-  double dzc[NTR], dze[NTR], dzn[NTR];  // t(k) - t(k-1)
-  double hw[NTR], hs[NTR], he[NTR], hn[NTR];  // west, south, east, north differences at level k
+  F dzc[NTR], dze[NTR], dzn[NTR];  // t(k) - t(k-1)
+  F hw[NTR], hs[NTR], he[NTR], hn[NTR];  // west, south, east, north differences at level k
   F ft_prev[NTR];
   F pe_below = 0, pn_below = 0;  // K pair sums of the east / north face on level k-1
 #pragma unroll
@@ -392,14 +393,14 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       vc[r] = __ldg(tr + ob);
       ve[r] = __ldg(tr + ob + 1);
       vn[r] = __ldg(tr + ob + P);
-      hw[r] = vc[r] - __ldg(tr + ob - 1);
-      hs[r] = vc[r] - __ldg(tr + ob - P);
-      he[r] = ve[r] - vc[r];
-      hn[r] = vn[r] - vc[r];
+      hw[r] = to_F<F>(vc[r] - __ldg(tr + ob - 1));
+      hs[r] = to_F<F>(vc[r] - __ldg(tr + ob - P));
+      he[r] = to_F<F>(ve[r] - vc[r]);
+      hn[r] = to_F<F>(vn[r] - vc[r]);
       if (k0 > 0) {
-        dzc[r] = vc[r] - __ldg(tr + ob - Q);
-        dze[r] = ve[r] - __ldg(tr + ob + 1 - Q);
-        dzn[r] = vn[r] - __ldg(tr + ob + P - Q);
+        dzc[r] = to_F<F>(vc[r] - __ldg(tr + ob - Q));
+        dze[r] = to_F<F>(ve[r] - __ldg(tr + ob + 1 - Q));
+        dzn[r] = to_F<F>(vn[r] - __ldg(tr + ob + P - Q));
       }
     }
     if (k0 > 0) {
@@ -457,12 +458,13 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
 #pragma unroll
       for (int r = 0; r < NTR; ++r) {
         // z differences above the own, east and north columns (0 on the top level)
-        const double zc = uc[r] - vc[r], ze = ue[r] - ve[r], zn = un[r] - vn[r];
+        const F zc = to_F<F>(uc[r] - vc[r]), ze = to_F<F>(ue[r] - ve[r]), zn = to_F<F>(un[r] - vn[r]);
         // east face (diffusion.py:25-47), north face (:52-77)
         fe[r] = face_flux(ce, dzc[r], dze[r], zc, ze, he[r]);
         fn[r] = pm(cosu_c, face_flux(cn, dzc[r], dzn[r], zc, zn, hn[r]));
         // horizontal differences on level k+1
-        const double hw1 = uc[r] - uw[r], he1 = ue[r] - uc[r], hs1 = uc[r] - us[r], hn1 = un[r] - uc[r];
+        const F hw1 = to_F<F>(uc[r] - uw[r]), he1 = to_F<F>(ue[r] - uc[r]);
+        const F hs1 = to_F<F>(uc[r] - us[r]), hn1 = to_F<F>(un[r] - uc[r]);
         if (up) ft[r] = top_face_flux(ct, hw[r], hw1, he[r], he1, hs[r], hs1, hn[r], hn1);  // (diffusion.py:85-111)
         vc[r] = uc[r];
         ve[r] = ue[r];

@@ -13,11 +13,15 @@ namespace vg {
 namespace {
 
 // NTR = 2: temp and salt in one pass over the tensor (b: salt); NTR = 1: a alone
-// Tiles of 32 x 8 columns (flux_span_kernel): one CTA per tile on large
-// domains, else every resident CTA with an equal share of the tile-levels.
+// Tiles of 32 x 8 columns in the FP64 form, 32 x 4 in the split form
+// (flux_span_kernel): one CTA per tile on large domains, else every resident
+// CTA with an equal share of the tile-levels. The split form's flux kernel is
+// latency-bound at 128 registers a thread; on 4-warp tiles its level barriers
+// wait for fewer warps (1 degree: 0.530 against 0.541 ms for the diffusion
+// stage; more CTAs per SM by a tighter register budget spill and gain nothing).
 template <typename F, int NTR>
 int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
-  constexpr int TY = 8;
+  constexpr int TY = sizeof(F) == sizeof(float) ? 4 : 8;
   const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
   const size_t smem = flux_smem_bytes(a.L.Z);
   const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, nbx * nby, a.L.Z, 8);
