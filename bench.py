@@ -266,6 +266,39 @@ def _reference_kernel_ab_line():
         return {"unavailable": (str(e).splitlines() or ["error"])[0]}
 
 
+def _dropin_loop(states, nloop):
+    """Cells/s of looping the drop-in functions over the members as Veros's
+    thermodynamics calls them (thermodynamics.py:226-241 with zero advection,
+    :425-432): new level and zeroed tendencies by tensor operations, then
+    isoneutral_diffusion_pre and isoneutral_diffusion for temp and salt on the
+    device-resident state. Wall clock over ``nloop`` sweeps after one warm-up
+    sweep; the members advance by those steps."""
+    import torch
+
+    import veros_gb300 as vg
+
+    def one(dev):
+        v = dev.variables
+        v.temp[..., v.taup1] = v.temp[..., v.tau] * v.maskT
+        v.salt[..., v.taup1] = v.salt[..., v.tau] * v.maskT
+        v.dtemp_iso.zero_()
+        v.dsalt_iso.zero_()
+        v.update(vg.isoneutral_diffusion_pre(dev))
+        vg.isoneutral_diffusion(dev, v.temp, True)
+        vg.isoneutral_diffusion(dev, v.salt, False)
+        v.taum1, v.tau, v.taup1 = v.tau, v.taup1, v.taum1
+
+    for dev in states:
+        one(dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(nloop):
+        for dev in states:
+            one(dev)
+    torch.cuda.synchronize()
+    return sum(d.nx * d.ny * d.nz for d in states) * nloop / (time.perf_counter() - t0)
+
+
 def run_ensemble(device, steps=20):
     """48 members of uneven extents: looping the single-domain step versus the
     batched persistent launches replayed from a CUDA graph of ``steps`` steps,
@@ -293,6 +326,7 @@ def run_ensemble(device, steps=20):
                 st.step(1)
         torch.cuda.synchronize()
         loop_value = cells * nloop / (time.perf_counter() - t0)
+        dropin_value = _dropin_loop(states, nloop) if precision == "f64" else None
         ens = Ensemble(states)
         tuning, timings = ens.autotune(steps=1)
         ens.replay(steps)  # records the graph for this phase and warms it
@@ -308,6 +342,9 @@ def run_ensemble(device, steps=20):
                           "ms_per_step": ms / steps,
                           "looped_single_domain_cells_per_s": loop_value,
                           "speedup_vs_loop": cells * steps / (ms / 1e3) / loop_value,
+                          "looped_dropin_cells_per_s": dropin_value,
+                          "speedup_vs_dropin_loop": (cells * steps / (ms / 1e3) / dropin_value
+                                                     if dropin_value else None),
                           "tuning": tuning, "candidates_timed": len(timings)}
         ens.close()
         del ens, steppers, states

@@ -8,7 +8,8 @@
 // diffusion_kernels.cuh). No CTA ever waits for another. The time-level
 // rotation is handled by three argument tables, one per phase; a step is
 // four launches plus one counter reset, so a rollout captures into a CUDA
-// graph. Tile height (columns per CTA), k-chunk and solver CTA size are
+// graph. As in the single-domain step, the prepare stage covers the two-cell
+// rim and the flux stage prepares the interior cells it updates. Tile height (columns per CTA), k-chunk and solver CTA size are
 // tuning parameters chosen by the caller (the Python autotuner).
 //
 // Why four launches and not one: every stage reads what the previous one
@@ -43,13 +44,25 @@ struct MemberArgs {
   DiffArgs<F> dT, dS;
 };
 
-// The prepare stage (new level, zeroed tendencies) of one level of one member.
+// The prepare stage (new level, zeroed tendencies) of the two-cell rim of one
+// level of one member; the flux stage prepares the interior cells
+// (DiffArgs::fuse_prepare).
 template <typename F>
 __device__ __forceinline__ void prepare_body(const DiffArgs<F> &t, const DiffArgs<F> &s, const double *T0,
                                              const double *S0, int k) {
   const Layout &L = t.L;
-  for (int p = threadIdx.x; p < L.X * L.Y; p += blockDim.x) {
-    const int i = p % L.X, j = p / L.X;
+  const int nrim = 4 * L.X + 4 * (L.Y - 4);
+  for (int p = threadIdx.x; p < nrim; p += blockDim.x) {
+    int i, j;
+    if (p < 4 * L.X) {
+      const int jr = p / L.X;
+      i = p % L.X;
+      j = jr < 2 ? jr : L.Y - 4 + jr;
+    } else {
+      const int q = p - 4 * L.X, c = q % 4;
+      i = c < 2 ? c : L.X - 4 + c;
+      j = 2 + q / 4;
+    }
     const long long o = L.at(i, j, k);
     const double mT = (__ldg(t.m + o) & VG_MASK_T) ? 1.0 : 0.0;
     t.trp[o] = T0[o] * mT;
@@ -431,6 +444,7 @@ int member_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *se
         (st = make_diff_args<F>(dom, grid, set, &f.ten, f.K_iso, f.mask_bits, f.kbot, &trS, 0, nullptr, out[p].dS)))
       return st;
     out[p].dT.kchunk = out[p].dS.kchunk = dom->Z;
+    out[p].dT.fuse_prepare = out[p].dS.fuse_prepare = 1;  // the flux stage prepares the interior
     out[p].dT.col_order = out[p].dS.col_order = f.column_order;  // optional per member
     tau[2 * p] = f.temp_tau;
     tau[2 * p + 1] = f.salt_tau;
