@@ -15,8 +15,10 @@ oracle (the reference algorithm, ``isoneutral_oracle.isoneutral_step``) in
 and compares its central differences along 16 seeded random unit directions
 (6 temp, 5 salt, 5 K_iso) with the CUDA adjoint's directional derivatives.
 
-    python oracle/adjoint_fd_check.py cpu CPU.json [procs]   # longdouble differences + NumPy adjoint
-    python oracle/adjoint_fd_check.py gpu GPU.json           # on a GPU: the CUDA adjoint
+    python oracle/adjoint_fd_check.py cpu CPU.json [procs]       # longdouble differences + NumPy adjoint
+    python oracle/adjoint_fd_check.py kinkfree CPU.json [procs]  # smaller steps, slope sign changes
+                                                                 # counted; the adjoint in longdouble
+    python oracle/adjoint_fd_check.py gpu GPU.json               # on a GPU: the CUDA adjoint
     python oracle/adjoint_fd_check.py compare CPU.json GPU.json
 
 The CPU mode evaluates the longdouble central differences and, on the same
