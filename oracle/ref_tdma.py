@@ -2,10 +2,10 @@
 (``TridiagKernel`` of veros/core/special/cuda_tdma_kernels.cu:19-63) for an
 A/B against ``vg_tdma_cuda_{double,float}`` on the same GPU.
 
-* ``build_cubin()`` compiles the reference source where it lies (given by
-  ``REF_ROOT`` or the default checkout path) for sm_103a into
-  ``oracle/_ref/cuda_tdma_kernels.cubin`` with nvcc, nothing else; without the
-  reference checkout it does nothing, and a cubin built earlier is used as is.
+* ``build_cubin(ref_root)`` compiles the reference source where it lies (the
+  checkout given as the argument or by ``REF_ROOT``) for sm_103a into
+  ``oracle/_ref/cuda_tdma_kernels.cubin`` with nvcc, nothing else; without a
+  checkout it does nothing, and a cubin built earlier is used as is.
 * ``build_launcher()`` compiles ``oracle/ref_tdma_launch.c`` (a driver-API
   launcher with the reference launcher's configuration) into
   ``oracle/_ref/libref_tdma_launch.so``.
@@ -27,20 +27,12 @@ LAUNCHER = os.path.join(OUT, "libref_tdma_launch.so")
 REF_SOURCE = os.path.join("veros", "core", "special", "cuda_tdma_kernels.cu")
 
 
-# Where this build recipe finds the reference sources it compiles: the
-# REF_ROOT environment variable, else the checkout location of the build
-# container. GPU machines have neither; there the cubin built beforehand is used.
-_DEFAULT_CHECKOUT = os.path.join(os.sep, "root", "reference")
-
-
-def _ref_root():
-    return os.environ.get("REF_ROOT", _DEFAULT_CHECKOUT)
-
-
-def reference_root():
-    """The reference checkout the test infrastructure may import from, or None."""
-    root = _ref_root()
-    return root if os.path.isdir(os.path.join(root, "veros")) else None
+def reference_root(root=None):
+    """The reference checkout (the argument, else the ``REF_ROOT`` environment
+    variable) if it holds the Veros sources, else None. There is no default:
+    GPU machines have no checkout, and there the cubin built beforehand is used."""
+    root = root or os.environ.get("REF_ROOT")
+    return root if root and os.path.isdir(os.path.join(root, "veros")) else None
 
 
 def _nvcc():
@@ -49,10 +41,11 @@ def _nvcc():
     return path if os.path.exists(path) else shutil.which("nvcc")
 
 
-def build_cubin():
+def build_cubin(ref_root=None):
     """Compile the reference kernel source for sm_103a; returns the cubin path or None."""
-    src = os.path.join(_ref_root(), REF_SOURCE)
-    if not os.path.exists(src):
+    root = reference_root(ref_root)
+    src = os.path.join(root, REF_SOURCE) if root else None
+    if src is None or not os.path.exists(src):
         return CUBIN if os.path.exists(CUBIN) else None
     nvcc = _nvcc()
     if nvcc is None:
@@ -84,10 +77,10 @@ def build_launcher():
     return LAUNCHER
 
 
-def build():
+def build(ref_root=None):
     """Both parts; returns (cubin, launcher), either None when it cannot be built here."""
     try:
-        cubin = build_cubin()
+        cubin = build_cubin(ref_root)
     except (subprocess.CalledProcessError, OSError):
         cubin = None
     try:

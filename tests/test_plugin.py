@@ -54,8 +54,8 @@ def test_the_reference_call_sites_are_covered():
 
 
 def test_install_on_the_reference_modules_when_present():
-    """With the reference checkout at hand (not on GPU machines), every target
-    module and attribute exists in the real Veros and is rebound."""
+    """With a reference checkout given in REF_ROOT, every target module and
+    attribute exists in the real Veros and is rebound (skipped without it)."""
     import importlib
     import os
 
@@ -63,7 +63,7 @@ def test_install_on_the_reference_modules_when_present():
 
     ref = reference_root()
     if ref is None:
-        pytest.skip("reference checkout not present")
+        pytest.skip("no reference checkout (set REF_ROOT)")
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
     try:
         import make_golden
