@@ -120,6 +120,17 @@ struct PreStage<true, TY> {
   unsigned char M[4][ROWS][MW];
 };
 
+// FP32 copies of the per-CTA grid tables the split form's arithmetic reads
+// (the FP64 form reads the double tables themselves), converted once per CTA
+// instead of once per point and level.
+template <typename F, int TY>
+struct SplitTables {};
+template <int TY>
+struct SplitTables<float, TY> {
+  float inv_dxu_cost[Tile<TY>::NP], inv_dyu[Tile<TY>::PY];
+  float dqx[2][Tile<TY>::PX], dqy[2][Tile<TY>::PY];
+};
+
 template <typename F, int TY>
 struct Smem {
   static constexpr int PX = Tile<TY>::PX, PY = Tile<TY>::PY, NP = Tile<TY>::NP;
@@ -132,6 +143,7 @@ struct Smem {
   // K_33 weights of the top face's slopes: dxu(i-1+ip) / (4 dxt(i)) by thread column,
   // cosu(j-1+jp) dyu(j-1+jp) / (4 dyt(j) cost(j)) by thread row
   double dqx[2][PX], dqy[2][PY];
+  SplitTables<F, TY> fv;
   uint8_t qm[2][NP];
   // wet-point ordering of the segment (see pre_tile_body): per plane point
   // the key (first level with a mask bit, counted from the segment's first
@@ -142,12 +154,14 @@ struct Smem {
   short okey[Tile<TY>::NT], olist[Tile<TY>::NT];
   unsigned slot0;  // %warpid of warp 0 (virtual_warp)
   // per level (dynamic tail): dzw, inv_dzw, 1/(4 dzt), eos constant; then
-  // two (Z + 2)-entry int tables for the key histograms / running offsets
+  // two (Z + 2)-entry int tables for the key histograms / running offsets;
+  // in the split form then dzw, 1/(4 dzt) and the eos constant in FP32
 };
 
 template <typename F, int TY>
 constexpr size_t pre_smem_bytes(int Z) {
-  return sizeof(Smem<F, TY>) + 4 * (size_t)Z * sizeof(double) + 2 * ((size_t)Z + 2) * sizeof(int);
+  return sizeof(Smem<F, TY>) + 4 * (size_t)Z * sizeof(double) + 2 * ((size_t)Z + 2) * sizeof(int) +
+         (sizeof(F) == sizeof(float) ? 3 * (size_t)Z * sizeof(float) : 0);
 }
 
 // Stable counting sort of n small keys (0 <= key < nkeys) by one warp:
@@ -295,6 +309,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   double *zinv_dzw = zdzw + Z;
   double *zq_dzt = zinv_dzw + Z;
   double *zeos = zq_dzt + Z;
+  // split form: dzw, 1/(4 dzt) and the eos constant per level in FP32 (after the two int tables)
+  float *zf = reinterpret_cast<float *>(reinterpret_cast<int *>(zeos + Z) + 2 * (Z + 2));
+  constexpr bool kF32 = sizeof(F) == sizeof(float);
 
   const int tid = threadIdx.x;
   const int warp = tid / 32, lane = tid % 32;
@@ -341,18 +358,27 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     const int j = min(max(j0 - 1 + p, 0), L.Y - 1);
     sm.inv_dyu[p] = 1.0 / a.g.dyu[j];
     sm.inv_cost[p] = 1.0 / a.g.cost[j];
+    if constexpr (kF32) sm.fv.inv_dyu[p] = to_F<float>(sm.inv_dyu[p]);
   }
   for (int p = tid; p < TX; p += NT) {
     const int i = min(i0 + p, L.X - 1);
     const double q = 1.0 / (4.0 * a.g.dxt[i]);
     sm.dqx[0][p] = a.g.dxu[i - 1] * q;
     sm.dqx[1][p] = a.g.dxu[i] * q;
+    if constexpr (kF32) {
+      sm.fv.dqx[0][p] = to_F<float>(sm.dqx[0][p]);
+      sm.fv.dqx[1][p] = to_F<float>(sm.dqx[1][p]);
+    }
   }
   for (int p = tid; p < TY; p += NT) {
     const int j = min(j0 + p, L.Y - 1);
     const double q = 1.0 / (4.0 * a.g.dyt[j] * a.g.cost[j]);
     sm.dqy[0][p] = a.g.cosu[j - 1] * a.g.dyu[j - 1] * q;  // facty (isoneutral.py:202)
     sm.dqy[1][p] = a.g.cosu[j] * a.g.dyu[j] * q;
+    if constexpr (kF32) {
+      sm.fv.dqy[0][p] = to_F<float>(sm.dqy[0][p]);
+      sm.fv.dqy[1][p] = to_F<float>(sm.dqy[1][p]);
+    }
   }
   for (int k = tid; k < Z; k += NT) {
     zdzw[k] = a.g.dzw[k];
@@ -369,6 +395,11 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     } else {
       zeos[k] = (2.0 * Eos::betaTs24 * Eos::theta0 - Eos::betaT) * Eos::rho0;
     }
+    if constexpr (kF32) {
+      zf[k] = to_F<float>(zdzw[k]);
+      zf[Z + k] = to_F<float>(zq_dzt[k]);
+      zf[2 * Z + k] = to_F<float>(zeos[k]);
+    }
   }
 
   // K_33 on the top level is zero on the whole plane (isoneutral.py:225)
@@ -379,10 +410,24 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     }
   }
   __syncthreads();
-  for (int p = tid; p < NP; p += NT) sm.inv_dxu_cost[p] = sm.inv_dxu[p % PX] * sm.inv_cost[p / PX];
+  for (int p = tid; p < NP; p += NT) {
+    sm.inv_dxu_cost[p] = sm.inv_dxu[p % PX] * sm.inv_cost[p / PX];
+    if constexpr (kF32) sm.fv.inv_dxu_cost[p] = to_F<float>(sm.inv_dxu_cost[p]);
+  }
   const double eos_c1 = a.eos_type == 3 ? -Eos::betaTs3 * Eos::rho0
                         : a.eos_type == 1 ? 0.0
                                           : -2.0 * Eos::betaTs24 * Eos::rho0;
+  const F eos_c1F = to_F<F>(eos_c1);
+  // the F-typed per-level and per-point grid factors
+  auto zeosF = [&](int k) -> F {
+    if constexpr (kF32) return zf[2 * Z + k]; else return zeos[k];
+  };
+  auto zdzwF = [&](int k) -> F {
+    if constexpr (kF32) return zf[k]; else return zdzw[k];
+  };
+  auto zqF_ = [&](int k) -> F {
+    if constexpr (kF32) return zf[Z + k]; else return zq_dzt[k];
+  };
 
   // ---- wet-point ordering of the segment -----------------------------------
   // An FP64 warp instruction holds the FP64 pipe for its whole warp, however
@@ -511,7 +556,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         }
         const double Tc = trc(0, 0, 0, 0), Sc = trc(1, 0, 0, 0);
         if (mk & VG_MASK_T) {
-          rT = to_F<F>(Tc) * to_F<F>(eos_c1) + to_F<F>(zeos[lev]);  // (isoneutral.py:40, get_rho.py:93-112)
+          rT = to_F<F>(Tc) * eos_c1F + zeosF(lev);  // (isoneutral.py:40, get_rho.py:93-112)
           rS = a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0);
         }
         // horizontal differences; their metric factors are applied in F below
@@ -539,7 +584,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         q[Q_RS][p] = rS;
         // face gradients (isoneutral.py:64-95): the FP64 difference times
         // 1/(dxu cost) or 1/dyu, the product in F (FP32 in the split form)
-        const F fx = to_F<F>(sm.inv_dxu_cost[p]), fy = to_F<F>(sm.inv_dyu[pj]);
+        F fx, fy;
+        if constexpr (kF32) {
+          fx = sm.fv.inv_dxu_cost[p];
+          fy = sm.fv.inv_dyu[pj];
+        } else {
+          fx = sm.inv_dxu_cost[p];
+          fy = sm.inv_dyu[pj];
+        }
         q[Q_TX][p] = to_F<F>(dTx) * fx;
         q[Q_SX][p] = to_F<F>(dSx) * fx;
         q[Q_TY][p] = to_F<F>(dTy) * fy;
@@ -673,6 +725,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
 
   const int i = i0 + tx, j = j0 + ty;
   const bool lin_steep = a.ksteep <= 0.0;
+  const F ksteepF = to_F<F>(a.ksteep);
   const bool east = i < L.X - 2 && j >= 2 && j < L.Y - 2;
   const bool north = i >= 2 && i < L.X - 2 && j < L.Y - 2;
   const bool top = i >= 2 && i < L.X - 2 && j >= 2 && j < L.Y - 2;
@@ -691,8 +744,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     const F(*pbn)[NP] = sm.pub[(k + 1) & 1];  // level k+1 (written only when k + 1 < Z; read only then)
     const long long o = L.at(i, j, k);
     // the face terms' grid factors in the derived-field type
-    const F dzwF[2] = {to_F<F>(zdzw[k > 0 ? k - 1 : 0]), to_F<F>(zdzw[k])}, qzF = to_F<F>(zq_dzt[k]);
-    const F ksteepF = to_F<F>(a.ksteep);
+    const F dzwF[2] = {zdzwF(k > 0 ? k - 1 : 0), zdzwF(k)}, qzF = zqF_(k);
     unsigned mk = 0;
     if ((east || north || top) && k - lo >= ok) mk = __ldg(a.m + o);  // before its key: no mask bit
 
@@ -784,8 +836,12 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
           a.Aby[o + jp * a.sp + a.sr] = a1;
           sy[jp] = a0 * F(s0.s) + a1 * F(s1.s);
         }
-        const F w = to_F<F>(sm.dqx[0][tx]) * sx[0] + to_F<F>(sm.dqx[1][tx]) * sx[1] +
-                    to_F<F>(sm.dqy[0][ty]) * sy[0] + to_F<F>(sm.dqy[1][ty]) * sy[1];
+        F w;
+        if constexpr (kF32)
+          w = sm.fv.dqx[0][tx] * sx[0] + sm.fv.dqx[1][tx] * sx[1] + sm.fv.dqy[0][ty] * sy[0] +
+              sm.fv.dqy[1][ty] * sy[1];
+        else
+          w = sm.dqx[0][tx] * sx[0] + sm.dqx[1][tx] * sx[1] + sm.dqy[0][ty] * sy[0] + sm.dqy[1][ty] * sy[1];
         k33 = __ldg(a.K + o) * w;
       } else {
 #pragma unroll
