@@ -213,8 +213,11 @@ __device__ __forceinline__ F top_flux(const Layout &L, const double *tr, long lo
 }
 
 // Dynamic shared memory of flux_div_body: 1/(4 dzt) and 1/dzt per level, then
-// a (Z + 1)-entry int table for the wet-point ordering.
-inline size_t flux_smem_bytes(int Z) { return 2 * (size_t)Z * sizeof(double) + ((size_t)Z + 1) * sizeof(int); }
+// a (Z + 1)-entry int table for the wet-point ordering, then the two level
+// tables in FP32 (used by the split form).
+inline size_t flux_smem_bytes(int Z) {
+  return 2 * (size_t)Z * sizeof(double) + ((size_t)Z + 1) * sizeof(int) + 2 * (size_t)Z * sizeof(float);
+}
 
 // True if any of n values loaded at p + off[m] is non-zero (either sign of
 // zero counts as zero), by integer operations on the bit patterns.
@@ -269,10 +272,24 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
   const int i0 = 2 + bx * TX, j0 = 2 + by * TY;
   const int nkeys = ke - kb + 1;
+  // the split form's FP32 copies of both tables (after the int table)
+  float *zf = reinterpret_cast<float *>(hist + Z + 1);
+  constexpr bool kF32 = sizeof(F) == sizeof(float);
   for (int k = tid; k < Z; k += NT) {
     zq_dzt[k] = 1.0 / (4.0 * a.g.dzt[k]);
     zinv_dzt[k] = 1.0 / a.g.dzt[k];
+    if constexpr (kF32) {
+      zf[k] = to_F<float>(zq_dzt[k]);
+      zf[Z + k] = to_F<float>(zinv_dzt[k]);
+    }
   }
+  // 1/(4 dzt[k]) (t = 0) or 1/dzt[k] (t = 1) in F
+  auto ztab = [&](int t, int k) -> F {
+    if constexpr (kF32)
+      return zf[t * Z + k];
+    else
+      return (t ? zinv_dzt : zq_dzt)[k];
+  };
   constexpr bool kOrder = sizeof(F) == sizeof(double);
   if (kOrder) {
     for (int n = tid; n < nkeys; n += NT) hist[n] = 0;
@@ -423,7 +440,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
     // reads before level k+2's writes to the same buffer
     const int b = k & 1;
     const long long o = L.at(i, j, k);
-    const F qz = to_F<F>(zq_dzt[k]);
+    const F qz = ztab(0, k);
     F fe[NTR], fn[NTR], ft[NTR];
 #pragma unroll
     for (int r = 0; r < NTR; ++r) fe[r] = fn[r] = ft[r] = 0.0;
@@ -534,7 +551,7 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
       for (int r = 0; r < NTR; ++r) {
         const DiffArgs<F> &t = A[r];
         F e = pfma(fe[r] - fe_s[b][r][ty][tx], inv_fx, pm(fn[r] - fn_s[b][r][ty][tx], inv_fy));
-        e = pfma(ft[r] - ft_prev[r], to_F<F>(zinv_dzt[k]), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
+        e = pfma(ft[r] - ft_prev[r], ztab(1, k), e);  // k = 0: ft_prev = 0 (diffusion.py:132-137)
         if (a.fuse_prepare) {
           // tr[taup1] = tr[tau] * 1 and dtracer_iso = 0 (thermodynamics.py:226-241, :427-429), then
           // the explicit update: the values the separate preparation and the update below give

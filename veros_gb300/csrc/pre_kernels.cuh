@@ -418,6 +418,7 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
                         : a.eos_type == 1 ? 0.0
                                           : -2.0 * Eos::betaTs24 * Eos::rho0;
   const F eos_c1F = to_F<F>(eos_c1);
+  const double rS_wet_d = to_D(a.eos_type == 4 ? F(0.0) : F(Eos::betaS * Eos::rho0));  // drho/dS of a wet point
   // the F-typed per-level and per-point grid factors
   auto zeosF = [&](int k) -> F {
     if constexpr (kF32) return zf[2 * Z + k]; else return zeos[k];
@@ -575,8 +576,9 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
         if (lev >= Z - 1) mk &= ~(unsigned)VG_MASK_W;  // no face above the top level
       }
       if (store) {
-        // vertical density gradients in FP64 (exact products of the split form's FP32 values)
-        const double rTd = to_D(rT), rSd = to_D(rS);
+        // vertical density gradients in FP64 (exact products of the split form's FP32 values);
+        // rS is 0 or the one constant of the equation of state
+        const double rTd = to_D(rT), rSd = (mk & VG_MASK_T) ? rS_wet_d : 0.0;
         const double G0 = rTd * carryT[s] + rSd * carryS[s];  // face below (kr = 0)
         const double G1 = rTd * dTz + rSd * dSz;                   // face above (kr = 1)
         F(*q)[NP] = sm.q[buf];
