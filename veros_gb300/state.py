@@ -95,6 +95,21 @@ def is_canonical(t, X, Y, Z):
     return P >= X and (Z == 1 or t.stride(2) == P * Y)
 
 
+
+def to_host(t):
+    """A NumPy array holding the device tensor ``t``, in page-locked memory.
+
+    The copy runs at the host link's DMA rate instead of through the driver's
+    staging of pageable memory. The array is a view of a pinned tensor from
+    torch's caching host allocator: while the array lives it keeps the block,
+    and once it is freed the block serves the next download of that size.
+    """
+    if t.device.type != "cuda":
+        return t.numpy()
+    out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    out.copy_(t)
+    return out.numpy()
+
 class Settings:
     """Attribute namespace of model settings."""
 
@@ -263,7 +278,7 @@ class DeviceState:
         if isinstance(t, torch.Tensor):
             DeviceState.transfer_bytes["d2h"] += t.numel() * t.element_size()
             # the reference layout (C order of the logical shape) formed on the device, then one copy
-            return t.detach().contiguous().cpu().numpy()
+            return to_host(t.detach().contiguous())
         return t
 
     # ---- derived device views --------------------------------------------

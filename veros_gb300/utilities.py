@@ -26,6 +26,7 @@ import numpy as np
 import torch
 
 from . import _capi
+from .state import to_host
 
 
 def create_water_masks(ks, nz):
@@ -107,7 +108,7 @@ def solve_implicit(a, b, c, d, water_mask, edge_mask, b_edge=None, d_edge=None, 
     if out.dtype != out_dtype:
         out = out.to(out_dtype)
     if host:
-        return out.cpu().numpy()
+        return to_host(out.contiguous())
     return out
 
 
