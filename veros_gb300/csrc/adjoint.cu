@@ -25,13 +25,14 @@
 //                            threads sharing the Thomas factorisation, columns
 //                            deepest first) and dL/dK_33 from
 //                            dL/ddelta_k = (x_{k+1} - x_k)(y_k/dzt_k - y_{k+1}/dzt_{k+1})
-//   4. adj_active_kernel     zero partial sums of the points whose faces carry no
-//                            term; the others listed
+//   4. adj_active_kernel     per point whether its faces carry a term (an
+//                            activity map); the points that do, listed
 //      adj_slope_kernel      per listed point: the eight slope adjoints (from the
 //                            stored tapers and slopes), written as per-point
 //                            partial sums onto the point's faces
 //   5. adj_gather_kernel     per point: sums the partials of the faces around
-//                            it into dL/dT_n, dL/dS_n and dL/dK_iso
+//                            it (those of active points; the others are zero)
+//                            into dL/dT_n, dL/dS_n and dL/dK_iso
 //
 // Every partial is written exactly once by the point that owns it and read
 // by its neighbours in the next launch: no atomics, results are deterministic.
@@ -77,9 +78,10 @@ inline size_t field_doubles(const Layout &L) { return (size_t)L.plane * L.Z; }
 // doubles before the active-point list (fields, then the grid tables)
 inline size_t list_offset(const Layout &L) { return (size_t)kFields * field_doubles(L) + table_doubles(L); }
 
-// fields, tables, then the active-point list (one int32 per point) and its count
+// fields, tables, then the active-point list (one int32 per point) and its
+// count, then one activity byte per point
 inline size_t scratch_bytes(const Layout &L) {
-  size_t n = list_offset(L) * sizeof(double) + (field_doubles(L) + 1) * sizeof(int32_t);
+  size_t n = list_offset(L) * sizeof(double) + (field_doubles(L) + 1) * sizeof(int32_t) + field_doubles(L);
   return (n + 255) & ~(size_t)255;
 }
 
@@ -491,23 +493,21 @@ __device__ __forceinline__ void adj_slope_point(const SlopeArgs &a, const SlopeF
 }
 
 // Active-point list: a point whose faces carry no term has all its partial
-// sums zero, which this pass writes; the others are appended to the list
-// (one atomic per warp, the lanes of a warp in x order), so that the slope
-// pass runs whole warps of points with terms: an FP64 warp instruction costs
-// the same however few of its lanes are active, and most points of a warp
-// row are dry on most levels. Block (32, 4): a warp is one x row.
-__global__ void __launch_bounds__(128) adj_active_kernel(Layout L, const uint8_t *__restrict__ m, double *part,
-                                                         long long F, int32_t *list, int *count) {
+// sums zero; it is marked so in the activity map (which the gather reads
+// instead of its partials) and the others are appended to the list (one
+// atomic per warp, the lanes of a warp in x order), so that the slope pass
+// runs whole warps of points with terms: an FP64 warp instruction costs the
+// same however few of its lanes are active, and most points of a warp row are
+// dry on most levels. Block (32, 4): a warp is one x row.
+__global__ void __launch_bounds__(128) adj_active_kernel(Layout L, const uint8_t *__restrict__ m, uint8_t *active,
+                                                         int32_t *list, int *count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z;
   const bool in = i < L.X && j < L.Y;
   const bool act = in && slope_faces(L, m, i, j, k).any();
   const long long o = in ? L.at(i, j, k) : 0;
-  if (in && !act) {
-#pragma unroll
-    for (int n = 0; n < P_N; ++n) part[n * F + o] = 0.0;
-  }
+  if (in) active[o] = act ? 1 : 0;
   const unsigned ball = __ballot_sync(0xffffffffu, act);
   if (!ball) return;
   const int lane = threadIdx.x & 31, leader = __ffs(ball) - 1;
@@ -547,6 +547,7 @@ struct GatherArgs {
   const double *__restrict__ part;
   long long field;
   double *gT, *gS, *gK;
+  const uint8_t *__restrict__ active;  // points whose partials the slope pass wrote (the others are zero)
 };
 
 __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(GatherArgs a) {
   const int X = L.X, Y = L.Y, Z = L.Z;
   const long long o = L.at(i, j, k), PW = L.pitch, PL = L.plane, F = a.field;
   const uint8_t *m = a.m;
-  auto part = [&](int comp, long long at) { return __ldg(a.part + comp * F + at); };
+  auto part = [&](int comp, long long at) { return __ldg(a.active + at) ? __ldg(a.part + comp * F + at) : 0.0; };
 
   const bool wet = __ldg(m + o) & VG_MASK_T;
   double lamT = wet ? __ldg(a.gTp + o) + drdT_dT(a.eos) * part(P_LRT, o) : 0.0;
@@ -697,9 +698,10 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   {
     int32_t *list = reinterpret_cast<int32_t *>(base + adj::list_offset(L));
     int *count = list + F;
+    uint8_t *active = reinterpret_cast<uint8_t *>(count + 1);
     cudaError_t e = cudaMemsetAsync(count, 0, sizeof(int), s);
     if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "adjoint list count: %s", cudaGetErrorString(e));
-    adj::adj_active_kernel<<<grd, block, 0, s>>>(L, f->mask_bits, part, F, list, count);
+    adj::adj_active_kernel<<<grd, block, 0, s>>>(L, f->mask_bits, active, list, count);
     if ((st = check_launch("adj_active_kernel"))) return st;
     adj::SlopeArgs a{L,      g,    gi,       set->eq_of_state_type, set->iso_slopec, 1.0 / set->iso_dslope,
                      set->K_iso_steep, f->temp, f->salt, f->K_iso, gK33, f->mask_bits, slopes, nu, ten.K_11,
@@ -716,8 +718,10 @@ extern "C" int vg_isoneutral_step_adjoint_f64(const VgDomain *dom, const VgGrid 
   }
   // 5. gather
   {
+    const uint8_t *active = reinterpret_cast<const uint8_t *>(
+        reinterpret_cast<const int32_t *>(base + adj::list_offset(L)) + F + 1);
     adj::GatherArgs a{L, g, gi, set->eq_of_state_type, gTp, gSp, f->mask_bits, part, F, f->gtemp, f->gsalt,
-                      f->gK_iso};
+                      f->gK_iso, active};
     adj::adj_gather_kernel<<<grd, block, 0, s>>>(a);
     if ((st = check_launch("adj_gather_kernel"))) return st;
   }
