@@ -93,6 +93,35 @@ def test_thermodynamics_sequence_through_installed_dropins(monkeypatch):
         assert isinstance(arr, np.ndarray) and arr.dtype == np.float64 and arr.shape == g[f"out_{name}"].shape
 
 
+def test_thermodynamics_sequence_on_float32_state(monkeypatch):
+    """A float32 run (runtime_settings.float_type = "float32", veros/runtime.py:93):
+    the installed functions compute in FP64 from the state's float32 arrays and
+    vs.update stores their results as float32, so every output is float32 and
+    stays within float32 rounding (1e-6 relative) of the same sequence on a
+    float64 state holding the same (float32-rounded) inputs."""
+    g = load_golden("thermo_cyclic")
+    g32 = {k: (v.astype(np.float32).astype(np.float64) if k.startswith("in_") and v.dtype == np.float64 else v)
+           for k, v in g.items()}
+    mods, handle = plugin_call_sites(monkeypatch)
+    try:
+        s32 = state_from_golden(g32, float_type=np.float32)
+        s64 = state_from_golden(g32)
+        iso, thermo = mods["veros.core.isoneutral"], mods["veros.core.thermodynamics"]
+        _thermo_sequence(iso, thermo, s32)
+        from veros_gb300.state import release_host_mirrors
+
+        release_host_mirrors()
+        _thermo_sequence(iso, thermo, s64)
+    finally:
+        handle.uninstall()
+    for name in OUT_FIELDS:
+        got, ref = getattr(s32.variables, name), getattr(s64.variables, name)
+        assert isinstance(got, np.ndarray) and got.dtype == np.float32 and got.shape == ref.shape, name
+        scale = float(np.max(np.abs(ref)))
+        err = float(np.max(np.abs(got.astype(np.float64) - ref))) / scale if scale else 0.0
+        assert err <= 1e-6, (name, err)  # measured <= 8e-8: a few float32 ulps
+
+
 def test_thermodynamics_sequence_on_device_state():
     """The same sequence with the fields resident on the GPU (DeviceState)."""
     from veros_gb300 import isoneutral, thermodynamics
