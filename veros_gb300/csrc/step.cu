@@ -57,21 +57,29 @@ namespace {
 // The step's preparation of the cells the fused diffusion does not cover:
 // the two-cell rim of every level (i < 2, i >= X-2, j < 2, j >= Y-2).
 template <typename F>
+// One thread per rim cell of a level: the two full rows at each end of y,
+// then the two columns at each end of x on the rows between.
 __global__ void prepare_rim_kernel(Layout L, const uint8_t *__restrict__ m, const double *__restrict__ T0,
                                    double *T1, const double *__restrict__ S0, double *S1, F *dT, F *dS, F *P) {
-  const int j = blockIdx.x, k = blockIdx.y;
-  const bool full = j < 2 || j >= L.Y - 2;
-  const int n = full ? L.X : 4;
-  for (int t = threadIdx.x; t < n; t += blockDim.x) {
-    const int i = full ? t : (t < 2 ? t : L.X - 4 + t);
-    const long long o = L.at(i, j, k);
-    const double mT = (__ldg(m + o) & VG_MASK_T) ? 1.0 : 0.0;
-    T1[o] = T0[o] * mT;
-    S1[o] = S0[o] * mT;
-    dT[o] = F(0.0);
-    dS[o] = F(0.0);
-    if (P) P[o] = F(0.0);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  if (r >= 4 * L.X + 4 * (L.Y - 4)) return;
+  int i, j;
+  if (r < 4 * L.X) {
+    const int jr = r / L.X;
+    i = r % L.X;
+    j = jr < 2 ? jr : L.Y - 4 + jr;
+  } else {
+    const int q = r - 4 * L.X, c = q % 4;
+    i = c < 2 ? c : L.X - 4 + c;
+    j = 2 + q / 4;
   }
+  const long long o = L.at(i, j, k);
+  const double mT = (__ldg(m + o) & VG_MASK_T) ? 1.0 : 0.0;
+  T1[o] = T0[o] * mT;
+  S1[o] = S0[o] * mT;
+  dT[o] = F(0.0);
+  dS[o] = F(0.0);
+  if (P) P[o] = F(0.0);
 }
 
 // Stage 0: the rim's preparation; 1: pre; 2: diffusion of temp and salt with
@@ -91,7 +99,8 @@ int step_stage(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
         !f->dsalt_iso)
       return fail(VG_ERR_ARG, "%s: NULL pointer argument", name);
     const Layout L = layout_of(dom);
-    prepare_rim_kernel<F><<<dim3(L.Y, L.Z), 128, 0, as_stream(stream)>>>(
+    const int nrim = 4 * L.X + 4 * (L.Y - 4);
+    prepare_rim_kernel<F><<<dim3((nrim + 127) / 128, L.Z), 128, 0, as_stream(stream)>>>(
         L, f->mask_bits, f->temp_tau, f->temp_taup1, f->salt_tau, f->salt_taup1, f->dtemp_iso, f->dsalt_iso,
         f->P_diss_iso);
     return check_launch("prepare_rim_kernel");
