@@ -223,6 +223,14 @@ typedef struct VgStepFields {
    * first keeps the lanes of a warp on columns of similar length. A
    * permutation of all (X-4)*(Y-4) interior columns. */
   const int32_t *column_order;
+  /* optional (NULL: equal counts of tile-levels per CTA): the work shares of
+   * the pre and flux kernels' CTAs, written by vg_isoneutral_step_shares for
+   * these masks on this device, n + 1 tile-level starts each, with the n of
+   * vg_isoneutral_step_shares_size; a kernel whose CTA count is not its n
+   * takes equal counts instead. Only the distribution of the work depends on
+   * them, not the results. */
+  const long long *pre_shares, *flux_shares;
+  int pre_shares_n, flux_shares_n;
 } VgStepFields;
 
 /* One isoneutral step as the reference's caller runs it
@@ -233,6 +241,22 @@ typedef struct VgStepFields {
  * Scratch as for vg_isoneutral_diffusion_pair_f64. */
 int vg_isoneutral_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                            const VgStepFields *f, void *scratch, size_t scratch_bytes, void *stream);
+
+/* Work shares of a step's persistent pre and flux kernels (no reference
+ * counterpart). precision 0: vg_isoneutral_step_f64, 1: the split form.
+ * With equal counts of tile-levels per CTA, CTAs holding dry tile-levels
+ * finish early; the shares give each CTA an equal part of a + (busy warps)
+ * summed over its tile-levels, the busy warps of a level being the wet points
+ * of the tile / 32, rounded up. vg_isoneutral_step_shares_size gives the
+ * number of CTAs of each kernel (0 for a kernel that takes no shares: one
+ * CTA per tile on large domains, and the split form's flux kernel) and the
+ * scratch bytes; vg_isoneutral_step_shares writes n + 1 tile-level starts
+ * per kernel into device arrays, on the stream, from the packed masks.
+ * Recompute them when the masks change; stale shares only cost time. */
+int vg_isoneutral_step_shares_size(const VgDomain *dom, int precision, int *n_pre, int *n_flux,
+                                   size_t *scratch_bytes);
+int vg_isoneutral_step_shares(const VgDomain *dom, int precision, const uint8_t *mask_bits, long long *pre_starts,
+                              long long *flux_starts, void *scratch, size_t scratch_bytes, void *stream);
 
 /* FP32 fields of one rollout step of the split form. */
 typedef struct VgStepFieldsF32 {
@@ -247,7 +271,9 @@ typedef struct VgStepFieldsF32 {
   float *dtemp_iso, *dsalt_iso;
   const float *int_drhodT_tau, *int_drhodS_tau;
   float *P_diss_iso;
-  const int32_t *column_order; /* as in VgStepFields */
+  const int32_t *column_order;               /* as in VgStepFields */
+  const long long *pre_shares, *flux_shares; /* as in VgStepFields */
+  int pre_shares_n, flux_shares_n;
 } VgStepFieldsF32;
 
 /* One isoneutral step of the FP32/FP64-split form (see vg_isoneutral_step_f64). */

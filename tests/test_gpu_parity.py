@@ -405,6 +405,32 @@ def test_fused_preparation_matches_separate_pass(precision, energy):
         np.testing.assert_array_equal(a.dev.download(n), b.dev.download(n), err_msg=n)
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32split"])
+def test_weighted_shares_change_no_result(precision):
+    """The pre and flux kernels' CTAs take shares of the tile-levels weighted
+    by their water (vg_isoneutral_step_shares): the starts cover the
+    tile-levels in order, and two steps give the fields of equal shares, bit
+    for bit."""
+    from veros_gb300 import synthetic
+    from veros_gb300.state import DeviceState
+    from veros_gb300.step import IsoneutralStepper
+
+    host = synthetic.global_1deg_state(seed=2, nz=20)
+    a = IsoneutralStepper(DeviceState.from_host(host, precision=precision))
+    b = IsoneutralStepper(DeviceState.from_host(host, precision=precision))
+    pre, flux = a.dev.step_shares()
+    assert pre is not None and (flux is not None) == (precision == "f64")  # the split flux kernel: equal counts
+    for starts in (pre,) + ((flux,) if flux is not None else ()):
+        s = starts.cpu().numpy()
+        assert s[0] == 0 and np.all(np.diff(s) >= 0) and s[-1] % host.nz == 0
+    b.dev.step_shares = lambda stream=None: (None, None)
+    a.step(2)
+    b.step(2)
+    torch.cuda.synchronize()
+    for n in ("temp", "salt", "dtemp_iso", "dsalt_iso", "K_11", "K_33", "Ai_ez", "Ai_by"):
+        np.testing.assert_array_equal(a.dev.download(n), b.dev.download(n), err_msg=n)
+
+
 def test_drop_in_signatures_on_device_state():
     import veros_gb300 as vg
     from veros_gb300 import synthetic

@@ -62,14 +62,16 @@ class VgStepFields(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
                                                 "mask_bits", "kbot")] + [("ten", VgTensorFields)] + [
         (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso",
-                                       "column_order")]
+                                       "column_order", "pre_shares", "flux_shares")] + [
+        ("pre_shares_n", ctypes.c_int), ("flux_shares_n", ctypes.c_int)]
 
 
 class VgStepFieldsF32(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in ("temp_tau", "temp_taup1", "salt_tau", "salt_taup1", "K_iso",
                                                 "mask_bits", "kbot")] + [("ten", VgTensorFieldsF32)] + [
         (n, ctypes.c_void_p) for n in ("dtemp_iso", "dsalt_iso", "int_drhodT_tau", "int_drhodS_tau", "P_diss_iso",
-                                       "column_order")]
+                                       "column_order", "pre_shares", "flux_shares")] + [
+        ("pre_shares_n", ctypes.c_int), ("flux_shares_n", ctypes.c_int)]
 
 
 class VgEnsembleTuning(ctypes.Structure):
@@ -169,6 +171,12 @@ SIGNATURES = {
                                               ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "vg_isoneutral_step_prepare_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgStepFields),
                                                       ctypes.c_void_p]),
+    "vg_isoneutral_step_shares_size": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_int,
+                                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                      ctypes.POINTER(ctypes.c_size_t)]),
+    "vg_isoneutral_step_shares": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.c_int, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                                 ctypes.c_void_p]),
     "vg_isoneutral_step_stage_f64": (ctypes.c_int, [ctypes.POINTER(VgDomain), ctypes.POINTER(VgGrid),
                                                     ctypes.POINTER(VgIsoSettings), ctypes.POINTER(VgStepFields),
                                                     ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,

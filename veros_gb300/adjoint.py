@@ -96,10 +96,14 @@ class IsoneutralAdjoint:
             self._check(n, t)
         dev = self.dev
         T_new, S_new = self.empty(), self.empty()
+        pre_sh, flux_sh = dev.step_shares()
+        ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         f = _capi.VgStepFields(T.data_ptr(), T_new.data_ptr(), S.data_ptr(), S_new.data_ptr(), K.data_ptr(),
                                dev.mask_bits().data_ptr(), dev.variables.kbot.data_ptr(), self._ten,
                                self._diag[0].data_ptr(), self._diag[1].data_ptr(), None, None, None,
-                               dev.column_order().data_ptr())
+                               dev.column_order().data_ptr(), ptr(pre_sh), ptr(flux_sh),
+                               0 if pre_sh is None else pre_sh.numel() - 1,
+                               0 if flux_sh is None else flux_sh.numel() - 1)
         _capi.check(self.lib.vg_isoneutral_step_f64(self._dom, self._grid, self._set, f, self._pair.data_ptr(),
                                                     self._pair.numel() * 8, self._stream()), "isoneutral step")
         return T_new, S_new

@@ -30,16 +30,19 @@ int validate_domain(const VgDomain *dom);
 // CTA). With at least four tiles per resident CTA slot, one CTA per tile: the
 // hardware then runs neighbouring tiles side by side (their halo reads meet
 // in L2) and its tail is short against the many waves. Otherwise every CTA
-// the device holds at once, each with an equal share (at least min_levels
+// the device holds at once, each with a share (at least min_levels
 // tile-levels), so that no SM idles through a partial last wave. 0 on error.
+// *per_tile (optional) tells which of the two.
 template <typename K>
-inline int span_ctas(K kernel, int threads, size_t smem, int ntiles, int Z, int min_levels) {
+inline int span_ctas(K kernel, int threads, size_t smem, int ntiles, int Z, int min_levels,
+                     bool *per_tile = nullptr) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess || per < 1)
     return 0;
   const long long slots = (long long)sms * per;
+  if (per_tile) *per_tile = ntiles >= 4 * slots;
   if (ntiles >= 4 * slots) return ntiles;
   const long long by_units = ((long long)ntiles * Z + min_levels - 1) / min_levels;
   return (int)std::max(1LL, std::min(slots, by_units));
@@ -241,15 +244,33 @@ struct Eos {
 // kernel also does a step's preparation of the interior cells (the step's
 // rim is prepared separately), instead of updating what a separate
 // preparation wrote.
+// flux_starts: optional work shares of the flux kernel's CTAs (span_shares.cu).
 int diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                const VgTensorFields *ten, const double *K_iso, const uint8_t *mask_bits,
                                const int32_t *kbot, const VgTracerArgs *temp, const VgTracerArgs *salt,
                                const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream,
-                               int fuse_prepare = 0);
+                               int fuse_prepare = 0, const long long *flux_starts = nullptr, int flux_nstarts = 0);
 int diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                     const VgTensorFieldsF32 *ten, const float *K_iso, const uint8_t *mask_bits,
                                     const int32_t *kbot, const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
                                     const int32_t *column_order, void *scratch, size_t scratch_bytes,
-                                    void *stream, int fuse_prepare = 0);
+                                    void *stream, int fuse_prepare = 0, const long long *flux_starts = nullptr,
+                                    int flux_nstarts = 0);
+
+// The pre and temp+salt flux kernels' tilings on this device: tiles along x,
+// tiles in all, and the CTAs that share the tile-levels (0 where the kernel
+// runs one CTA per tile); F = double or float (the split form).
+template <typename F>
+int pre_span_plan(const VgDomain *dom, int *ntx, int *ntiles, int *nctas);
+template <typename F>
+int flux_span_plan(const VgDomain *dom, int *ntx, int *ntiles, int *nctas);
+
+// The pre kernel of a step, with optional work shares of its CTAs.
+int pre_for_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                     const double *salt_tau, const double *K_iso, const uint8_t *mask_bits,
+                     const VgTensorFields *out, const long long *starts, int nstarts, void *stream);
+int pre_for_step_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                          const double *salt_tau, const float *K_iso, const uint8_t *mask_bits,
+                          const VgTensorFieldsF32 *out, const long long *starts, int nstarts, void *stream);
 
 }  // namespace vg

@@ -594,18 +594,21 @@ __device__ __forceinline__ void flux_div_body(const DiffArgs<F> *A, double *zq_d
   __syncthreads();
 }
 
-// One domain: every resident CTA takes an equal share of the ntiles * Z
+// One domain: every resident CTA takes a share of the ntiles * Z
 // tile-levels, tile-major, as one segment per tile it touches (a segment
-// starting above level 0 pays the restart of a k-chunk); the body ends with a
-// barrier before its buffers are reused.
+// starting above level 0 pays the restart of a k-chunk): starts[c] ..
+// starts[c+1] (weighted by the water on each tile-level, span_shares.cu) or,
+// without starts, equal counts; the body ends with a barrier before its
+// buffers are reused.
 template <typename F, int TY, int NTR>
-__global__ void __launch_bounds__(TX * TY, 16 / TY) flux_span_kernel(DiffArgs<F> a, DiffArgs<F> b, int ntx, int ntiles) {
+__global__ void __launch_bounds__(TX * TY, 16 / TY) flux_span_kernel(DiffArgs<F> a, DiffArgs<F> b, int ntx, int ntiles,
+                                                                      const long long *__restrict__ starts) {
   extern __shared__ double zq_dzt[];
   const DiffArgs<F> A[2] = {a, b};
   const int Z = a.L.Z;
   const long long W = (long long)ntiles * Z;
-  long long p = W * blockIdx.x / gridDim.x;
-  const long long end = W * (blockIdx.x + 1) / gridDim.x;
+  long long p = starts ? starts[blockIdx.x] : W * blockIdx.x / gridDim.x;
+  const long long end = starts ? starts[blockIdx.x + 1] : W * (blockIdx.x + 1) / gridDim.x;
   while (p < end) {
     const int t = (int)(p / Z), kb = (int)(p % Z);
     const int ke = (int)min((long long)Z, end - (long long)t * Z);

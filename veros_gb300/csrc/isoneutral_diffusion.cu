@@ -15,19 +15,39 @@ namespace {
 // NTR = 2: temp and salt in one pass over the tensor (b: salt); NTR = 1: a alone
 // Tiles of 32 x 8 columns in the FP64 form, 32 x 4 in the split form
 // (flux_span_kernel): one CTA per tile on large domains, else every resident
-// CTA with an equal share of the tile-levels. The split form's flux kernel is
+// CTA with a share of the tile-levels. The split form's flux kernel is
 // latency-bound at 128 registers a thread; on 4-warp tiles its level barriers
 // wait for fewer warps (1 degree: 0.530 against 0.541 ms for the diffusion
 // stage; more CTAs per SM by a tighter register budget spill and gain nothing).
+template <typename F>
+constexpr int flux_rows() {
+  return sizeof(F) == sizeof(float) ? 4 : 8;
+}
+
 template <typename F, int NTR>
-int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s) {
-  constexpr int TY = sizeof(F) == sizeof(float) ? 4 : 8;
-  const int nbx = (a.L.X - 4 + TX - 1) / TX, nby = (a.L.Y - 4 + TY - 1) / TY;
-  const size_t smem = flux_smem_bytes(a.L.Z);
-  const int nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, nbx * nby, a.L.Z, 8);
+int flux_geometry(const Layout &L, int &nbx, int &nby, size_t &smem, int &nc, bool &per_tile) {
+  constexpr int TY = flux_rows<F>();
+  nbx = (L.X - 4 + TX - 1) / TX;
+  nby = (L.Y - 4 + TY - 1) / TY;
+  smem = flux_smem_bytes(L.Z);
+  nc = span_ctas(flux_span_kernel<F, TY, NTR>, TX * TY, smem, nbx * nby, L.Z, 8, &per_tile);
   if (nc < 1) return fail(VG_ERR_LAUNCH, "flux_span_kernel: occupancy query failed");
+  return VG_OK;
+}
+
+template <typename F, int NTR>
+int launch_flux_div(DiffArgs<F> &a, DiffArgs<F> &b, cudaStream_t s, const long long *starts = nullptr,
+                    int nstarts = 0) {
+  constexpr int TY = flux_rows<F>();
+  int nbx, nby, nc;
+  size_t smem;
+  bool per_tile;
+  int st = flux_geometry<F, NTR>(a.L, nbx, nby, smem, nc, per_tile);
+  if (st) return st;
   a.kchunk = b.kchunk = a.L.Z;
-  flux_span_kernel<F, TY, NTR><<<nc, TX * TY, smem, s>>>(a, b, nbx, nbx * nby);
+  // shares apply where the CTAs split the tile-levels (not one CTA per tile)
+  const long long *sh = !per_tile && nstarts == nc ? starts : nullptr;
+  flux_span_kernel<F, TY, NTR><<<nc, TX * TY, smem, s>>>(a, b, nbx, nbx * nby, sh);
   return check_launch("flux_span_kernel");
 }
 
@@ -130,7 +150,7 @@ template <typename F, typename Ten, typename Tr>
 int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const Ten *ten,
                    const F *K_iso, const uint8_t *mask_bits, const int32_t *kbot, const Tr *temp, const Tr *salt,
                    void *scratch, size_t scratch_bytes, void *stream, const int32_t *col_order = nullptr,
-                   int fuse_prepare = 0) {
+                   int fuse_prepare = 0, const long long *flux_starts = nullptr, int flux_nstarts = 0) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -147,7 +167,7 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
   if (fuse_prepare && aT.P != aS.P)
     return fail(VG_ERR_ARG, "step diffusion: temp and salt must share P_diss_iso");
   cudaStream_t s = as_stream(stream);
-  if ((st = launch_flux_div<F, 2>(aT, aS, s))) return st;
+  if ((st = launch_flux_div<F, 2>(aT, aS, s, flux_starts, flux_nstarts))) return st;
   if ((st = launch_implicit<F, 2>(aT, aS, s))) return st;
   if (aT.save_fluxes && (st = launch_energy<F>(aT, &aS, s))) return st;
   return VG_OK;
@@ -159,19 +179,37 @@ int diffusion_pair_ordered_f64(const VgDomain *dom, const VgGrid *grid, const Vg
                                const VgTensorFields *ten, const double *K_iso, const uint8_t *mask_bits,
                                const int32_t *kbot, const VgTracerArgs *temp, const VgTracerArgs *salt,
                                const int32_t *column_order, void *scratch, size_t scratch_bytes, void *stream,
-                               int fuse_prepare) {
+                               int fuse_prepare, const long long *flux_starts, int flux_nstarts) {
   return diffusion_pair<double>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
-                                stream, column_order, fuse_prepare);
+                                stream, column_order, fuse_prepare, flux_starts, flux_nstarts);
 }
 
 int diffusion_pair_ordered_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                     const VgTensorFieldsF32 *ten, const float *K_iso, const uint8_t *mask_bits,
                                     const int32_t *kbot, const VgTracerArgsF32 *temp, const VgTracerArgsF32 *salt,
                                     const int32_t *column_order, void *scratch, size_t scratch_bytes,
-                                    void *stream, int fuse_prepare) {
+                                    void *stream, int fuse_prepare, const long long *flux_starts,
+                                    int flux_nstarts) {
   return diffusion_pair<float>(dom, grid, set, ten, K_iso, mask_bits, kbot, temp, salt, scratch, scratch_bytes,
-                               stream, column_order, fuse_prepare);
+                               stream, column_order, fuse_prepare, flux_starts, flux_nstarts);
 }
+
+// The temp+salt flux kernel's tiling on this device: tiles along x, tiles in
+// all, and CTAs (as many as tiles where it runs one CTA per tile).
+template <typename F>
+int flux_span_plan(const VgDomain *dom, int *ntx, int *ntiles, int *nctas) {
+  int nbx, nby, nc;
+  size_t smem;
+  bool per_tile;
+  const int st = flux_geometry<F, 2>(layout_of(dom), nbx, nby, smem, nc, per_tile);
+  if (st) return st;
+  *ntx = nbx;
+  *ntiles = nbx * nby;
+  *nctas = per_tile ? 0 : nc;
+  return VG_OK;
+}
+template int flux_span_plan<double>(const VgDomain *, int *, int *, int *);
+template int flux_span_plan<float>(const VgDomain *, int *, int *, int *);
 
 }  // namespace vg
 

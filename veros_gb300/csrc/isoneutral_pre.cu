@@ -8,10 +8,38 @@ namespace {
 
 using namespace detail;
 
+// tiles of 32 x 8 columns (FP64: two CTAs of 8 warps per SM) or 32 x 4
+// (split form: four CTAs of 4 warps, whose level barriers overlap); one CTA
+// per tile on large domains, else every resident CTA with a share of the
+// tile-levels. The FP64 form on 32 x 4 tiles measured 1.04 against 0.85 ms
+// at 1 degree: its halo rows then cost more FP64 work than the overlapping
+// barriers save.
+template <typename F>
+struct PreGeometry {
+  static constexpr int TY = sizeof(F) == sizeof(double) ? 8 : 4, TX = 32;
+  int nbx, nby, nc;
+  bool per_tile;  // one CTA per tile (no shares)
+  size_t smem;
+};
+
+template <typename F>
+int pre_geometry(const Layout &L, PreGeometry<F> &g) {
+  constexpr int TY = PreGeometry<F>::TY, TX = PreGeometry<F>::TX;
+  g.nbx = (L.X - 3 + TX - 1) / TX;
+  g.nby = (L.Y - 3 + TY - 1) / TY;
+  g.smem = pre_smem_bytes<F, TY>(L.Z);
+  cudaError_t e =
+      cudaFuncSetAttribute(pre_span_kernel<F, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+  if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_span_kernel smem %zu: %s", g.smem, cudaGetErrorString(e));
+  g.nc = span_ctas(pre_span_kernel<F, TY>, TX * TY, g.smem, g.nbx * g.nby, L.Z, 8, &g.per_tile);
+  if (g.nc < 1) return fail(VG_ERR_LAUNCH, "pre_span_kernel: occupancy query failed");
+  return VG_OK;
+}
+
 template <typename F, typename Out>
 int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
                const double *salt_tau, const F *K_iso, const uint8_t *mask_bits, const Out *out, void *stream,
-               const char *name, double *slopes = nullptr) {
+               const char *name, double *slopes = nullptr, const long long *starts = nullptr, int nstarts = 0) {
   clear_error();
   int st = validate_domain(dom);
   if (st) return st;
@@ -45,26 +73,46 @@ int launch_pre(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   a.slopes = slopes;
   a.slope_field = (long long)a.L.plane * a.L.Z;
   a.stage_ok = pre_stage_ok(a);
-  // tiles of 32 x 8 columns (FP64: two CTAs of 8 warps per SM) or 32 x 4
-  // (split form: four CTAs of 4 warps, whose level barriers overlap); one CTA
-  // per tile on large domains, else every resident CTA with an equal share
-  // of the tile-levels. The FP64 form on 32 x 4 tiles measured 1.04 against
-  // 0.85 ms at 1 degree: its halo rows then cost more FP64 work than the
-  // overlapping barriers save.
-  constexpr int TY = sizeof(F) == sizeof(double) ? 8 : 4, TX = 32;
-  const int nbx = (a.L.X - 3 + TX - 1) / TX, nby = (a.L.Y - 3 + TY - 1) / TY;
-  const size_t smem = pre_smem_bytes<F, TY>(a.L.Z);
-  cudaError_t e =
-      cudaFuncSetAttribute(pre_span_kernel<F, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return fail(VG_ERR_LAUNCH, "pre_span_kernel smem %zu: %s", smem, cudaGetErrorString(e));
-  const int nc = span_ctas(pre_span_kernel<F, TY>, TX * TY, smem, nbx * nby, a.L.Z, 8);
-  if (nc < 1) return fail(VG_ERR_LAUNCH, "pre_span_kernel: occupancy query failed");
+  PreGeometry<F> g;
+  if ((st = pre_geometry<F>(a.L, g))) return st;
+  constexpr int TY = PreGeometry<F>::TY, TX = PreGeometry<F>::TX;
   a.kchunk = a.L.Z;
-  pre_span_kernel<F, TY><<<nc, TX * TY, smem, as_stream(stream)>>>(a, nbx, nbx * nby);
+  // shares apply where the CTAs split the tile-levels (not one CTA per tile)
+  const long long *sh = !g.per_tile && nstarts == g.nc ? starts : nullptr;
+  pre_span_kernel<F, TY><<<g.nc, TX * TY, g.smem, as_stream(stream)>>>(a, g.nbx, g.nbx * g.nby, sh);
   return check_launch("pre_span_kernel");
 }
 
 }  // namespace
+
+// The pre kernel's tiling on this device: tiles along x, tiles in all, and
+// CTAs (as many as tiles where it runs one CTA per tile).
+template <typename F>
+int pre_span_plan(const VgDomain *dom, int *ntx, int *ntiles, int *nctas) {
+  PreGeometry<F> g;
+  const int st = pre_geometry<F>(layout_of(dom), g);
+  if (st) return st;
+  *ntx = g.nbx;
+  *ntiles = g.nbx * g.nby;
+  *nctas = g.per_tile ? 0 : g.nc;
+  return VG_OK;
+}
+template int pre_span_plan<double>(const VgDomain *, int *, int *, int *);
+template int pre_span_plan<float>(const VgDomain *, int *, int *, int *);
+
+int pre_for_step_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                     const double *salt_tau, const double *K_iso, const uint8_t *mask_bits,
+                     const VgTensorFields *out, const long long *starts, int nstarts, void *stream) {
+  return launch_pre<double>(dom, grid, set, temp_tau, salt_tau, K_iso, mask_bits, out, stream,
+                            "vg_isoneutral_step_stage_f64 (pre)", nullptr, starts, nstarts);
+}
+
+int pre_for_step_f32split(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
+                          const double *salt_tau, const float *K_iso, const uint8_t *mask_bits,
+                          const VgTensorFieldsF32 *out, const long long *starts, int nstarts, void *stream) {
+  return launch_pre<float>(dom, grid, set, temp_tau, salt_tau, K_iso, mask_bits, out, stream,
+                           "vg_isoneutral_step_stage_f32split (pre)", nullptr, starts, nstarts);
+}
 
 int pre_f64_with_slopes(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set, const double *temp_tau,
                         const double *salt_tau, const double *K_iso, const uint8_t *mask_bits,

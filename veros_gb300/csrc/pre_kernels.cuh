@@ -860,18 +860,21 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
   }
 }
 
-// Persistent form with an even share per CTA: the ntiles * Z tile-levels,
-// tile-major, are cut into gridDim.x equal ranges, and CTA c walks range c
-// as one segment per tile it touches (a segment starting above level 0 pays
-// the restart of a k-chunk). With a whole number of tiles per SM rarely
-// available, equal shares keep every SM busy to the end of the launch.
+// Persistent form: the ntiles * Z tile-levels, tile-major, are cut into
+// gridDim.x ranges, and CTA c walks range c as one segment per tile it
+// touches (a segment starting above level 0 pays the restart of a k-chunk).
+// The ranges are starts[c] .. starts[c+1] (shares weighted by the water on
+// each tile-level, span_shares.cu) or, without starts, equal counts of
+// tile-levels. With a whole number of tiles per SM rarely available, shares
+// keep every SM busy to the end of the launch.
 template <typename F, int TY>
-__global__ void __launch_bounds__(32 * TY, 16 / TY) pre_span_kernel(PreArgs<F> a, int ntx, int ntiles) {
+__global__ void __launch_bounds__(32 * TY, 16 / TY) pre_span_kernel(PreArgs<F> a, int ntx, int ntiles,
+                                                                     const long long *__restrict__ starts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int Z = a.L.Z;
   const long long W = (long long)ntiles * Z;
-  long long p = W * blockIdx.x / gridDim.x;
-  const long long end = W * (blockIdx.x + 1) / gridDim.x;
+  long long p = starts ? starts[blockIdx.x] : W * blockIdx.x / gridDim.x;
+  const long long end = starts ? starts[blockIdx.x + 1] : W * (blockIdx.x + 1) / gridDim.x;
   while (p < end) {
     const int t = (int)(p / Z), kb = (int)(p % Z);
     const int ke = (int)min((long long)Z, end - (long long)t * Z);

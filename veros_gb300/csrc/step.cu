@@ -107,20 +107,23 @@ int step_stage(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set
   }
   if (stage == 1) {
     if constexpr (sizeof(F) == sizeof(double))
-      return vg_isoneutral_pre_f64(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten, stream);
+      return pre_for_step_f64(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten,
+                              f->pre_shares, f->pre_shares_n, stream);
     else
-      return vg_isoneutral_pre_f32split(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten,
-                                        stream);
+      return pre_for_step_f32split(dom, grid, set, f->temp_tau, f->salt_tau, f->K_iso, f->mask_bits, &f->ten,
+                                   f->pre_shares, f->pre_shares_n, stream);
   }
   if (stage != 2) return fail(VG_ERR_ARG, "%s: stage %d not in 0..2", name, stage);
   TrA trT{f->temp_tau, f->temp_taup1, f->dtemp_iso, f->int_drhodT_tau, f->P_diss_iso};
   TrA trS{f->salt_tau, f->salt_taup1, f->dsalt_iso, f->int_drhodS_tau, f->P_diss_iso};
   if constexpr (sizeof(F) == sizeof(double))
     return diffusion_pair_ordered_f64(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
-                                      f->column_order, scratch, scratch_bytes, stream, 1);
+                                      f->column_order, scratch, scratch_bytes, stream, 1, f->flux_shares,
+                                      f->flux_shares_n);
   else
     return diffusion_pair_ordered_f32split(dom, grid, set, &f->ten, f->K_iso, f->mask_bits, f->kbot, &trT, &trS,
-                                           f->column_order, scratch, scratch_bytes, stream, 1);
+                                           f->column_order, scratch, scratch_bytes, stream, 1, f->flux_shares,
+                                           f->flux_shares_n);
 }
 
 }  // namespace

@@ -11,6 +11,7 @@ element size, as the tensor-memory-access engine requires). Time levels and
 tensor components are whole x-y-z blocks.
 """
 
+import ctypes
 import warnings
 import weakref
 from collections import namedtuple
@@ -304,6 +305,33 @@ class DeviceState:
                                           self._mask_bits.data_ptr(), s), "vg_pack_masks")
             self._mask_version = version
         return self._mask_bits
+
+    def step_shares(self, stream=None):
+        """Work shares of the step's pre and flux kernels for these masks on
+        this device (vg_isoneutral_step_shares): two int64 device tensors of
+        CTA starts, or None for a kernel that runs one CTA per tile. Cached
+        per mask version; only the distribution of the work depends on them."""
+        bits = self.mask_bits(stream)
+        key = (self._mask_version, self.precision, str(self.device))
+        if getattr(self, "_shares_key", None) != key:
+            lib = _capi.load()
+            dom = self.domain()
+            prec = 0 if self.precision == "f64" else 1
+            n_pre, n_flux, nbytes = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+            _capi.check(lib.vg_isoneutral_step_shares_size(dom, prec, ctypes.byref(n_pre), ctypes.byref(n_flux),
+                                                           ctypes.byref(nbytes)), "vg_isoneutral_step_shares_size")
+            mk = lambda n: torch.empty(n + 1, dtype=torch.int64, device=self.device) if n > 0 else None  # noqa: E731
+            pre, flux = mk(n_pre.value), mk(n_flux.value)
+            if pre is not None or flux is not None:
+                scratch = torch.empty(max(1, nbytes.value // 8), dtype=torch.float64, device=self.device)
+                s = stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+                ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+                _capi.check(lib.vg_isoneutral_step_shares(dom, prec, bits.data_ptr(), ptr(pre), ptr(flux),
+                                                          scratch.data_ptr(), nbytes.value, s),
+                            "vg_isoneutral_step_shares")
+            self._shares = (pre, flux)
+            self._shares_key = key
+        return self._shares
 
     def column_order(self):
         """Interior columns, as indices (i-2) + (j-2)*(X-4), deepest first

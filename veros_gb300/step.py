@@ -31,11 +31,15 @@ class IsoneutralStepper:
         dev.check_layout(("temp", "salt", "K_iso", "K_11", "K_22", "K_33", "Ai_ez", "Ai_nz", "Ai_bx", "Ai_by",
                           "dtemp_iso", "dsalt_iso", "P_diss_iso", "int_drhodT", "int_drhodS"))
         cls = _capi.VgStepFields if dev.precision == "f64" else _capi.VgStepFieldsF32
+        pre_sh, flux_sh = dev.step_shares()
+        ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        nshares = lambda t: 0 if t is None else t.numel() - 1  # noqa: E731
         return cls(
             lvl(v.temp, v.tau), lvl(v.temp, v.taup1), lvl(v.salt, v.tau), lvl(v.salt, v.taup1), v.K_iso.data_ptr(),
             dev.mask_bits().data_ptr(), v.kbot.data_ptr(), dev.tensor_fields(), v.dtemp_iso.data_ptr(),
             v.dsalt_iso.data_ptr(), lvl(v.int_drhodT, v.tau) if energy else None,
-            lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr(), dev.column_order().data_ptr())
+            lvl(v.int_drhodS, v.tau) if energy else None, v.P_diss_iso.data_ptr(), dev.column_order().data_ptr(),
+            ptr(pre_sh), ptr(flux_sh), nshares(pre_sh), nshares(flux_sh))
 
     def _fn(self, name):
         suffix = "_f64" if self.dev.precision == "f64" else "_f32split"
