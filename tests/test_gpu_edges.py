@@ -2,8 +2,9 @@
 
 The smallest domain the path accepts (one interior column, two levels), a
 domain of land only, water at full depth everywhere, a single wet column in
-land, and extents that leave partial tiles in x and y (the kernels' 32-wide
-rows and their 8- and 4-row tiles). Each: one FP64 step against one oracle
+land, extents that leave partial tiles in x and y (the kernels' 32-wide
+rows and their 8- and 4-row tiles), and 160 levels (the per-level tables,
+and the implicit solve's shared memory at half its column count). Each: one FP64 step against one oracle
 step at the 1e-12 parity bar (energy branch on and off), and one split step
 whose tracers stay within 1e-6 of the oracle's.
 """
@@ -25,7 +26,7 @@ def _edge_state(case, energy):
 
     shapes = {"minimum": (1, 1, 2, 0.0), "all_land": (20, 12, 6, 1.0), "full_depth": (40, 17, 12, 0.0),
               "single_column": (9, 9, 10, 1.0), "partial_tiles": (33, 9, 7, 0.2),
-              "partial_tiles_small": (31, 7, 3, 0.2)}
+              "partial_tiles_small": (31, 7, 3, 0.2), "deep": (36, 20, 160, 0.2)}
     nx, ny, nz, land = shapes[case]
     host = synthetic.make_state(nx, ny, nz, seed=sum(map(ord, case)), eq_of_state_type=3, land_fraction=land,
                                 dz_bottom=250.0, settings=dict(enable_conserve_energy=energy))
@@ -54,7 +55,7 @@ def _edge_state(case, energy):
     return host
 
 
-CASES = ["minimum", "all_land", "full_depth", "single_column", "partial_tiles", "partial_tiles_small"]
+CASES = ["minimum", "all_land", "full_depth", "single_column", "partial_tiles", "partial_tiles_small", "deep"]
 
 
 @pytest.mark.parametrize("energy", [False, True])
