@@ -293,7 +293,9 @@ int vg_isoneutral_step_prepare_f64(const VgDomain *dom, const VgStepFields *f, v
  * diffusion of temp and salt, whose flux kernel also prepares the interior
  * cells (each wet cell's new level and tendency written once, from tr[tau]
  * and its flux divergence, instead of a separate preparation followed by a
- * read-modify-write). */
+ * read-modify-write). Stage 2 reads the tensor stage 1 wrote for the same
+ * masks: the faces of a cell without mask bits carry zero coefficients
+ * there, and the flux kernel does not read them. */
 int vg_isoneutral_step_stage_f64(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *set,
                                  const VgStepFields *f, void *scratch, size_t scratch_bytes, int stage,
                                  void *stream);

@@ -445,6 +445,7 @@ int member_args(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings *se
       return st;
     out[p].dT.kchunk = out[p].dS.kchunk = dom->Z;
     out[p].dT.fuse_prepare = out[p].dS.fuse_prepare = 1;  // the flux stage prepares the interior
+    out[p].dT.tensor_from_pre = out[p].dS.tensor_from_pre = 1;  // the step's own tensor
     out[p].dT.col_order = out[p].dS.col_order = f.column_order;  // optional per member
     tau[2 * p] = f.temp_tau;
     tau[2 * p + 1] = f.salt_tau;

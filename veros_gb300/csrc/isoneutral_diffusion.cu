@@ -164,6 +164,7 @@ int diffusion_pair(const VgDomain *dom, const VgGrid *grid, const VgIsoSettings 
     return st;
   aT.col_order = aS.col_order = col_order;
   aT.fuse_prepare = aS.fuse_prepare = fuse_prepare;
+  aT.tensor_from_pre = aS.tensor_from_pre = fuse_prepare;  // the step's own tensor (stage 1)
   if (fuse_prepare && aT.P != aS.P)
     return fail(VG_ERR_ARG, "step diffusion: temp and salt must share P_diss_iso");
   cudaStream_t s = as_stream(stream);

@@ -539,6 +539,14 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
       unsigned mk = 0;
       if (i < L.X && j < L.Y) {
         const long long o = L.at(i, j, lev);
+        if constexpr (!kStage) {
+          // the plane two levels up, which compute_plane(lev + 1) reads as its upper
+          // neighbours: in L2 by then (the FP64 form loads T/S from global memory)
+          if (store && lev + 2 < Z) {
+            prefetch_l2(a.T + o + 2 * L.plane);
+            prefetch_l2(a.S + o + 2 * L.plane);
+          }
+        }
         // T/S at the point, its east and north neighbours and the point above:
         // from the staged ring (split form, rows aligned) or global memory
         auto trc = [&](int which, int di, int dj, int dl) -> double {
@@ -736,6 +744,13 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     if (k + 1 < Z) compute_plane(k + 1, (k + 1) & 1, true);
     // this thread's copies of plane k+3 (issued one level ago) have landed
     if (stage) cp_async_wait_all();
+    // the own point's mask on level k, from the plane copy compute_plane(k) stored (zero before the
+    // point's key, like the mask itself); read before this level's barrier, after which
+    // compute_plane(k + 2) may rewrite the buffer. The face loads of K_iso then need no global
+    // round trip for the mask first.
+    const unsigned mk = (east || north || top) ? (unsigned)sm.qm[k & 1][pc] : 0u;
+    // K_iso of the next level's faces, in L2 by then
+    if (k + 1 < Z && (east || north || top) && k + 1 - lo >= ok) prefetch_l2(a.K + L.at(i, j, k + 1));
     // plane k+1 complete; the slopes of level k published; nobody still reads the buffers rewritten next;
     // the staged plane k+3 visible
     __syncthreads();
@@ -747,8 +762,6 @@ __device__ __forceinline__ void pre_tile_body(const PreArgs<F> &a, unsigned char
     const long long o = L.at(i, j, k);
     // the face terms' grid factors in the derived-field type
     const F dzwF[2] = {zdzwF(k > 0 ? k - 1 : 0), zdzwF(k)}, qzF = zqF_(k);
-    unsigned mk = 0;
-    if ((east || north || top) && k - lo >= ok) mk = __ldg(a.m + o);  // before its key: no mask bit
 
     // east face: Ai_ez, K_11 (isoneutral.py:100-132); ip = 0 is this point, ip = 1 the east neighbour
     if (east) {

@@ -18,12 +18,13 @@
 namespace vg {
 namespace {
 
-// cost[w] = a + ceil(wet T points / 32) of tile-level w (tile-major: tile
+// cost[w] = a + ceil(wet T points / 32) of tile-level w, d if it has no wet
+// T point (tile-major: tile
 // w / Z, level w % Z); tiles of 32 x ty points from (i0s, j0s), ntx along x,
 // points limited to i < xe, j < ye. One warp per tile-level.
 __global__ void __launch_bounds__(256) tile_level_cost_kernel(Layout L, const uint8_t *__restrict__ m, int i0s,
                                                               int j0s, int xe, int ye, int ty, int ntx, long long W,
-                                                              double a, double *cost) {
+                                                              double a, double d, double *cost) {
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x & 31;
   if (w >= W) return;  // the lanes of a warp share w
@@ -36,7 +37,7 @@ __global__ void __launch_bounds__(256) tile_level_cost_kernel(Layout L, const ui
     const bool v = i < xe && j < ye && (__ldg(m + L.at(i, j, k)) & VG_MASK_T);
     wet += __popc(__ballot_sync(0xffffffffu, v));
   }
-  if (lane == 0) cost[w] = a + (double)((wet + 31) / 32);
+  if (lane == 0) cost[w] = wet ? a + (double)((wet + 31) / 32) : d;
 }
 
 // One CTA: cost[] becomes its exclusive prefix sums, then starts[c] is the
@@ -88,17 +89,26 @@ __global__ void __launch_bounds__(1024) share_partition_kernel(double *cost, lon
   }
 }
 
-// Fixed cost of a tile-level in units of one busy warp's (see the header).
-// Fixed cost of a tile-level in units of one busy warp's. The per-CTA fit
-// above puts it near 1 (pre) and 5 (flux), but a share of many dry
-// tile-levels also pays a segment restart per tile it crosses, which the
-// per-level model leaves out; measured at 1 degree (FP64 step 1.745 ms with
-// equal counts): pre 1 -> 1.00 ms, 4 -> 0.824, 8 -> 0.812 (0.850 equal);
-// flux 3 -> 1.018 ms, 5 -> 0.870, 8 -> 0.845, 10 -> 0.849 (0.887 equal): step
-// 1.676 ms. The split form's flux kernel gains nothing from shares (its
-// fixed cost per level dominates) and takes equal counts; its pre kernel
-// takes 16 (0.363 against 0.369 ms).
-constexpr double kPreFixedF64 = 8.0, kFluxFixedF64 = 8.0, kPreFixedSplit = 16.0;
+// The cost of a tile-level in units of one busy warp's: a + busy warps if it
+// holds water, d if not. The per-CTA fit of the header puts a near 1 (pre)
+// and 5 (flux), but what the shares have to balance is measured CTA time,
+// which a share of many dry tile-levels (a polar cap, the rim rows) also
+// spends on segment restarts and on the dry levels' own stores; so the
+// constants are the measured optimum at 1 degree, FP64 step in ms (CUDA
+// events, 30 steps):
+//   pre  a / d:  8 / 8 0.781,  8 / 1 0.743,  8 / 0.5 1.106,  8 / 2 0.755,
+//                6 / 1 0.755, 10 / 1 0.806 (equal counts 0.850 before the
+//                L2 prefetches)
+//   flux a / d:  8 / 8 0.775, 12 / 6 0.759, 12 / 8 0.765, 10 / 8 0.764,
+//                8 / 1 2.244, 8 / 12 0.789
+// Below the optimum of d a share takes so many dry tile-levels that it
+// becomes the longest (the flux kernel's dry tile-levels still prepare the
+// new time level of their cells). The split form's flux kernel gains nothing
+// from shares (its fixed cost per level dominates) and takes equal counts;
+// its pre kernel takes a = d = 16 (0.345 against 0.352 ms with d = 8).
+constexpr double kPreFixedF64 = 8.0, kPreDryF64 = 1.0;
+constexpr double kFluxFixedF64 = 12.0, kFluxDryF64 = 6.0;
+constexpr double kPreFixedSplit = 16.0, kPreDrySplit = 16.0;
 
 struct SharePlan {
   int n_pre, n_flux;  // CTAs with shares (0: the kernel runs one CTA per tile)
@@ -159,16 +169,17 @@ extern "C" int vg_isoneutral_step_shares(const VgDomain *dom, int precision, con
   const int ty = precision == 0 ? 8 : 4;
   struct Part {
     int n, ntx, ntiles, i0, xe_off;
-    double a;
+    double a, d;
     long long *starts;
-  } parts[2] = {{p.n_pre, p.ntx_pre, p.ntiles_pre, 1, 1, precision == 0 ? kPreFixedF64 : kPreFixedSplit, pre_starts},
-                {p.n_flux, p.ntx_flux, p.ntiles_flux, 2, 2, kFluxFixedF64, flux_starts}};
+  } parts[2] = {{p.n_pre, p.ntx_pre, p.ntiles_pre, 1, 1, precision == 0 ? kPreFixedF64 : kPreFixedSplit,
+                 precision == 0 ? kPreDryF64 : kPreDrySplit, pre_starts},
+                {p.n_flux, p.ntx_flux, p.ntiles_flux, 2, 2, kFluxFixedF64, kFluxDryF64, flux_starts}};
   for (const Part &q : parts) {
     if (q.n == 0) continue;
     const long long W = (long long)q.ntiles * L.Z;
     const long long threads = W * 32;
     tile_level_cost_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-        L, mask_bits, q.i0, q.i0, L.X - q.xe_off, L.Y - q.xe_off, ty, q.ntx, W, q.a, cost);
+        L, mask_bits, q.i0, q.i0, L.X - q.xe_off, L.Y - q.xe_off, ty, q.ntx, W, q.a, q.d, cost);
     if ((st = check_launch("tile_level_cost_kernel"))) return st;
     share_partition_kernel<<<1, 1024, 0, s>>>(cost, W, q.n, q.starts);
     if ((st = check_launch("share_partition_kernel"))) return st;
