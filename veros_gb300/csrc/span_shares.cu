@@ -103,10 +103,12 @@ __global__ void __launch_bounds__(1024) share_partition_kernel(double *cost, lon
 //                8 / 1 2.244, 8 / 12 0.789
 // Below the optimum of d a share takes so many dry tile-levels that it
 // becomes the longest (the flux kernel's dry tile-levels still prepare the
-// new time level of their cells). The split form's flux kernel gains nothing
+// new time level of their cells). With the pre kernel's rotated plane
+// points: a / d = 8 / 1 0.704, 8 / 2 0.704, 6 / 1 0.706, 10 / 1 0.800,
+// 12 / 1 0.888 ms; 8 / 2 keeps the ratio well below where the cliff starts. The split form's flux kernel gains nothing
 // from shares (its fixed cost per level dominates) and takes equal counts;
 // its pre kernel takes a = d = 16 (0.345 against 0.352 ms with d = 8).
-constexpr double kPreFixedF64 = 8.0, kPreDryF64 = 1.0;
+constexpr double kPreFixedF64 = 8.0, kPreDryF64 = 2.0;
 constexpr double kFluxFixedF64 = 12.0, kFluxDryF64 = 6.0;
 constexpr double kPreFixedSplit = 16.0, kPreDrySplit = 16.0;
 
