@@ -510,7 +510,8 @@ def test_energy_branch_per_tracer_calls_match_fused_step(precision):
 def test_host_buffer_step_matches_device_step(precision):
     """step_host (reference-layout host buffers, layout conversion on the
     device) gives the device step's fields bit for bit, on a domain whose X
-    and Z are not multiples of the 32-wide conversion tiles."""
+    and Z are not multiples of the 32-wide conversion tiles and whose Y (25)
+    leaves a partial group of the conversion's four rows per CTA."""
     from veros_gb300 import synthetic
     from veros_gb300.state import DeviceState
     from veros_gb300.step import IsoneutralStepper
