@@ -420,9 +420,15 @@ def test_weighted_shares_change_no_result(precision):
     b = IsoneutralStepper(DeviceState.from_host(host, precision=precision))
     pre, flux = a.dev.step_shares()
     assert pre is not None and (flux is not None) == (precision == "f64")  # the split flux kernel: equal counts
-    for starts in (pre,) + ((flux,) if flux is not None else ()):
+    X, Y, Z = a.dev.X, a.dev.Y, a.dev.Z
+    ty = 8 if precision == "f64" else 4  # the kernels' tile rows (32 columns wide)
+    ntiles = {"pre": -(-(X - 3) // 32) * -(-(Y - 3) // ty), "flux": -(-(X - 4) // 32) * -(-(Y - 4) // ty)}
+    for name, starts in (("pre", pre), ("flux", flux)):
+        if starts is None:
+            continue
         s = starts.cpu().numpy()
-        assert s[0] == 0 and np.all(np.diff(s) >= 0) and s[-1] % host.nz == 0
+        # every tile-level once, in order: CTA c takes [s[c], s[c+1])
+        assert s[0] == 0 and np.all(np.diff(s) >= 0) and s[-1] == ntiles[name] * Z, name
     b.dev.step_shares = lambda stream=None: (None, None)
     a.step(2)
     b.step(2)
